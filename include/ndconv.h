@@ -1,0 +1,155 @@
+/*
+ * ndconv -- C ABI of the GB300 (sm_103a) convolution library.
+ *
+ * Drop-in boundary for the convolution hot path of the ndarray-conv crate
+ * (v0.6.1).  Every entry point names the reference interface it replaces.
+ * Plain pointers and sizes only: device pointers for data, kernel and
+ * output; `stream` is a cudaStream_t passed as void* (NULL = legacy default
+ * stream).  All calls are asynchronous on `stream` unless stated.
+ *
+ * Arrays are row-major N-d views (N = rank, 1..3) with ELEMENT strides
+ * (0 in every slot = contiguous).  Complex elements are interleaved re, im.
+ * Outputs are always written contiguous row-major.
+ *
+ * Status codes mirror the reference's Result<_, Error<N>>
+ * (src/lib.rs:148-159); the reference's panics become
+ * NDCONV_ERR_PAD_OUT_OF_RANGE.
+ */
+#ifndef NDCONV_H
+#define NDCONV_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NDCONV_MAX_RANK 3
+
+/* element type (InElem / T of the reference traits) */
+typedef enum {
+    NDCONV_F32 = 0,
+    NDCONV_F64 = 1,
+    NDCONV_I32 = 2, /* direct conv only, wrapping arithmetic (release-mode Rust) */
+    NDCONV_C32 = 3, /* num_complex::Complex<f32> */
+    NDCONV_C64 = 4
+} ndconv_dtype;
+
+typedef enum {
+    NDCONV_OK = 0,
+    NDCONV_ERR_DATA_SHAPE = 1,      /* Error::DataShape (also zero-size kernel on the FFT path, src/conv_fft/mod.rs:211-212) */
+    NDCONV_ERR_KERNEL_SHAPE = 2,    /* Error::KernelShape (direct path, src/conv/mod.rs:142-144) */
+    NDCONV_ERR_MISMATCH_SHAPE = 3,  /* Error::MismatchShape (src/conv/mod.rs:152-158, src/conv_fft/mod.rs:220-227) */
+    NDCONV_ERR_PAD_OUT_OF_RANGE = 4,/* the reference panics: reflect index out of range (src/padding/half_dim.rs:192-210,233-258) */
+    NDCONV_ERR_UNSUPPORTED = 5,     /* e.g. integer FFT (documented broken upstream, src/conv_fft/processor/mod.rs:46-59) */
+    NDCONV_ERR_INVALID = 6,         /* bad argument (rank, zero stride/dilation, null pointer) */
+    NDCONV_ERR_CUDA = 7,
+    NDCONV_ERR_TIMEOUT = 8,         /* a bounded device-side wait ran out */
+    NDCONV_ERR_NO_MEMORY = 9
+} ndconv_status;
+
+/* ConvMode<N> (src/lib.rs:81-105) */
+typedef enum {
+    NDCONV_MODE_FULL = 0,
+    NDCONV_MODE_SAME = 1,
+    NDCONV_MODE_VALID = 2,
+    NDCONV_MODE_CUSTOM = 3,   /* padding[i][0] on both sides, strides[i] */
+    NDCONV_MODE_EXPLICIT = 4  /* padding[i][0..2], strides[i] */
+} ndconv_conv_mode;
+
+/* BorderType<T> (src/lib.rs:131-143) */
+typedef enum {
+    NDCONV_BORDER_ZEROS = 0,
+    NDCONV_BORDER_CONST = 1,
+    NDCONV_BORDER_REFLECT = 2,
+    NDCONV_BORDER_REPLICATE = 3,
+    NDCONV_BORDER_CIRCULAR = 4
+} ndconv_border;
+
+/* PaddingMode<N, T> (src/lib.rs:111-127) */
+typedef enum {
+    NDCONV_PAD_ZEROS = 0,
+    NDCONV_PAD_CONST = 1,
+    NDCONV_PAD_REFLECT = 2,
+    NDCONV_PAD_REPLICATE = 3,
+    NDCONV_PAD_CIRCULAR = 4,
+    NDCONV_PAD_CUSTOM = 5,    /* border_kind[i][0] per axis, both sides */
+    NDCONV_PAD_EXPLICIT = 6   /* border_kind[i][0] front, [i][1] back */
+} ndconv_padding_mode;
+
+/*
+ * One convolution problem: data view, kernel view with dilation and the
+ * reverse flag (KernelWithDilation, src/dilation/mod.rs:8-12), ConvMode and
+ * PaddingMode.
+ */
+typedef struct ndconv_problem {
+    int32_t dtype;                 /* ndconv_dtype */
+    int32_t rank;                  /* 1..3 */
+    int64_t data_shape[3];
+    int64_t kernel_shape[3];
+    int64_t dilation[3];           /* >= 1 (with_dilation, src/dilation/mod.rs:103-126) */
+    int32_t reverse;               /* 1 = convolution (default), 0 = no_reverse() */
+    int32_t conv_mode;             /* ndconv_conv_mode */
+    int64_t mode_padding[3][2];
+    int64_t mode_strides[3];
+    int32_t padding_mode;          /* ndconv_padding_mode */
+    int32_t border_kind[3][2];     /* ndconv_border */
+    double border_value[3][2][2];  /* BorderType::Const(c): (re, im) per axis and side */
+    double const_value[2];         /* PaddingMode::Const(c): (re, im) */
+    int64_t data_strides[3];       /* element strides, all 0 = contiguous */
+    int64_t kernel_strides[3];     /* element strides, all 0 = contiguous */
+} ndconv_problem;
+
+typedef struct ndconv_fft_processor ndconv_fft_processor;
+
+/* Output shape and argument checks, host only (no device work).
+ * algo: 0 = direct (ConvExt::conv), 1 = FFT (ConvFFTExt::conv_fft); the two
+ * paths report zero-size kernels and padding panics in the reference's
+ * different orders. */
+int ndconv_output_shape(const ndconv_problem *p, int32_t algo, int64_t out_shape[3]);
+
+/* ConvExt::conv (src/conv/mod.rs:78-116, impl :128-200).
+ * data, kernel: device pointers to p->dtype elements; out: device pointer
+ * with room for the contiguous output (ndconv_output_shape). */
+int ndconv_conv(const ndconv_problem *p, const void *data, const void *kernel, void *out,
+                void *stream);
+
+/* ConvFFTExt::conv_fft / conv_fft_with_processor / conv_fft_par
+ * (src/conv_fft/mod.rs:81-183, impl :185-292, :394-423).
+ * proc may be NULL (fresh-processor semantics); with a processor the
+ * workspace, twiddle tables and a cached kernel spectrum are reused.
+ * dtype F32, F64, C32, C64. */
+int ndconv_conv_fft(const ndconv_problem *p, const void *data, const void *kernel, void *out,
+                    ndconv_fft_processor *proc, void *stream);
+
+/* GetProcessor::get_processor / get_fft_processor::<T, InElem>()
+ * (src/conv_fft/processor/mod.rs:71-73,125-143; src/lib.rs:75-77).
+ * dtype F32/F64 selects the real processor (real.rs), C32/C64 the complex
+ * one (complex.rs). */
+int ndconv_fft_processor_create(int32_t dtype, ndconv_fft_processor **out);
+int ndconv_fft_processor_destroy(ndconv_fft_processor *proc);
+
+/* Processor::forward (src/conv_fft/processor/mod.rs:79-100; real.rs:24-155,
+ * complex.rs:119-128).  Output layout is the reference's: axes rotated right
+ * after each pass; out_shape receives it (query with out == NULL). */
+int ndconv_fft_forward(ndconv_fft_processor *proc, int32_t rank, const int64_t shape[3],
+                       const void *in, void *out, int64_t out_shape[3], void *stream);
+
+/* Processor::backward (processor/mod.rs:102-119; real.rs:157-281,
+ * complex.rs:131-144): inverse of forward, divided by the element count.
+ * The real processor uses the last-axis length remembered by its last
+ * forward call, like the reference's rp_origin_len. */
+int ndconv_fft_backward(ndconv_fft_processor *proc, int32_t rank, const int64_t shape[3],
+                        const void *in, void *out, int64_t out_shape[3], void *stream);
+
+/* Message for the last non-OK status returned on this thread. */
+const char *ndconv_last_error(void);
+
+/* Library version string. */
+const char *ndconv_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NDCONV_H */

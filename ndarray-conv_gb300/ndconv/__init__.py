@@ -1,0 +1,7 @@
+"""ndconv: GB300 (sm_103a) drop-in for the ndarray-conv convolution hot path.
+
+Python mirror of the crate's API over the C ABI in include/ndconv.h.
+"""
+from .api import (BorderType, ConvError, ConvMode, DataShape, KernelShape,  # noqa: F401
+                  KernelWithDilation, MismatchShape, PaddingMode, PaddingOutOfRange,
+                  Unsupported, build_problem, no_reverse, reverse, with_dilation)
