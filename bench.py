@@ -1,0 +1,334 @@
+"""Benchmark: convolution GB/s and % of HBM roofline on one GB300.
+
+Workload (config 2 of the reference's benchmark set, batched): B
+independent instances of a 2-D f32 convolution x[200, 5000] with a kernel
+[11, 31] dilated by 2, ConvMode::Same, PaddingMode::Custom([Reflect,
+Circular]); every instance has its own seeded Uniform[0,1) data and kernel.
+A step is one pass of conv_fft (default) or conv over all B instances.
+B = 64 makes the inputs (256 MB) larger than L2, so no flush is needed.
+
+Metric: algorithmic bytes 4 * (|x| + |k| + |y|) per instance / time.
+  value   device-resident inputs, CUDA-event timed (max over ranks)
+  e2e     the same calls with pinned-host inputs: H2D copy + conv + D2H of
+          the outputs inside the timed region
+Reference arm (--impl reference): the oracle port of conv_fft_par (same
+algorithm as the crate, rayon-style threads on all host cores) on a
+bounded sample of the same workload.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path[:0] = [ROOT, os.path.join(ROOT, "ndarray-conv_gb300")]
+
+import numpy as np  # noqa: E402
+
+SHAPE_X = (200, 5000)
+SHAPE_K = (11, 31)
+DIL = 2
+
+
+def algorithmic_bytes(out_shape):
+    return 4 * (np.prod(SHAPE_X) + np.prod(SHAPE_K) + np.prod(out_shape))
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def problem_args():
+    import ndconv
+    from ndconv import BorderType, ConvMode, PaddingMode
+    return ConvMode.Same, PaddingMode.Custom([BorderType.Reflect, BorderType.Circular]), ndconv
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(seconds=10.0, nthreads=None):
+    """The oracle port of conv_fft_par on the host cores, one instance per
+    call, repeated for ~`seconds`.  Returns (GB/s, cores, sample text)."""
+    from oracle import oracle as O
+    from ndconv import _abi, build_problem, with_dilation
+    mode, pm, _ = problem_args()
+    nthreads = nthreads or os.cpu_count() or 1
+    rng = np.random.default_rng(12345)
+    x = rng.random(SHAPE_X).astype(np.float32)
+    k = rng.random(SHAPE_K).astype(np.float32)
+    p = build_problem(_abi.F32, SHAPE_X, with_dilation(k, DIL), mode, pm)
+    st, y = O.conv_fft(p, x, k, nthreads)  # warm-up
+    assert st == 0
+    n, t0 = 0, time.perf_counter()
+    while True:
+        O.conv_fft(p, x, k, nthreads)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    gbs = algorithmic_bytes(y.shape) * n / el / 1e9
+    return gbs, nthreads, f"{n} instances of x[200,5000]*k[11,31] (conv_fft_par port, f32) in {el:.1f} s"
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    steps, warm = args.steps, args.warmup
+    # each step: a bounded sample (`per_step_s` of CPU work) of the workload
+    from oracle import oracle as O
+    from ndconv import _abi, build_problem, with_dilation
+    mode, pm, _ = problem_args()
+    nth = os.cpu_count() or 1
+    rng = np.random.default_rng(12345)
+    x = rng.random(SHAPE_X).astype(np.float32)
+    k = rng.random(SHAPE_K).astype(np.float32)
+    p = build_problem(_abi.F32, SHAPE_X, with_dilation(k, DIL), mode, pm)
+    for _ in range(max(1, warm)):
+        st, y = O.conv_fft(p, x, k, nth)
+    per_step = max(1, int(args.ref_instances))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for _ in range(per_step):
+            O.conv_fft(p, x, k, nth)
+    el = time.perf_counter() - t0
+    gbs = algorithmic_bytes(y.shape) * per_step * steps / el / 1e9
+    sample = f"{per_step} instance(s) of x[200,5000]*k[11,31] per step (conv_fft_par port, f32)"
+    line = {"metric": "conv GB/s (algorithmic bytes 4*(|x|+|k|+|y|)), conv_fft x[200,5000]*k[11,31] dil 2",
+            "value": gbs, "unit": "GB/s", "n_gpus": world, "steps": steps, "warmup": warm,
+            "ms_per_step": el / steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Uniform[0,1))",
+            "impl": "reference",
+            "config": {"workload": "config2: 2-D f32 x[200,5000] * k[11,31] dilation 2, Same, "
+                                   "Custom([Reflect, Circular]); conv_fft"},
+            "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": nth, "kind": "port", "sample": sample},
+            "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--algo", default="fft", choices=["fft", "direct"])
+    ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ref-instances", type=int, default=4)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        import __graft_entry__  # noqa: F401  (paths)
+        from oracle import oracle as O
+        O.build()
+        return run_reference(args, rank, world)
+
+    import torch
+    import __graft_entry__ as g
+    g.build()
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    mode, pm, ndconv = problem_args()
+    from ndconv import _abi, build_problem, with_dilation
+    L = _abi.lib()
+
+    B = args.batch
+    gen = torch.Generator(device="cuda").manual_seed(1000 + rank)
+    xs = [torch.rand(SHAPE_X, generator=gen, device="cuda") for _ in range(B)]
+    ks = [torch.rand(SHAPE_K, generator=gen, device="cuda") for _ in range(B)]
+    p = build_problem(_abi.F32, SHAPE_X, with_dilation(ks[0], DIL), mode, pm)
+    osh = (ctypes.c_int64 * 3)()
+    algo = 1 if args.algo == "fft" else 0
+    st = L.ndconv_output_shape(ctypes.byref(p), algo, osh)
+    assert st == 0, _abi.last_error()
+    out_shape = (osh[0], osh[1])
+    ys = [torch.empty(out_shape, device="cuda") for _ in range(B)]
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    proc = ndconv.get_fft_processor(torch.float32)
+    pp = ctypes.byref(p)
+
+    def step(xl, kl, yl):
+        for i in range(B):
+            if algo == 1:
+                s = L.ndconv_conv_fft(pp, ctypes.c_void_p(xl[i].data_ptr()), ctypes.c_void_p(kl[i].data_ptr()),
+                                      ctypes.c_void_p(yl[i].data_ptr()), proc._handle, sp)
+            else:
+                s = L.ndconv_conv(pp, ctypes.c_void_p(xl[i].data_ptr()), ctypes.c_void_p(kl[i].data_ptr()),
+                                  ctypes.c_void_p(yl[i].data_ptr()), sp)
+            if s:
+                raise RuntimeError(_abi.last_error())
+
+    for _ in range(args.warmup):
+        step(xs, ks, ys)
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    barrier()
+    n0 = L.ndconv_kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step(xs, ks, ys)
+        e1.record(stream)
+        barrier()
+    launches = L.ndconv_kernel_launches() - n0
+    ms = e0.elapsed_time(e1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    bytes_step = algorithmic_bytes(out_shape) * B
+    value = bytes_step * world / (ms * 1e-3) / 1e9
+    per_launch_ms = ms / B  # one instance's convolution
+    peak, peak_kind = peaks()
+    achieved = algorithmic_bytes(out_shape) / (per_launch_ms * 1e-3) / 1e9
+
+    # ---- end to end: pinned host inputs, H2D + conv + D2H per step
+    hx = [x.cpu().pin_memory() for x in xs]
+    hk = [k.cpu().pin_memory() for k in ks]
+    hy = [torch.empty(out_shape).pin_memory() for _ in range(B)]
+    dx = [torch.empty_like(x) for x in xs]
+    dk = [torch.empty_like(k) for k in ks]
+
+    def e2e_step():
+        for i in range(B):
+            dx[i].copy_(hx[i], non_blocking=True)
+            dk[i].copy_(hk[i], non_blocking=True)
+        step(dx, dk, ys)
+        for i in range(B):
+            hy[i].copy_(ys[i], non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    barrier()
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    if dist:
+        t = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    h2d = 4 * (np.prod(SHAPE_X) + np.prod(SHAPE_K)) * B
+    d2h = 4 * int(np.prod(out_shape)) * B
+
+    # ---- parity spot check on instance 0 against the f64 oracle
+    from oracle import oracle as O
+    x0, k0 = xs[0].cpu().numpy(), ks[0].cpu().numpy()
+    p64 = build_problem(_abi.F64, SHAPE_X, with_dilation(k0, DIL), mode, pm)
+    stt, y64 = O.conv(p64, x0.astype(np.float64), k0.astype(np.float64))
+    y0 = ys[0].cpu().numpy().astype(np.float64)
+    err = float(np.linalg.norm(y0 - y64) / np.linalg.norm(y64)) if stt == 0 else None
+
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            gbs, cores, sample = cpu_baseline(args.cpu_seconds)
+            cpu = {"value": gbs, "unit": "GB/s", "cores": cores, "kind": "port", "sample": sample}
+        line = {
+            "metric": "conv GB/s (algorithmic bytes 4*(|x|+|k|+|y|)), conv_fft x[200,5000]*k[11,31] dil 2",
+            "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded Uniform[0,1), distinct data and kernel per instance)",
+            "config": {"workload": f"config2 x{B}: 2-D f32 x[200,5000] * k[11,31] dilation 2, Same, "
+                                   f"Custom([Reflect, Circular]); {'conv_fft' if algo else 'conv'} per instance",
+                       "batch_per_gpu": B, "algo": args.algo,
+                       "l2": "inputs (256 MB per GPU) larger than L2, no flush"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "kernel": "one instance's convolution (all its launches)",
+                         "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": bytes_step * world / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s",
+                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+            "normwise_err_vs_f64": err,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -142,6 +142,10 @@ int ndconv_fft_forward(ndconv_fft_processor *proc, int32_t rank, const int64_t s
 int ndconv_fft_backward(ndconv_fft_processor *proc, int32_t rank, const int64_t shape[3],
                         const void *in, void *out, int64_t out_shape[3], void *stream);
 
+/* Number of CUDA kernels this library has launched in this process.
+ * Diagnostics only; no counterpart in the reference. */
+uint64_t ndconv_kernel_launches(void);
+
 /* Message for the last non-OK status returned on this thread. */
 const char *ndconv_last_error(void);
 

@@ -1,0 +1,23 @@
+// Direct convolution launcher (ConvExt::conv on the GPU).
+#pragma once
+#include "common.cuh"
+
+namespace ndconv {
+
+template <typename T> struct DirectParams {
+    Geom3<T> g;
+    int reverse;
+    // tiling, filled by the launcher
+    int64_t cky, ckx;        // kernel rows / columns per staged chunk
+    int64_t max_rows, max_cols;
+    int64_t tile_elems, w_elems;
+    int64_t maps_off;        // byte offset of the int64 border maps in shared memory
+};
+
+// x, k: device pointers (strided per g.ax[i].xs / ks); y: contiguous output.
+// force_naive selects the unstaged kernel (tests use it as a second path).
+template <typename T>
+cudaError_t direct_conv_launch(const T *x, const T *k, T *y, DirectParams<T> P, cudaStream_t st,
+                               int force_naive);
+
+}  // namespace ndconv

@@ -1,0 +1,998 @@
+// FFT convolution (ConvFFTExt::conv_fft, src/conv_fft/mod.rs:185-292) and
+// the FFT processor (src/conv_fft/processor/{real,complex}.rs) on sm_103a.
+//
+// conv_fft on the canonical 3-axis geometry (axis 2 contiguous):
+//   kernel spectrum Kh[F0][F1][H]: row pass over the dilated (optionally
+//     flipped) kernel buffer, then column passes over axes 1 and 0;
+//   data: row pass (padding evaluated in the load through the border map,
+//     zero beyond the padded extent) -> S[P0][F1][H];
+//   column pass on axis 1 (3-D only);
+//   fused pass on the first non-trivial axis: forward FFT, multiply by Kh,
+//     inverse FFT, keep only the rows the crop/stride selects;
+//   inverse column pass on axis 1 keeping cropped rows (3-D only);
+//   inverse row pass: c2r, scale 1 / prod(F), crop [k_eff-1, pds) step s,
+//     write the contiguous output.
+// For rank 1 the whole convolution is one fused row kernel.  FFT lengths
+// are the smallest 2^a 3^b 5^c 7^d >= pds (even on the real axis): any
+// length >= pds gives the same cropped result as the reference's good_size
+// (the circular wrap only touches indices < k_eff - 1).
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+#include "fft.h"
+#include "fft_core.cuh"
+
+namespace ndconv {
+
+// ------------------------------------------------------------- twiddles --
+template <typename C>
+__global__ void gen_twiddles_kernel(C *tw, int L) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < L; t += gridDim.x * blockDim.x) {
+        double s, c;
+        sincospi(-2.0 * (double)t / (double)L, &s, &c);  // exp(-2 pi i t / L) in FP64
+        tw[t].re = (decltype(tw[t].re))c;
+        tw[t].im = (decltype(tw[t].im))s;
+    }
+}
+
+namespace {
+std::mutex g_tw_mu;
+std::map<std::tuple<int, int, int>, void *> g_tw;  // (device, bytes-per-complex, L) -> table
+
+template <typename C> int get_twiddles(int L, const C **out) {
+    int dev = 0;
+    NDCONV_CUDA_OK(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_tw_mu);
+    auto key = std::make_tuple(dev, (int)sizeof(C), L);
+    auto it = g_tw.find(key);
+    if (it != g_tw.end()) {
+        *out = (const C *)it->second;
+        return NDCONV_OK;
+    }
+    void *p = nullptr;
+    NDCONV_CUDA_OK(cudaMalloc(&p, sizeof(C) * (size_t)(L > 0 ? L : 1)));
+    cudaStream_t s;
+    NDCONV_CUDA_OK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    int blocks = (L + 255) / 256;
+    if (blocks > 1024) blocks = 1024;
+    if (blocks < 1) blocks = 1;
+    gen_twiddles_kernel<C><<<blocks, 256, 0, s>>>((C *)p, L);
+    ndconv_count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    if (e != cudaSuccess) {
+        cudaFree(p);
+        return ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e));
+    }
+    g_tw[key] = p;
+    *out = (const C *)p;
+    return NDCONV_OK;
+}
+}  // namespace
+
+// Radix factorisation: 8s, 4, 2, 3s, 5s, then other primes (generic
+// butterfly up to kMaxGenericRadix).  Returns false if a prime factor is
+// larger than that.
+bool make_plan(int L, FftPlanDev &pl) {
+    pl.L = L;
+    pl.nst = 0;
+    int r = L;
+    while (r % 8 == 0) { pl.rad[pl.nst++] = 8; r /= 8; }
+    if (r % 4 == 0) { pl.rad[pl.nst++] = 4; r /= 4; }
+    if (r % 2 == 0) { pl.rad[pl.nst++] = 2; r /= 2; }
+    for (int f = 3; r > 1; f += 2) {
+        while (r % f == 0) {
+            if (f > kMaxGenericRadix || pl.nst >= kMaxStages) return false;
+            pl.rad[pl.nst++] = f;
+            r /= f;
+        }
+        if ((int64_t)f * f > r && r > 1) {
+            if (r > kMaxGenericRadix || pl.nst >= kMaxStages) return false;
+            pl.rad[pl.nst++] = r;
+            r = 1;
+        }
+    }
+    return true;
+}
+
+int64_t smooth_size(int64_t n, bool even) {
+    // smallest 2^a 3^b 5^c 7^d >= n (and even when asked)
+    if (n <= 1) return even ? 2 : 1;
+    int64_t best = INT64_MAX;
+    for (int64_t p7 = 1; p7 < 2 * n + 8; p7 *= 7)
+        for (int64_t p5 = p7; p5 < 2 * n + 8; p5 *= 5)
+            for (int64_t p3 = p5; p3 < 2 * n + 8; p3 *= 3) {
+                int64_t v = p3;
+                while (v < n || (even && (v & 1))) v *= 2;
+                if (v < best) best = v;
+            }
+    return best;
+}
+
+// ------------------------------------------------------------- row pass --
+enum RowMode : int {
+    ROW_FWD_DATA = 0,    // padded data row -> spectrum row
+    ROW_FWD_KERNEL = 1,  // dilated kernel buffer row -> spectrum row
+    ROW_INV_OUT = 2,     // spectrum row -> scaled, cropped output row
+    ROW_FUSED = 3,       // rank 1: data row -> fwd -> * Kh -> inv -> cropped output
+    ROW_FWD_PLAIN = 4,   // contiguous input row -> spectrum row (processor API)
+    ROW_INV_PLAIN = 5,   // spectrum row -> scaled contiguous output row (processor API)
+};
+enum RowKind : int { RK_COMPLEX = 0, RK_REAL_EVEN = 1, RK_REAL_ODD = 2 };
+
+template <typename T> struct RowArgs {
+    using C = typename CplxT<typename Elem<T>::Real>::type;
+    using R = typename Elem<T>::Real;
+    int mode, kind;
+    int64_t F;           // samples per row (real or complex)
+    int64_t H;           // spectrum bins per row
+    int64_t n_rows, n1;  // row r -> (r / n1, r % n1)
+    int64_t spec_s0, spec_s1;
+    C *spec;
+    const C *kspec;
+    const T *x;
+    Geom3<T> g;
+    const T *k;
+    int reverse;
+    T *y;
+    int64_t y_s0, y_s1, out_n, crop_off, crop_step;
+    const T *pin;
+    T *pout;
+    FftPlanDev pl;   // length M = F/2 (real even) or F
+    const C *tw;     // table for pl.L
+    const C *twF;    // table for F (real even)
+    R scale;
+    int nb, lognb;
+};
+
+// kernel-buffer value at padded position j of one axis: tap index or -1
+// (src/conv_fft/padding.rs:78-111: k[i] at i*d, or at k_eff-1-i*d when !reverse)
+__device__ __forceinline__ int64_t kbuf_tap(const AxisGeom &a, int64_t j, int reverse) {
+    const int64_t q = reverse ? j : (a.keff - 1 - j);
+    if (q < 0 || q >= a.keff || q % a.d) return -1;
+    return q / a.d;
+}
+
+template <typename T> struct RealPart {
+    __device__ static typename Elem<T>::Real re(T v) { return v; }
+    __device__ static typename Elem<T>::Real im(T) { return 0; }
+};
+template <> struct RealPart<c32> {
+    __device__ static float re(c32 v) { return v.re; }
+    __device__ static float im(c32 v) { return v.im; }
+};
+template <> struct RealPart<c64> {
+    __device__ static double re(c64 v) { return v.re; }
+    __device__ static double im(c64 v) { return v.im; }
+};
+
+template <typename T> __device__ __forceinline__ T make_elem(typename Elem<T>::Real re, typename Elem<T>::Real im) {
+    if constexpr (Elem<T>::kComplex) return T{re, im};
+    else return (T)re;
+}
+
+// sample j of row (i0, i1) for the forward loads
+template <typename T>
+__device__ __forceinline__ T row_sample(const RowArgs<T> &A, int64_t m0, int64_t m1, int64_t t0, int64_t t1,
+                                        int64_t row, int64_t j) {
+    if (A.mode == ROW_FWD_PLAIN) return A.pin[row * A.F + j];
+    if (A.mode == ROW_FWD_KERNEL) {
+        if (t0 < 0 || t1 < 0) return Elem<T>::zero();
+        const int64_t t2 = kbuf_tap(A.g.ax[2], j, A.reverse);
+        if (t2 < 0) return Elem<T>::zero();
+        return A.k[t0 * A.g.ax[0].ks + t1 * A.g.ax[1].ks + t2 * A.g.ax[2].ks];
+    }
+    // data (FWD_DATA / FUSED): zero beyond the padded extent
+    if (j >= A.g.ax[2].L) return Elem<T>::zero();
+    return resolve_padded<T>(A.x, A.g, m0, m1, axis_map(A.g.ax[2], j));
+}
+
+// r2c post-processing: X[k] (k = 0..M) from Z = FFT_M(x[2m] + i x[2m+1])
+template <typename C>
+__device__ void r2c_post(const C *Z, C *X, int64_t M, int nb, int lognb, const C *__restrict__ twF) {
+    using R = decltype(Z[0].re);
+    const int64_t total = (M + 1) << lognb;
+    for (int64_t u = threadIdx.x; u < total; u += blockDim.x) {
+        const int b = (int)(u & (nb - 1));
+        const int64_t k = u >> lognb;
+        const C a = Z[(k == M ? 0 : k) * nb + b];
+        const C c = cconj(Z[(k == 0 ? 0 : M - k) * nb + b]);
+        const C e = C{(R)0.5 * (a.re + c.re), (R)0.5 * (a.im + c.im)};
+        const C d = C{(R)0.5 * (a.re - c.re), (R)0.5 * (a.im - c.im)};
+        const C o = C{d.im, -d.re};  // -i * d
+        const C w = twF[k];
+        const C wo = cmul(w, o);
+        X[k * nb + b] = C{e.re + wo.re, e.im + wo.im};
+    }
+}
+
+// c2r pre-processing: Z[k] (k < M) such that IFFT_M(Z)[j] = x[2j] + i x[2j+1]
+// for the unnormalised length-2M inverse of the Hermitian spectrum X[0..M]
+// (imaginary parts of the DC and Nyquist bins ignored).
+template <typename C>
+__device__ void c2r_pre(const C *X, C *Z, int64_t M, int nb, int lognb, const C *__restrict__ twF) {
+    const int64_t total = M << lognb;
+    for (int64_t u = threadIdx.x; u < total; u += blockDim.x) {
+        const int b = (int)(u & (nb - 1));
+        const int64_t k = u >> lognb;
+        C a = X[k * nb + b], c = X[(M - k) * nb + b];
+        if (k == 0) {
+            a.im = 0;
+            c.im = 0;
+        }
+        c = cconj(c);
+        const C e = cadd(a, c);
+        const C d = csub(a, c);
+        const C o = cmul(d, cconj(twF[k]));
+        Z[k * nb + b] = C{e.re - o.im, e.im + o.re};  // e + i*o
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) row_kernel(RowArgs<T> A) {
+    using C = typename RowArgs<T>::C;
+    using R = typename RowArgs<T>::R;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nb = A.nb, lognb = A.lognb;
+    const int64_t M = A.pl.L;  // transform length
+    const int64_t cap = (A.kind == RK_REAL_EVEN ? M + 1 : M) * nb;
+    C *buf0 = reinterpret_cast<C *>(smem_raw);
+    C *buf1 = buf0 + cap;
+    int64_t *rinfo = reinterpret_cast<int64_t *>(buf1 + cap);  // per row: m0, m1, t0, t1, i0, i1
+    const int64_t rbase = (int64_t)blockIdx.x * nb;
+
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+        const int64_t r = rbase + b;
+        const int64_t i0 = r / A.n1, i1 = r % A.n1;
+        int64_t *ri = rinfo + 6 * b;
+        ri[4] = i0;
+        ri[5] = i1;
+        if (A.mode == ROW_FWD_DATA || A.mode == ROW_FUSED) {
+            ri[0] = axis_map(A.g.ax[0], i0);
+            ri[1] = axis_map(A.g.ax[1], i1);
+        } else if (A.mode == ROW_FWD_KERNEL) {
+            ri[2] = kbuf_tap(A.g.ax[0], i0, A.reverse);
+            ri[3] = kbuf_tap(A.g.ax[1], i1, A.reverse);
+        }
+    }
+    __syncthreads();
+
+    const bool fwd = (A.mode == ROW_FWD_DATA || A.mode == ROW_FWD_KERNEL || A.mode == ROW_FUSED ||
+                      A.mode == ROW_FWD_PLAIN);
+    C *res;
+    if (fwd) {
+        // ---- load samples
+        const int64_t total = M << lognb;
+        for (int64_t u = threadIdx.x; u < total; u += blockDim.x) {
+            const int b = (int)(u / M);
+            const int64_t i = u - (int64_t)b * M;
+            const int64_t r = rbase + b;
+            C v = C{0, 0};
+            if (r < A.n_rows) {
+                const int64_t *ri = rinfo + 6 * b;
+                if (A.kind == RK_REAL_EVEN) {
+                    const T s0 = row_sample(A, ri[0], ri[1], ri[2], ri[3], r, 2 * i);
+                    const T s1 = row_sample(A, ri[0], ri[1], ri[2], ri[3], r, 2 * i + 1);
+                    v = C{RealPart<T>::re(s0), RealPart<T>::re(s1)};
+                } else {
+                    const T s = row_sample(A, ri[0], ri[1], ri[2], ri[3], r, i);
+                    v = C{RealPart<T>::re(s), RealPart<T>::im(s)};
+                }
+            }
+            buf0[i * nb + b] = v;
+        }
+        __syncthreads();
+        res = block_fft<false>(buf0, buf1, nb, lognb, A.pl, A.tw);
+        C *other = (res == buf0) ? buf1 : buf0;
+        if (A.kind == RK_REAL_EVEN) {
+            r2c_post(res, other, M, nb, lognb, A.twF);
+            __syncthreads();
+            C *t = res;
+            res = other;
+            other = t;
+        }
+        if (A.mode != ROW_FUSED) {
+            // store H bins per row
+            const int64_t tot = A.H << lognb;
+            for (int64_t u = threadIdx.x; u < tot; u += blockDim.x) {
+                const int b = (int)(u / A.H);
+                const int64_t k = u - (int64_t)b * A.H;
+                const int64_t r = rbase + b;
+                if (r >= A.n_rows) continue;
+                const int64_t *ri = rinfo + 6 * b;
+                A.spec[ri[4] * A.spec_s0 + ri[5] * A.spec_s1 + k] = res[k * nb + b];
+            }
+            return;
+        }
+        // ---- fused: multiply by the kernel spectrum, back to the time domain
+        {
+            const int64_t tot = A.H << lognb;
+            for (int64_t u = threadIdx.x; u < tot; u += blockDim.x) {
+                const int b = (int)(u & (nb - 1));
+                const int64_t k = u >> lognb;
+                res[k * nb + b] = cmul(res[k * nb + b], A.kspec[k]);
+            }
+            __syncthreads();
+        }
+        if (A.kind == RK_REAL_EVEN) {
+            c2r_pre(res, other, M, nb, lognb, A.twF);
+            __syncthreads();
+            res = block_fft<true>(other, res, nb, lognb, A.pl, A.tw);
+        } else {
+            res = block_fft<true>(res, other, nb, lognb, A.pl, A.tw);
+        }
+    } else {
+        // ---- inverse: load spectrum rows
+        const int64_t tot = A.H << lognb;
+        C *dst = (A.kind == RK_REAL_EVEN) ? buf1 : buf0;
+        for (int64_t u = threadIdx.x; u < tot; u += blockDim.x) {
+            const int b = (int)(u / A.H);
+            const int64_t k = u - (int64_t)b * A.H;
+            const int64_t r = rbase + b;
+            C v = C{0, 0};
+            if (r < A.n_rows) {
+                const int64_t *ri = rinfo + 6 * b;
+                v = A.spec[ri[4] * A.spec_s0 + ri[5] * A.spec_s1 + k];
+            }
+            dst[k * nb + b] = v;
+        }
+        __syncthreads();
+        if (A.kind == RK_REAL_ODD) {
+            // Hermitian extension to the full length (DC imaginary part ignored)
+            const int64_t tot2 = M << lognb;
+            for (int64_t u = threadIdx.x; u < tot2; u += blockDim.x) {
+                const int b = (int)(u & (nb - 1));
+                const int64_t k = u >> lognb;
+                if (k >= A.H) buf0[k * nb + b] = cconj(buf0[(M - k) * nb + b]);
+                else if (k == 0) buf0[b].im = 0;
+            }
+            __syncthreads();
+        }
+        if (A.kind == RK_REAL_EVEN) {
+            c2r_pre(buf1, buf0, M, nb, lognb, A.twF);
+            __syncthreads();
+        }
+        res = block_fft<true>(buf0, buf1, nb, lognb, A.pl, A.tw);
+    }
+    // ---- store time-domain samples (scaled; cropped + strided for INV_OUT / FUSED)
+    const bool plain = (A.mode == ROW_INV_PLAIN);
+    const int64_t n_out = plain ? A.F : A.out_n;
+    const int64_t tot = n_out << lognb;
+    for (int64_t u = threadIdx.x; u < tot; u += blockDim.x) {
+        const int b = (int)(u / n_out);
+        const int64_t o = u - (int64_t)b * n_out;
+        const int64_t r = rbase + b;
+        if (r >= A.n_rows) continue;
+        const int64_t p = plain ? o : (A.crop_off + o * A.crop_step);
+        R vr, vi;
+        if (A.kind == RK_REAL_EVEN) {
+            const C z = res[(p >> 1) * nb + b];
+            vr = (p & 1) ? z.im : z.re;
+            vi = 0;
+        } else {
+            const C z = res[p * nb + b];
+            vr = z.re;
+            vi = z.im;
+        }
+        const T v = make_elem<T>(vr * A.scale, vi * A.scale);
+        if (plain) {
+            A.pout[r * A.F + o] = v;
+        } else {
+            const int64_t *ri = rinfo + 6 * b;
+            A.y[ri[4] * A.y_s0 + ri[5] * A.y_s1 + o] = v;
+        }
+    }
+}
+
+// ---------------------------------------------------------- column pass --
+enum ColMode : int { COL_FWD = 0, COL_INV = 1, COL_FUSED = 2 };
+
+template <typename C> struct ColArgs {
+    int mode;
+    const C *src;
+    C *dst;
+    int64_t n_inner, n_outer;
+    int64_t src_outer, src_axis, dst_outer, dst_axis;
+    int64_t valid_in;
+    int64_t crop_off, crop_step, n_out;
+    const C *kspec;
+    int64_t k_axis;
+    FftPlanDev pl;
+    const C *tw;
+    int nb, lognb;
+};
+
+template <typename C>
+__global__ void __launch_bounds__(256) col_kernel(ColArgs<C> A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nb = A.nb, lognb = A.lognb;
+    const int64_t F = A.pl.L;
+    C *buf0 = reinterpret_cast<C *>(smem_raw);
+    C *buf1 = buf0 + F * nb;
+    const int64_t h0 = (int64_t)blockIdx.x * nb;
+    for (int64_t outer = blockIdx.y; outer < A.n_outer; outer += gridDim.y) {
+        const C *src = A.src + outer * A.src_outer + h0;
+        const int64_t tot_in = F << lognb;
+        for (int64_t u = threadIdx.x; u < tot_in; u += blockDim.x) {
+            const int b = (int)(u & (nb - 1));
+            const int64_t i = u >> lognb;
+            C v = C{0, 0};
+            if (i < A.valid_in && h0 + b < A.n_inner) v = src[i * A.src_axis + b];
+            buf0[u] = v;
+        }
+        __syncthreads();
+        C *res;
+        if (A.mode == COL_INV) {
+            res = block_fft<true>(buf0, buf1, nb, lognb, A.pl, A.tw);
+        } else {
+            res = block_fft<false>(buf0, buf1, nb, lognb, A.pl, A.tw);
+            if (A.mode == COL_FUSED) {
+                for (int64_t u = threadIdx.x; u < tot_in; u += blockDim.x) {
+                    const int b = (int)(u & (nb - 1));
+                    const int64_t k = u >> lognb;
+                    if (h0 + b < A.n_inner) res[u] = cmul(res[u], A.kspec[k * A.k_axis + h0 + b]);
+                }
+                __syncthreads();
+                C *other = (res == buf0) ? buf1 : buf0;
+                res = block_fft<true>(res, other, nb, lognb, A.pl, A.tw);
+            }
+        }
+        C *dst = A.dst + outer * A.dst_outer + h0;
+        const int64_t n_out = (A.mode == COL_FWD) ? F : A.n_out;
+        const int64_t tot_out = n_out << lognb;
+        for (int64_t u = threadIdx.x; u < tot_out; u += blockDim.x) {
+            const int b = (int)(u & (nb - 1));
+            const int64_t o = u >> lognb;
+            if (h0 + b >= A.n_inner) continue;
+            const int64_t p = (A.mode == COL_FWD) ? o : (A.crop_off + o * A.crop_step);
+            dst[o * A.dst_axis + b] = res[p * nb + b];
+        }
+        __syncthreads();
+    }
+}
+
+// ----------------------------------------------------------- transpose --
+template <typename C>
+__global__ void transpose_kernel(const C *__restrict__ in, C *__restrict__ out, int64_t rows, int64_t cols) {
+    __shared__ C tile[32][33];
+    const int64_t c0 = (int64_t)blockIdx.x * 32, r0 = (int64_t)blockIdx.y * 32;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int64_t r = r0 + i, c = c0 + threadIdx.x;
+        if (r < rows && c < cols) tile[i][threadIdx.x] = in[r * cols + c];
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int64_t c = c0 + i, r = r0 + threadIdx.x;
+        if (r < rows && c < cols) out[c * rows + r] = tile[threadIdx.x][i];
+    }
+}
+
+// ------------------------------------------------------------- launchers --
+namespace {
+constexpr int kThreads = 256;
+constexpr size_t kFftSmemMax = 200 * 1024;
+
+int ilog2(int v) {
+    int l = 0;
+    while ((1 << l) < v) l++;
+    return l;
+}
+
+template <typename K> int ensure_smem(K fn) {
+    static int done = 0;  // one per instantiation
+    if (!done) {
+        NDCONV_CUDA_OK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFftSmemMax));
+        done = 1;
+    }
+    return NDCONV_OK;
+}
+
+template <typename T> size_t row_smem(const RowArgs<T> &A) {
+    using C = typename RowArgs<T>::C;
+    const int64_t cap = (A.kind == RK_REAL_EVEN ? A.pl.L + 1 : A.pl.L) * A.nb;
+    return sizeof(C) * 2 * cap + sizeof(int64_t) * 6 * A.nb;
+}
+
+// rows per CTA: enough to give each CTA ~2K samples, at least 1
+int pick_nb(int64_t len, int64_t rows, size_t per_row_bytes) {
+    int nb = 1;
+    while (nb < 64 && (int64_t)nb * 2 * len <= 2048 && nb * 2 <= rows + 1 &&
+           per_row_bytes * nb * 2 <= kFftSmemMax)
+        nb *= 2;
+    return nb;
+}
+
+template <typename T> int launch_row(RowArgs<T> A, cudaStream_t st) {
+    using C = typename RowArgs<T>::C;
+    if (A.n_rows <= 0) return NDCONV_OK;
+    const size_t per_row = sizeof(C) * 2 * (A.pl.L + 1) + sizeof(int64_t) * 6;
+    A.nb = pick_nb(A.pl.L, A.n_rows, per_row);
+    A.lognb = ilog2(A.nb);
+    const size_t sm = row_smem(A);
+    if (sm > kFftSmemMax) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "FFT row length exceeds shared memory");
+    int st_ = ensure_smem(row_kernel<T>);
+    if (st_) return st_;
+    const int64_t grid = (A.n_rows + A.nb - 1) / A.nb;
+    if (grid > 0x7fffffff) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "too many FFT rows");
+    row_kernel<T><<<(unsigned)grid, kThreads, sm, st>>>(A);
+    ndconv_count_launch();
+    NDCONV_CUDA_OK(cudaGetLastError());
+    return NDCONV_OK;
+}
+
+template <typename C> int launch_col(ColArgs<C> A, cudaStream_t st) {
+    if (A.n_outer <= 0 || A.n_inner <= 0) return NDCONV_OK;
+    const int64_t F = A.pl.L;
+    int nb = 1;
+    while (nb < 32 && (int64_t)nb * 2 <= A.n_inner + 1 && sizeof(C) * 2 * F * nb * 2 <= 96 * 1024) nb *= 2;
+    A.nb = nb;
+    A.lognb = ilog2(nb);
+    const size_t sm = sizeof(C) * 2 * F * nb;
+    if (sm > kFftSmemMax) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "FFT column length exceeds shared memory");
+    int st_ = ensure_smem(col_kernel<C>);
+    if (st_) return st_;
+    const int64_t gx = (A.n_inner + nb - 1) / nb;
+    const int64_t gy = A.n_outer < 65535 ? A.n_outer : 65535;
+    if (gx > 0x7fffffff) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "too many FFT columns");
+    col_kernel<C><<<dim3((unsigned)gx, (unsigned)gy), kThreads, sm, st>>>(A);
+    ndconv_count_launch();
+    NDCONV_CUDA_OK(cudaGetLastError());
+    return NDCONV_OK;
+}
+
+template <typename C> int plan_with_tw(int64_t L, FftPlanDev &pl, const C **tw) {
+    if (L > (1 << 24) || !make_plan((int)L, pl))
+        return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "FFT length has a prime factor above 64");
+    return get_twiddles<C>((int)L, tw);
+}
+
+// Row plans for a row of F samples: kind, transform plan + tables.
+template <typename T> int row_plan(int64_t F, bool real, RowArgs<T> &A) {
+    using C = typename RowArgs<T>::C;
+    A.F = F;
+    if (!real) {
+        A.kind = RK_COMPLEX;
+        A.H = F;
+        A.twF = nullptr;
+        return plan_with_tw<C>(F, A.pl, &A.tw);
+    }
+    if (F % 2 == 0) {
+        A.kind = RK_REAL_EVEN;
+        A.H = F / 2 + 1;
+        int s = plan_with_tw<C>(F / 2, A.pl, &A.tw);
+        if (s) return s;
+        return get_twiddles<C>((int)F, &A.twF);
+    }
+    A.kind = RK_REAL_ODD;
+    A.H = F / 2 + 1;
+    A.twF = nullptr;
+    return plan_with_tw<C>(F, A.pl, &A.tw);
+}
+
+// workspace: processor-owned (grow only) or stream-ordered per call
+struct Workspace {
+    ndconv_fft_processor *proc;
+    cudaStream_t st;
+    void *ptr = nullptr;
+    bool owned = false;
+    int get(size_t bytes, void **out);
+    ~Workspace() {
+        if (owned && ptr) cudaFreeAsync(ptr, st);
+    }
+};
+}  // namespace
+
+}  // namespace ndconv
+
+struct ndconv_fft_processor {
+    int32_t dtype;
+    int64_t rp_origin_len;
+    void *ws;
+    size_t ws_bytes;
+    int device;
+};
+
+namespace ndconv {
+namespace {
+int Workspace::get(size_t bytes, void **out) {
+    if (bytes == 0) bytes = 16;
+    if (proc) {
+        if (proc->ws_bytes < bytes) {
+            if (proc->ws) {
+                NDCONV_CUDA_OK(cudaStreamSynchronize(st));
+                cudaFree(proc->ws);
+                proc->ws = nullptr;
+                proc->ws_bytes = 0;
+            }
+            NDCONV_CUDA_OK(cudaMalloc(&proc->ws, bytes));
+            proc->ws_bytes = bytes;
+        }
+        *out = proc->ws;
+        return NDCONV_OK;
+    }
+    NDCONV_CUDA_OK(cudaMallocAsync(&ptr, bytes, st));
+    owned = true;
+    *out = ptr;
+    return NDCONV_OK;
+}
+}  // namespace
+
+// ------------------------------------------------------------ conv_fft --
+template <typename T>
+int conv_fft_run(const Geom3<T> &g, int reverse, const T *x, const T *k, T *y,
+                 ndconv_fft_processor *proc, cudaStream_t st, void *scratch, size_t scratch_bytes) {
+    using R = typename Elem<T>::Real;
+    using C = typename CplxT<R>::type;
+    const bool real = !Elem<T>::kComplex;
+    const AxisGeom &A0 = g.ax[0], &A1 = g.ax[1], &A2 = g.ax[2];
+    int64_t P[3] = {A0.L, A1.L, A2.L}, F[3];
+    for (int a = 0; a < 3; a++) F[a] = (P[a] == 1) ? 1 : smooth_size(P[a], real && a == 2);
+    const int astar = F[0] > 1 ? 0 : (F[1] > 1 ? 1 : 2);
+
+    RowArgs<T> rk{};
+    int s = row_plan<T>(F[2], real, rk);
+    if (s) return s;
+    const int64_t H = rk.H;
+    FftPlanDev pl0{}, pl1{};
+    const C *tw0 = nullptr, *tw1 = nullptr;
+    if (F[0] > 1 && (s = plan_with_tw<C>(F[0], pl0, &tw0))) return s;
+    if (F[1] > 1 && (s = plan_with_tw<C>(F[1], pl1, &tw1))) return s;
+
+    // buffers: kernel spectrum Kh[F0][F1][H], data spectrum S[P0][F1][H]
+    const size_t nK = (size_t)F[0] * F[1] * H;
+    const size_t nS = (astar == 2) ? 0 : (size_t)P[0] * F[1] * H;
+    const size_t bytes = sizeof(C) * (nK + nS) + 256;
+    Workspace ws{proc, st};
+    void *base = scratch;
+    if (base) {
+        if (scratch_bytes < bytes) return ndconv_fail(NDCONV_ERR_NO_MEMORY, "scratch too small");
+    } else if ((s = ws.get(bytes, &base))) {
+        return s;
+    }
+    C *Kh = reinterpret_cast<C *>(base);
+    C *S = Kh + nK;
+
+    // ---- kernel spectrum
+    RowArgs<T> kr = rk;
+    kr.mode = ROW_FWD_KERNEL;
+    kr.g = g;
+    kr.k = k;
+    kr.reverse = reverse;
+    kr.n1 = A1.keff;
+    kr.n_rows = A0.keff * A1.keff;
+    kr.spec = Kh;
+    kr.spec_s0 = F[1] * H;
+    kr.spec_s1 = H;
+    kr.scale = 1;
+    if ((s = launch_row(kr, st))) return s;
+    if (F[1] > 1) {
+        ColArgs<C> c{};
+        c.mode = COL_FWD;
+        c.src = c.dst = Kh;
+        c.n_inner = H;
+        c.n_outer = A0.keff;
+        c.src_outer = c.dst_outer = F[1] * H;
+        c.src_axis = c.dst_axis = H;
+        c.valid_in = A1.keff;
+        c.pl = pl1;
+        c.tw = tw1;
+        if ((s = launch_col(c, st))) return s;
+    }
+    if (F[0] > 1) {
+        ColArgs<C> c{};
+        c.mode = COL_FWD;
+        c.src = c.dst = Kh;
+        c.n_inner = F[1] * H;
+        c.n_outer = 1;
+        c.src_axis = c.dst_axis = F[1] * H;
+        c.valid_in = A0.keff;
+        c.pl = pl0;
+        c.tw = tw0;
+        if ((s = launch_col(c, st))) return s;
+    }
+    const R scale = (R)(1.0 / ((double)F[0] * (double)F[1] * (double)F[2]));
+
+    if (astar == 2) {
+        RowArgs<T> fr = rk;
+        fr.mode = ROW_FUSED;
+        fr.g = g;
+        fr.x = x;
+        fr.n1 = 1;
+        fr.n_rows = 1;
+        fr.kspec = Kh;
+        fr.y = y;
+        fr.y_s0 = 0;
+        fr.y_s1 = 0;
+        fr.out_n = A2.out;
+        fr.crop_off = A2.keff - 1;
+        fr.crop_step = A2.s;
+        fr.scale = scale;
+        return launch_row(fr, st);
+    }
+
+    // ---- data: forward row pass into S
+    RowArgs<T> dr = rk;
+    dr.mode = ROW_FWD_DATA;
+    dr.g = g;
+    dr.x = x;
+    dr.n1 = P[1];
+    dr.n_rows = P[0] * P[1];
+    dr.spec = S;
+    dr.spec_s0 = F[1] * H;
+    dr.spec_s1 = H;
+    dr.scale = 1;
+    if ((s = launch_row(dr, st))) return s;
+    if (astar == 0 && F[1] > 1) {
+        ColArgs<C> c{};
+        c.mode = COL_FWD;
+        c.src = c.dst = S;
+        c.n_inner = H;
+        c.n_outer = P[0];
+        c.src_outer = c.dst_outer = F[1] * H;
+        c.src_axis = c.dst_axis = H;
+        c.valid_in = P[1];
+        c.pl = pl1;
+        c.tw = tw1;
+        if ((s = launch_col(c, st))) return s;
+    }
+    {
+        ColArgs<C> c{};
+        c.mode = COL_FUSED;
+        c.src = c.dst = S;
+        c.n_outer = 1;
+        c.kspec = Kh;
+        if (astar == 0) {
+            c.n_inner = F[1] * H;
+            c.src_axis = c.dst_axis = F[1] * H;
+            c.valid_in = P[0];
+            c.k_axis = F[1] * H;
+            c.crop_off = A0.keff - 1;
+            c.crop_step = A0.s;
+            c.n_out = A0.out;
+            c.pl = pl0;
+            c.tw = tw0;
+        } else {
+            c.n_inner = H;
+            c.src_axis = c.dst_axis = H;
+            c.valid_in = P[1];
+            c.k_axis = H;
+            c.crop_off = A1.keff - 1;
+            c.crop_step = A1.s;
+            c.n_out = A1.out;
+            c.pl = pl1;
+            c.tw = tw1;
+        }
+        if ((s = launch_col(c, st))) return s;
+    }
+    if (astar == 0 && F[1] > 1) {
+        ColArgs<C> c{};
+        c.mode = COL_INV;
+        c.src = c.dst = S;
+        c.n_inner = H;
+        c.n_outer = A0.out;
+        c.src_outer = c.dst_outer = F[1] * H;
+        c.src_axis = c.dst_axis = H;
+        c.valid_in = F[1];
+        c.crop_off = A1.keff - 1;
+        c.crop_step = A1.s;
+        c.n_out = A1.out;
+        c.pl = pl1;
+        c.tw = tw1;
+        if ((s = launch_col(c, st))) return s;
+    }
+    RowArgs<T> ir = rk;
+    ir.mode = ROW_INV_OUT;
+    ir.n1 = A1.out;
+    ir.n_rows = A0.out * A1.out;
+    ir.spec = S;
+    ir.spec_s0 = F[1] * H;
+    ir.spec_s1 = H;
+    ir.y = y;
+    ir.y_s0 = A1.out * A2.out;
+    ir.y_s1 = A2.out;
+    ir.out_n = A2.out;
+    ir.crop_off = A2.keff - 1;
+    ir.crop_step = A2.s;
+    ir.scale = scale;
+    return launch_row(ir, st);
+}
+
+template <typename T> size_t conv_fft_scratch_bytes(const Geom3<T> &g) {
+    using R = typename Elem<T>::Real;
+    using C = typename CplxT<R>::type;
+    const bool real = !Elem<T>::kComplex;
+    int64_t P[3] = {g.ax[0].L, g.ax[1].L, g.ax[2].L}, F[3];
+    for (int a = 0; a < 3; a++) F[a] = (P[a] == 1) ? 1 : smooth_size(P[a], real && a == 2);
+    const int64_t H = real ? (F[2] % 2 == 0 ? F[2] / 2 + 1 : F[2] / 2 + 1) : F[2];
+    const int astar = F[0] > 1 ? 0 : (F[1] > 1 ? 1 : 2);
+    const size_t nK = (size_t)F[0] * F[1] * H;
+    const size_t nS = (astar == 2) ? 0 : (size_t)P[0] * F[1] * H;
+    return sizeof(C) * (nK + nS) + 256;
+}
+
+#define NDCONV_INST_FFT(T)                                                                          \
+    template int conv_fft_run<T>(const Geom3<T> &, int, const T *, const T *, T *,                \
+                                 ndconv_fft_processor *, cudaStream_t, void *, size_t);          \
+    template size_t conv_fft_scratch_bytes<T>(const Geom3<T> &);
+NDCONV_INST_FFT(float)
+NDCONV_INST_FFT(double)
+NDCONV_INST_FFT(c32)
+NDCONV_INST_FFT(c64)
+
+// ---------------------------------------------------- processor forward --
+// Natural-layout N-d transform of a contiguous array, then the reference's
+// rotated layout (axes rotated right after each pass = the transpose of
+// [d0] x [rest] for rank >= 2).
+template <typename T>
+int proc_forward(ndconv_fft_processor *proc, int rank, const int64_t *shape, const T *in,
+                 typename CplxT<typename Elem<T>::Real>::type *out, cudaStream_t st) {
+    using R = typename Elem<T>::Real;
+    using C = typename CplxT<R>::type;
+    const bool real = !Elem<T>::kComplex;
+    int64_t s3[3] = {1, 1, 1};
+    for (int i = 0; i < rank; i++) s3[3 - rank + i] = shape[i];
+    RowArgs<T> r{};
+    int s = row_plan<T>(s3[2], real, r);
+    if (s) return s;
+    const int64_t H = r.H;
+    const size_t n = (size_t)s3[0] * s3[1] * H;
+    Workspace ws{proc, st};
+    void *base = nullptr;
+    C *nat = out;
+    if (rank >= 2) {
+        if ((s = ws.get(sizeof(C) * n, &base))) return s;
+        nat = reinterpret_cast<C *>(base);
+    }
+    r.mode = ROW_FWD_PLAIN;
+    r.pin = in;
+    r.n1 = s3[1];
+    r.n_rows = s3[0] * s3[1];
+    r.spec = nat;
+    r.spec_s0 = s3[1] * H;
+    r.spec_s1 = H;
+    r.scale = 1;
+    if ((s = launch_row(r, st))) return s;
+    for (int a = 1; a >= 0; a--) {
+        if (s3[a] <= 1) continue;
+        ColArgs<C> c{};
+        c.mode = COL_FWD;
+        c.src = c.dst = nat;
+        if ((s = plan_with_tw<C>(s3[a], c.pl, &c.tw))) return s;
+        if (a == 1) {
+            c.n_inner = H;
+            c.n_outer = s3[0];
+            c.src_outer = c.dst_outer = s3[1] * H;
+            c.src_axis = c.dst_axis = H;
+        } else {
+            c.n_inner = s3[1] * H;
+            c.n_outer = 1;
+            c.src_axis = c.dst_axis = s3[1] * H;
+        }
+        c.valid_in = s3[a];
+        if ((s = launch_col(c, st))) return s;
+    }
+    if (rank >= 2) {
+        const int64_t rows = shape[0], cols = (int64_t)(n / shape[0]);
+        dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
+        transpose_kernel<C><<<grid, dim3(32, 8), 0, st>>>(nat, out, rows, cols);
+        ndconv_count_launch();
+        NDCONV_CUDA_OK(cudaGetLastError());
+    }
+    proc->rp_origin_len = shape[rank - 1];
+    return NDCONV_OK;
+}
+
+template <typename T>
+int proc_backward(ndconv_fft_processor *proc, int rank, const int64_t *spec_shape,
+                  const typename CplxT<typename Elem<T>::Real>::type *in, T *out, int64_t *out_shape,
+                  cudaStream_t st) {
+    using R = typename Elem<T>::Real;
+    using C = typename CplxT<R>::type;
+    const bool real = !Elem<T>::kComplex;
+    // natural shape: last axis of the rotated layout is d0
+    int64_t nat_shape[3];
+    if (rank == 1) nat_shape[0] = spec_shape[0];
+    else {
+        nat_shape[0] = spec_shape[rank - 1];
+        for (int i = 1; i < rank; i++) nat_shape[i] = spec_shape[i - 1];
+    }
+    const int64_t H = nat_shape[rank - 1];
+    const int64_t n_last = real ? proc->rp_origin_len : H;
+    if (real && (n_last <= 0 || n_last / 2 + 1 != H))
+        return ndconv_fail(NDCONV_ERR_INVALID, "spectrum does not match the last forward length");
+    int64_t s3[3] = {1, 1, 1};
+    for (int i = 0; i < rank; i++) s3[3 - rank + i] = nat_shape[i];
+    size_t n = 1;
+    for (int i = 0; i < rank; i++) n *= (size_t)nat_shape[i];
+    Workspace ws{proc, st};
+    void *base = nullptr;
+    int s;
+    if ((s = ws.get(sizeof(C) * n, &base))) return s;
+    C *nat = reinterpret_cast<C *>(base);
+    if (rank >= 2) {
+        const int64_t rows = (int64_t)(n / nat_shape[0]), cols = nat_shape[0];
+        dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
+        transpose_kernel<C><<<grid, dim3(32, 8), 0, st>>>(in, nat, rows, cols);
+        ndconv_count_launch();
+        NDCONV_CUDA_OK(cudaGetLastError());
+    } else {
+        NDCONV_CUDA_OK(cudaMemcpyAsync(nat, in, sizeof(C) * n, cudaMemcpyDeviceToDevice, st));
+    }
+    for (int a = 0; a <= 1; a++) {
+        if (s3[a] <= 1) continue;
+        ColArgs<C> c{};
+        c.mode = COL_INV;
+        c.src = c.dst = nat;
+        if ((s = plan_with_tw<C>(s3[a], c.pl, &c.tw))) return s;
+        if (a == 1) {
+            c.n_inner = H;
+            c.n_outer = s3[0];
+            c.src_outer = c.dst_outer = s3[1] * H;
+            c.src_axis = c.dst_axis = H;
+        } else {
+            c.n_inner = s3[1] * H;
+            c.n_outer = 1;
+            c.src_axis = c.dst_axis = s3[1] * H;
+        }
+        c.valid_in = s3[a];
+        c.crop_off = 0;
+        c.crop_step = 1;
+        c.n_out = s3[a];
+        if ((s = launch_col(c, st))) return s;
+    }
+    RowArgs<T> r{};
+    if ((s = row_plan<T>(n_last, real, r))) return s;
+    r.mode = ROW_INV_PLAIN;
+    r.pout = out;
+    r.n1 = s3[1];
+    r.n_rows = s3[0] * s3[1];
+    r.spec = nat;
+    r.spec_s0 = s3[1] * H;
+    r.spec_s1 = H;
+    double count = (double)n_last;
+    for (int i = 0; i < rank - 1; i++) count *= (double)nat_shape[i];
+    r.scale = (R)(1.0 / count);
+    for (int i = 0; i < rank; i++) out_shape[i] = nat_shape[i];
+    out_shape[rank - 1] = n_last;
+    return launch_row(r, st);
+}
+
+#define NDCONV_INST_PROC(T)                                                                          \
+    template int proc_forward<T>(ndconv_fft_processor *, int, const int64_t *, const T *,          \
+                                 CplxT<Elem<T>::Real>::type *, cudaStream_t);                       \
+    template int proc_backward<T>(ndconv_fft_processor *, int, const int64_t *,                     \
+                                  const CplxT<Elem<T>::Real>::type *, T *, int64_t *, cudaStream_t);
+NDCONV_INST_PROC(float)
+NDCONV_INST_PROC(double)
+NDCONV_INST_PROC(c32)
+NDCONV_INST_PROC(c64)
+
+}  // namespace ndconv
+
+// ----------------------------------------------------- processor object --
+extern "C" int ndconv_fft_processor_create(int32_t dtype, ndconv_fft_processor **out) {
+    if (!out) return ndconv_fail(NDCONV_ERR_INVALID, "null output pointer");
+    if (dtype != NDCONV_F32 && dtype != NDCONV_F64 && dtype != NDCONV_C32 && dtype != NDCONV_C64)
+        return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "FFT processor needs f32/f64/c32/c64");
+    auto *p = new ndconv_fft_processor{};
+    p->dtype = dtype;
+    cudaGetDevice(&p->device);
+    *out = p;
+    return NDCONV_OK;
+}
+
+extern "C" int ndconv_fft_processor_destroy(ndconv_fft_processor *p) {
+    if (!p) return NDCONV_OK;
+    if (p->ws) {
+        cudaDeviceSynchronize();
+        cudaFree(p->ws);
+    }
+    delete p;
+    return NDCONV_OK;
+}
+
+int64_t ndconv_proc_origin_len(const ndconv_fft_processor *p) { return p->rp_origin_len; }
+int32_t ndconv_proc_dtype(const ndconv_fft_processor *p) { return p->dtype; }

@@ -1,0 +1,30 @@
+// FFT convolution and processor entry points (host side).
+#pragma once
+#include "common.cuh"
+#include "fft_core.cuh"
+
+namespace ndconv {
+
+// conv_fft on the canonical geometry.  scratch (optional) must hold
+// conv_fft_scratch_bytes(g) bytes; otherwise the processor's workspace or
+// a stream-ordered allocation is used.
+template <typename T>
+int conv_fft_run(const Geom3<T> &g, int reverse, const T *x, const T *k, T *y,
+                 ndconv_fft_processor *proc, cudaStream_t st, void *scratch, size_t scratch_bytes);
+template <typename T> size_t conv_fft_scratch_bytes(const Geom3<T> &g);
+
+template <typename T>
+int proc_forward(ndconv_fft_processor *proc, int rank, const int64_t *shape, const T *in,
+                 typename CplxT<typename Elem<T>::Real>::type *out, cudaStream_t st);
+template <typename T>
+int proc_backward(ndconv_fft_processor *proc, int rank, const int64_t *spec_shape,
+                  const typename CplxT<typename Elem<T>::Real>::type *in, T *out, int64_t *out_shape,
+                  cudaStream_t st);
+
+bool make_plan(int L, FftPlanDev &pl);
+int64_t smooth_size(int64_t n, bool even);
+
+}  // namespace ndconv
+
+int64_t ndconv_proc_origin_len(const ndconv_fft_processor *p);
+int32_t ndconv_proc_dtype(const ndconv_fft_processor *p);

@@ -1,0 +1,188 @@
+// Shared-memory FFT building blocks (sm_103a).
+//
+// A CTA transforms nb transforms of length L held in shared memory with
+// element (b, i) at buf[i * nb + b] (nb a power of two).  Each stage is a
+// Stockham autosort radix-R step (no bit reversal), ping-ponging between
+// two buffers: butterfly j reads buf[j + r L/R], applies the twiddles
+// w^(r * (j mod Ns)) with w = exp(-+2 pi i / (Ns R)), does a radix-R DFT in
+// registers and writes to (j / Ns) Ns R + (j mod Ns) + r Ns.  After all
+// stages the result is in natural order.  Twiddles come from a table
+// tw[t] = exp(-2 pi i t / L) evaluated in FP64 on the GPU and rounded once.
+#pragma once
+#include "common.cuh"
+
+namespace ndconv {
+
+template <typename R> struct CplxT;
+template <> struct CplxT<float> { using type = c32; };
+template <> struct CplxT<double> { using type = c64; };
+
+constexpr int kMaxStages = 40;
+constexpr int kMaxGenericRadix = 64;
+
+struct FftPlanDev {
+    int L;
+    int nst;
+    int rad[kMaxStages];
+};
+
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+    return C{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return C{a.re + b.re, a.im + b.im}; }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { return C{a.re - b.re, a.im - b.im}; }
+template <typename C> __device__ __forceinline__ C cconj(C a) { return C{a.re, -a.im}; }
+// multiply by -i (forward) or +i (inverse)
+template <bool INV, typename C> __device__ __forceinline__ C mul_mi(C a) {
+    return INV ? C{-a.im, a.re} : C{a.im, -a.re};
+}
+template <typename C, typename R> __device__ __forceinline__ C cscale(C a, R s) { return C{a.re * s, a.im * s}; }
+
+template <bool INV, typename C> __device__ __forceinline__ void dft2(C *v) {
+    C a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+}
+template <bool INV, typename C> __device__ __forceinline__ void dft4(C &a0, C &a1, C &a2, C &a3) {
+    C s02 = cadd(a0, a2), d02 = csub(a0, a2), s13 = cadd(a1, a3), d13 = mul_mi<INV>(csub(a1, a3));
+    a0 = cadd(s02, s13);
+    a2 = csub(s02, s13);
+    a1 = cadd(d02, d13);
+    a3 = csub(d02, d13);
+}
+template <bool INV, typename C> __device__ __forceinline__ void dft3(C *v) {
+    using R = decltype(v[0].re);
+    const R h = (R)0.5, s = (R)0.86602540378443864676;  // cos(pi/3), sin(pi/3)
+    C a0 = v[0], sum = cadd(v[1], v[2]), dif = csub(v[1], v[2]);
+    C t = C{a0.re - h * sum.re, a0.im - h * sum.im};
+    C u = mul_mi<INV>(cscale(dif, s));
+    v[0] = cadd(a0, sum);
+    v[1] = cadd(t, u);
+    v[2] = csub(t, u);
+}
+template <bool INV, typename C> __device__ __forceinline__ void dft5(C *v) {
+    using R = decltype(v[0].re);
+    const R c1 = (R)0.30901699437494742410, c2 = (R)-0.80901699437494742410;  // cos(2pi/5), cos(4pi/5)
+    const R s1 = (R)0.95105651629515357212, s2 = (R)0.58778525229247312917;   // sin(2pi/5), sin(4pi/5)
+    C a0 = v[0];
+    C b1 = cadd(v[1], v[4]), b2 = cadd(v[2], v[3]), d1 = csub(v[1], v[4]), d2 = csub(v[2], v[3]);
+    C t1 = C{a0.re + c1 * b1.re + c2 * b2.re, a0.im + c1 * b1.im + c2 * b2.im};
+    C t2 = C{a0.re + c2 * b1.re + c1 * b2.re, a0.im + c2 * b1.im + c1 * b2.im};
+    C u1 = mul_mi<INV>(C{s1 * d1.re + s2 * d2.re, s1 * d1.im + s2 * d2.im});
+    C u2 = mul_mi<INV>(C{s2 * d1.re - s1 * d2.re, s2 * d1.im - s1 * d2.im});
+    v[0] = cadd(a0, cadd(b1, b2));
+    v[1] = cadd(t1, u1);
+    v[4] = csub(t1, u1);
+    v[2] = cadd(t2, u2);
+    v[3] = csub(t2, u2);
+}
+template <bool INV, typename C> __device__ __forceinline__ void dft8(C *v) {
+    using R = decltype(v[0].re);
+    const R r2 = (R)0.70710678118654752440;
+    C e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+    C o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+    dft4<INV>(e0, e1, e2, e3);
+    dft4<INV>(o0, o1, o2, o3);
+    // o_k *= w8^k, w8 = exp(-+ i pi / 4)
+    o1 = INV ? C{r2 * (o1.re - o1.im), r2 * (o1.re + o1.im)} : C{r2 * (o1.re + o1.im), r2 * (o1.im - o1.re)};
+    o2 = mul_mi<INV>(o2);
+    o3 = INV ? C{-r2 * (o3.re + o3.im), r2 * (o3.re - o3.im)} : C{r2 * (o3.im - o3.re), -r2 * (o3.re + o3.im)};
+    v[0] = cadd(e0, o0);
+    v[4] = csub(e0, o0);
+    v[1] = cadd(e1, o1);
+    v[5] = csub(e1, o1);
+    v[2] = cadd(e2, o2);
+    v[6] = csub(e2, o2);
+    v[3] = cadd(e3, o3);
+    v[7] = csub(e3, o3);
+}
+
+template <bool INV, typename C>
+__device__ __forceinline__ C twiddle(const C *__restrict__ tw, int64_t e) {
+    C w = tw[e];
+    return INV ? cconj(w) : w;
+}
+
+// One radix-R Stockham stage over nb interleaved transforms.
+template <bool INV, int RAD, typename C>
+__device__ __forceinline__ void stockham_stage(const C *src, C *dst, int L, int nb, int lognb, int Ns,
+                                               const C *__restrict__ tw) {
+    const int nr = L / RAD;
+    const int twstep = L / (Ns * RAD);
+    const int total = nr << lognb;
+    for (int u = threadIdx.x; u < total; u += blockDim.x) {
+        const int b = u & (nb - 1);
+        const int j = u >> lognb;
+        const int t = j % Ns;
+        C v[RAD];
+#pragma unroll
+        for (int r = 0; r < RAD; r++) v[r] = src[(j + r * nr) * nb + b];
+        if (t) {
+#pragma unroll
+            for (int r = 1; r < RAD; r++) v[r] = cmul(v[r], twiddle<INV>(tw, (int64_t)t * r * twstep));
+        }
+        if constexpr (RAD == 2) dft2<INV>(v);
+        else if constexpr (RAD == 3) dft3<INV>(v);
+        else if constexpr (RAD == 4) dft4<INV>(v[0], v[1], v[2], v[3]);
+        else if constexpr (RAD == 5) dft5<INV>(v);
+        else if constexpr (RAD == 8) dft8<INV>(v);
+        const int base = (j / Ns) * Ns * RAD + t;
+#pragma unroll
+        for (int r = 0; r < RAD; r++) dst[(base + r * Ns) * nb + b] = v[r];
+    }
+}
+
+// Generic odd-prime radix (O(p^2), runtime p <= kMaxGenericRadix).
+template <bool INV, typename C>
+__device__ void stockham_stage_generic(const C *src, C *dst, int L, int nb, int lognb, int Ns, int RAD,
+                                       const C *__restrict__ tw) {
+    const int nr = L / RAD;
+    const int twstep = L / (Ns * RAD);
+    const int wstep = L / RAD;  // tw index step for the radix's own roots
+    const int total = nr << lognb;
+    for (int u = threadIdx.x; u < total; u += blockDim.x) {
+        const int b = u & (nb - 1);
+        const int j = u >> lognb;
+        const int t = j % Ns;
+        C v[kMaxGenericRadix];
+        for (int r = 0; r < RAD; r++) {
+            C x = src[(j + r * nr) * nb + b];
+            if (t && r) x = cmul(x, twiddle<INV>(tw, (int64_t)t * r * twstep));
+            v[r] = x;
+        }
+        const int base = (j / Ns) * Ns * RAD + t;
+        for (int k = 0; k < RAD; k++) {
+            C acc = v[0];
+            for (int m = 1; m < RAD; m++) acc = cadd(acc, cmul(v[m], twiddle<INV>(tw, (int64_t)((m * k) % RAD) * wstep)));
+            dst[(base + k * Ns) * nb + b] = acc;
+        }
+    }
+}
+
+// Full transform of nb interleaved length-L sequences starting in `a`, using
+// `b` as the second buffer.  Returns the buffer holding the result.  Must be
+// called by all threads of the CTA; ends with a barrier.
+template <bool INV, typename C>
+__device__ C *block_fft(C *a, C *b, int nb, int lognb, const FftPlanDev &pl, const C *__restrict__ tw) {
+    C *src = a, *dst = b;
+    int Ns = 1;
+    for (int s = 0; s < pl.nst; s++) {
+        const int R = pl.rad[s];
+        switch (R) {
+        case 2: stockham_stage<INV, 2>(src, dst, pl.L, nb, lognb, Ns, tw); break;
+        case 3: stockham_stage<INV, 3>(src, dst, pl.L, nb, lognb, Ns, tw); break;
+        case 4: stockham_stage<INV, 4>(src, dst, pl.L, nb, lognb, Ns, tw); break;
+        case 5: stockham_stage<INV, 5>(src, dst, pl.L, nb, lognb, Ns, tw); break;
+        case 8: stockham_stage<INV, 8>(src, dst, pl.L, nb, lognb, Ns, tw); break;
+        default: stockham_stage_generic<INV>(src, dst, pl.L, nb, lognb, Ns, R, tw); break;
+        }
+        __syncthreads();
+        Ns *= R;
+        C *tmp = src;
+        src = dst;
+        dst = tmp;
+    }
+    return src;
+}
+
+}  // namespace ndconv

@@ -1,0 +1,35 @@
+// Canonical (three-axis) plan of one convolution problem, built on the host
+// by plan_problem() in abi.cu.
+#pragma once
+#include "common.cuh"
+#include "direct.h"
+
+namespace ndconv {
+
+struct Plan3 {
+    int rank;
+    int dtype;
+    int reverse;
+    AxisGeom ax[3];
+    double cval[3][2][2];  // per axis, side (front, back), (re, im)
+
+    template <typename T> Geom3<T> geom() const {
+        Geom3<T> g;
+        for (int a = 0; a < 3; a++) {
+            g.ax[a] = ax[a];
+            g.cf[a] = Elem<T>::from(cval[a][0][0], cval[a][0][1]);
+            g.cb[a] = Elem<T>::from(cval[a][1][0], cval[a][1][1]);
+        }
+        return g;
+    }
+    template <typename T> DirectParams<T> direct() const {
+        DirectParams<T> d{};
+        d.g = geom<T>();
+        d.reverse = reverse;
+        return d;
+    }
+};
+
+int plan_problem(const ndconv_problem *p, int algo, Plan3 *out);
+
+}  // namespace ndconv

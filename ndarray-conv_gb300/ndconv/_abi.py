@@ -84,6 +84,7 @@ def lib():
         "ndconv_fft_backward": (ctypes.c_int, [vp, i32, i64p, vp, vp, i64p, vp]),
         "ndconv_last_error": (ctypes.c_char_p, []),
         "ndconv_version": (ctypes.c_char_p, []),
+        "ndconv_kernel_launches": (ctypes.c_uint64, []),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

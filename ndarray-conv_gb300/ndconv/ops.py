@@ -1,0 +1,154 @@
+"""conv / conv_fft / FFT processor over the C ABI (device tensors via torch).
+
+Mirrors ConvExt::conv (src/conv/mod.rs:78-116), ConvFFTExt::{conv_fft,
+conv_fft_with_processor, conv_fft_par} (src/conv_fft/mod.rs:81-183) and
+get_fft_processor / Processor::{forward, backward}
+(src/conv_fft/processor/mod.rs:71-143).  Inputs may be CUDA tensors (used
+in place, any strides) or numpy arrays (copied to the GPU; the result comes
+back as numpy).  Every call runs the CUDA library; there is no CPU path.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _abi
+from .api import build_problem, dtype_code, into_kernel_with_dilation, raise_for_status
+
+_TORCH_OF = {_abi.F32: torch.float32, _abi.F64: torch.float64, _abi.I32: torch.int32,
+             _abi.C32: torch.complex64, _abi.C64: torch.complex128}
+
+
+def _to_device(a):
+    if isinstance(a, torch.Tensor):
+        if not a.is_cuda:
+            return a.cuda(), True
+        return a, False
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda(), True
+
+
+def _stream_ptr(stream):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _prepare(data, kernel, conv_mode, padding_mode):
+    kwd = into_kernel_with_dilation(kernel)
+    x, x_host = _to_device(data)
+    k, _ = _to_device(kwd.kernel)
+    if x.dtype != k.dtype:
+        raise TypeError(f"data {x.dtype} and kernel {k.dtype} element types differ")
+    dt = dtype_code(x.dtype)
+    from .api import KernelWithDilation
+    kwd = KernelWithDilation(k, kwd.dilation, kwd.reverse_flag)
+    p = build_problem(dt, tuple(x.shape), kwd, conv_mode, padding_mode,
+                      data_strides=x.stride(), kernel_strides=k.stride())
+    return p, x, k, x_host
+
+
+def _run(algo, data, kernel, conv_mode, padding_mode, processor=None, stream=None):
+    L = _abi.lib()
+    p, x, k, x_host = _prepare(data, kernel, conv_mode, padding_mode)
+    shape = (ctypes.c_int64 * 3)()
+    raise_for_status(L.ndconv_output_shape(ctypes.byref(p), algo, shape), p, algo)
+    y = torch.empty([shape[i] for i in range(p.rank)], dtype=x.dtype, device=x.device)
+    sp = _stream_ptr(stream)
+    if algo == 0:
+        st = L.ndconv_conv(ctypes.byref(p), ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(k.data_ptr()),
+                           ctypes.c_void_p(y.data_ptr()), sp)
+    else:
+        h = processor._handle if processor is not None else None
+        st = L.ndconv_conv_fft(ctypes.byref(p), ctypes.c_void_p(x.data_ptr()),
+                               ctypes.c_void_p(k.data_ptr()), ctypes.c_void_p(y.data_ptr()), h, sp)
+    raise_for_status(st, p, algo)
+    if x_host:
+        return y.cpu().numpy()
+    return y
+
+
+def conv(data, kernel, conv_mode, padding_mode, stream=None):
+    """ConvExt::conv: direct convolution (kernel may carry dilation/no_reverse)."""
+    return _run(0, data, kernel, conv_mode, padding_mode, stream=stream)
+
+
+def conv_fft(data, kernel, conv_mode, padding_mode, stream=None):
+    """ConvFFTExt::conv_fft (f32, f64, complex64, complex128)."""
+    return _run(1, data, kernel, conv_mode, padding_mode, stream=stream)
+
+
+def conv_fft_with_processor(data, kernel, conv_mode, padding_mode, processor, stream=None):
+    """ConvFFTExt::conv_fft_with_processor: reuses the processor's workspace."""
+    return _run(1, data, kernel, conv_mode, padding_mode, processor=processor, stream=stream)
+
+
+def conv_fft_par(data, kernel, conv_mode, padding_mode, stream=None):
+    """ConvFFTExt::conv_fft_par: on the GPU the same kernels as conv_fft."""
+    return _run(1, data, kernel, conv_mode, padding_mode, stream=stream)
+
+
+class FftProcessor:
+    """Processor<T, InElem> (src/conv_fft/processor/mod.rs:79-119)."""
+
+    def __init__(self, dtype):
+        self.dtype = dtype_code(dtype)
+        h = ctypes.c_void_p()
+        st = _abi.lib().ndconv_fft_processor_create(self.dtype, ctypes.byref(h))
+        if st:
+            raise RuntimeError(_abi.last_error())
+        self._handle = h
+
+    def close(self):
+        if self._handle:
+            _abi.lib().ndconv_fft_processor_destroy(self._handle)
+            self._handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _cdtype(self):
+        return torch.complex64 if self.dtype in (_abi.F32, _abi.C32) else torch.complex128
+
+    def forward(self, x, stream=None):
+        """Spectrum in the reference's rotated axis layout."""
+        xd, host = _to_device(x)
+        xd = xd.contiguous()
+        rank = xd.dim()
+        shape = (ctypes.c_int64 * 3)(*list(xd.shape))
+        osh = (ctypes.c_int64 * 3)()
+        L = _abi.lib()
+        st = L.ndconv_fft_forward(self._handle, rank, shape, None, None, osh, None)
+        if st:
+            raise RuntimeError(_abi.last_error())
+        out = torch.empty([osh[i] for i in range(rank)], dtype=self._cdtype(), device=xd.device)
+        st = L.ndconv_fft_forward(self._handle, rank, shape, ctypes.c_void_p(xd.data_ptr()),
+                                  ctypes.c_void_p(out.data_ptr()), osh, _stream_ptr(stream))
+        if st:
+            raise RuntimeError(_abi.last_error())
+        return out.cpu().numpy() if host else out
+
+    def backward(self, spec, stream=None):
+        sd, host = _to_device(spec)
+        sd = sd.contiguous()
+        rank = sd.dim()
+        shape = (ctypes.c_int64 * 3)(*list(sd.shape))
+        osh = (ctypes.c_int64 * 3)()
+        L = _abi.lib()
+        st = L.ndconv_fft_backward(self._handle, rank, shape, None, None, osh, None)
+        if st:
+            raise RuntimeError(_abi.last_error())
+        odt = _TORCH_OF[self.dtype]
+        out = torch.empty([osh[i] for i in range(rank)], dtype=odt, device=sd.device)
+        st = L.ndconv_fft_backward(self._handle, rank, shape, ctypes.c_void_p(sd.data_ptr()),
+                                   ctypes.c_void_p(out.data_ptr()), osh, _stream_ptr(stream))
+        if st:
+            raise RuntimeError(_abi.last_error())
+        return out.cpu().numpy() if host else out
+
+
+def get_fft_processor(dtype=torch.float32):
+    """get_fft_processor::<T, InElem>() (src/lib.rs:75-77): real dtype -> real
+    processor, complex dtype -> complex processor."""
+    return FftProcessor(dtype)

@@ -533,7 +533,10 @@ int orc_fft_buffers(const orc_problem *p, const int64_t *fft_size, const double 
     cstrides(fft_size, rank, fst);
     cstrides(p->ks, rank, kst);
     for (long i = 0; i < nF; i++) { dbuf[i] = 0; kbuf[i] = 0; }
-    for (long f = 0; f < npd; f++) {
+    /* the data buffer is only defined when the padded data fits fft_size */
+    int fits = 1;
+    for (int i = 0; i < rank; i++) if (pds[i] > fft_size[i]) fits = 0;
+    for (long f = 0; fits && f < npd; f++) {
         long r = f, o = 0;
         for (int i = 0; i < rank; i++) { long idx = r / pst[i]; r %= pst[i]; o += idx * fst[i]; }
         dbuf[o] = pd[f];
