@@ -122,6 +122,20 @@ int ndconv_conv(const ndconv_problem *p, const void *data, const void *kernel, v
 int ndconv_conv_fft(const ndconv_problem *p, const void *data, const void *kernel, void *out,
                     ndconv_fft_processor *proc, void *stream);
 
+/* ndconv_conv_fft for callers that cannot allocate device memory (inside
+ * a CUDA graph being captured, hosts that forbid allocation after start-up,
+ * plugins whose host owns every allocation).  No counterpart in the
+ * reference.  Same arguments and results as ndconv_conv_fft without a
+ * processor, but the spectra and twiddle tables live in one fixed 16 MiB
+ * device array that the library holds on every GPU where it is loaded; it
+ * never calls cudaMalloc or cudaFree.  Problems whose spectra need more
+ * than 16 MiB get NDCONV_ERR_NO_MEMORY.  The first call on each device
+ * looks up the array's address, so make it before any stream capture.
+ * Calls share the array: calls whose GPU work overlaps race and must be
+ * serialised by the caller. */
+int ndconv_conv_fft_noalloc(const ndconv_problem *p, const void *data, const void *kernel, void *out,
+                            void *stream);
+
 /* GetProcessor::get_processor / get_fft_processor::<T, InElem>()
  * (src/conv_fft/processor/mod.rs:71-73,125-143; src/lib.rs:75-77).
  * dtype F32/F64 selects the real processor (real.rs), C32/C64 the complex

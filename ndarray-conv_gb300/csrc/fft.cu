@@ -37,11 +37,45 @@ __global__ void gen_twiddles_kernel(C *tw, int L) {
     }
 }
 
+thread_local TwArena *g_tw_arena = nullptr;
+
+TwArenaScope::TwArenaScope(TwArena *a) : prev(g_tw_arena) { g_tw_arena = a; }
+TwArenaScope::~TwArenaScope() { g_tw_arena = prev; }
+
 namespace {
 std::mutex g_tw_mu;
 std::map<std::tuple<int, int, int>, void *> g_tw;  // (device, bytes-per-complex, L) -> table
 
+// Tables carved from a caller-provided arena and generated on its stream
+// (no allocation, no synchronisation).
+template <typename C> int arena_twiddles(TwArena *a, int L, const C **out) {
+    for (int i = 0; i < a->n; i++)
+        if (a->len[i] == L && a->elem[i] == (int)sizeof(C)) {
+            *out = (const C *)a->table[i];
+            return NDCONV_OK;
+        }
+    const size_t off = (a->used + 255) / 256 * 256;
+    const size_t bytes = sizeof(C) * (size_t)(L > 0 ? L : 1);
+    if (a->n >= TwArena::kMaxTables || off + bytes > a->cap)
+        return ndconv_fail(NDCONV_ERR_NO_MEMORY, "twiddle tables do not fit the provided scratch");
+    C *p = reinterpret_cast<C *>(a->base + off);
+    int blocks = (L + 255) / 256;
+    if (blocks > 1024) blocks = 1024;
+    if (blocks < 1) blocks = 1;
+    gen_twiddles_kernel<C><<<blocks, 256, 0, a->st>>>(p, L);
+    ndconv_count_launch();
+    NDCONV_CUDA_OK(cudaGetLastError());
+    a->used = off + bytes;
+    a->len[a->n] = L;
+    a->elem[a->n] = (int)sizeof(C);
+    a->table[a->n] = p;
+    a->n++;
+    *out = p;
+    return NDCONV_OK;
+}
+
 template <typename C> int get_twiddles(int L, const C **out) {
+    if (g_tw_arena) return arena_twiddles<C>(g_tw_arena, L, out);
     int dev = 0;
     NDCONV_CUDA_OK(cudaGetDevice(&dev));
     std::lock_guard<std::mutex> lk(g_tw_mu);

@@ -22,6 +22,24 @@ int proc_backward(ndconv_fft_processor *proc, int rank, const int64_t *spec_shap
                   cudaStream_t st);
 
 bool make_plan(int L, FftPlanDev &pl);
+
+// Optional home for twiddle tables: while a TwArenaScope is alive on the
+// calling thread, tables are carved from `base` and generated on `st`
+// instead of the process-wide cache (which allocates and synchronises).
+struct TwArena {
+    static constexpr int kMaxTables = 8;
+    unsigned char *base;
+    size_t cap, used;
+    cudaStream_t st;
+    int n;
+    int len[kMaxTables], elem[kMaxTables];
+    void *table[kMaxTables];
+};
+struct TwArenaScope {
+    explicit TwArenaScope(TwArena *a);
+    ~TwArenaScope();
+    TwArena *prev;
+};
 int64_t smooth_size(int64_t n, bool even);
 
 }  // namespace ndconv
