@@ -122,6 +122,18 @@ int ndconv_conv(const ndconv_problem *p, const void *data, const void *kernel, v
 int ndconv_conv_fft(const ndconv_problem *p, const void *data, const void *kernel, void *out,
                     ndconv_fft_processor *proc, void *stream);
 
+/* Batched ConvExt::conv / ConvFFTExt::conv_fft over n instances that share
+ * one problem geometry (shapes, dilation, modes); each instance has its
+ * own data, kernel and output.  data / kernel / out are DEVICE arrays of n
+ * device pointers.  The crate has no batch call: these are the loops
+ * `for i in 0..n { x[i].conv(k[i], ..) }` and `.conv_fft(..)` in one
+ * submission.  The FFT batch runs in waves whose spectra stay in L2. */
+int ndconv_conv_batch(const ndconv_problem *p, int64_t n, const void *const *data,
+                      const void *const *kernel, void *const *out, void *stream);
+int ndconv_conv_fft_batch(const ndconv_problem *p, int64_t n, const void *const *data,
+                          const void *const *kernel, void *const *out, ndconv_fft_processor *proc,
+                          void *stream);
+
 /* ndconv_conv_fft for callers that cannot allocate device memory (inside
  * a CUDA graph being captured, hosts that forbid allocation after start-up,
  * plugins whose host owns every allocation).  No counterpart in the

@@ -11,6 +11,9 @@
 #include "geometry.h"
 
 #include <atomic>
+#include <mutex>
+#include <set>
+#include <utility>
 
 namespace {
 thread_local std::string g_last_error;
@@ -20,6 +23,20 @@ std::atomic<uint64_t> g_launches{0};
 void ndconv_count_launch(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 extern "C" uint64_t ndconv_kernel_launches(void) { return g_launches.load(); }
+
+cudaError_t ndconv_allow_smem(const void *kernel, int bytes) {
+    static std::mutex mu;
+    static std::set<std::pair<int, std::pair<const void *, int>>> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    auto key = std::make_pair(dev, std::make_pair(kernel, bytes));
+    if (done.count(key)) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) done.insert(key);
+    return e;
+}
 
 int ndconv_fail(int status, const char *msg) {
     g_last_error = msg ? msg : "";
@@ -239,6 +256,46 @@ extern "C" int ndconv_conv_fft(const ndconv_problem *p, const void *data, const 
     case NDCONV_F64: return conv_fft_run<double>(P.geom<double>(), P.reverse, (const double *)data, (const double *)kernel, (double *)out, proc, st, nullptr, 0);
     case NDCONV_C32: return conv_fft_run<c32>(P.geom<c32>(), P.reverse, (const c32 *)data, (const c32 *)kernel, (c32 *)out, proc, st, nullptr, 0);
     case NDCONV_C64: return conv_fft_run<c64>(P.geom<c64>(), P.reverse, (const c64 *)data, (const c64 *)kernel, (c64 *)out, proc, st, nullptr, 0);
+    default: return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "integer FFT convolution is not supported (documented broken upstream)");
+    }
+}
+
+extern "C" int ndconv_conv_batch(const ndconv_problem *p, int64_t n, const void *const *data,
+                                 const void *const *kernel, void *const *out, void *stream) {
+    Plan3 P;
+    int s = plan_problem(p, 0, &P);
+    if (s) return s;
+    if (n < 0) return ndconv_fail(NDCONV_ERR_INVALID, "negative batch size");
+    if (n == 0) return NDCONV_OK;
+    if (!data || !kernel || !out) return ndconv_fail(NDCONV_ERR_INVALID, "null pointer array");
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaSuccess;
+    switch (P.dtype) {
+    case NDCONV_F32: e = direct_conv_batch_launch<float>(n, (const float *const *)data, (const float *const *)kernel, (float *const *)out, P.direct<float>(), st); break;
+    case NDCONV_F64: e = direct_conv_batch_launch<double>(n, (const double *const *)data, (const double *const *)kernel, (double *const *)out, P.direct<double>(), st); break;
+    case NDCONV_I32: e = direct_conv_batch_launch<int32_t>(n, (const int32_t *const *)data, (const int32_t *const *)kernel, (int32_t *const *)out, P.direct<int32_t>(), st); break;
+    case NDCONV_C32: e = direct_conv_batch_launch<c32>(n, (const c32 *const *)data, (const c32 *const *)kernel, (c32 *const *)out, P.direct<c32>(), st); break;
+    case NDCONV_C64: e = direct_conv_batch_launch<c64>(n, (const c64 *const *)data, (const c64 *const *)kernel, (c64 *const *)out, P.direct<c64>(), st); break;
+    }
+    if (e != cudaSuccess) return ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e));
+    return NDCONV_OK;
+}
+
+extern "C" int ndconv_conv_fft_batch(const ndconv_problem *p, int64_t n, const void *const *data,
+                                     const void *const *kernel, void *const *out, ndconv_fft_processor *proc,
+                                     void *stream) {
+    Plan3 P;
+    int s = plan_problem(p, 1, &P);
+    if (s) return s;
+    if (n < 0) return ndconv_fail(NDCONV_ERR_INVALID, "negative batch size");
+    if (n == 0) return NDCONV_OK;
+    if (!data || !kernel || !out) return ndconv_fail(NDCONV_ERR_INVALID, "null pointer array");
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (P.dtype) {
+    case NDCONV_F32: return conv_fft_batch_run<float>(P.geom<float>(), P.reverse, n, (const float *const *)data, (const float *const *)kernel, (float *const *)out, proc, st);
+    case NDCONV_F64: return conv_fft_batch_run<double>(P.geom<double>(), P.reverse, n, (const double *const *)data, (const double *const *)kernel, (double *const *)out, proc, st);
+    case NDCONV_C32: return conv_fft_batch_run<c32>(P.geom<c32>(), P.reverse, n, (const c32 *const *)data, (const c32 *const *)kernel, (c32 *const *)out, proc, st);
+    case NDCONV_C64: return conv_fft_batch_run<c64>(P.geom<c64>(), P.reverse, n, (const c64 *const *)data, (const c64 *const *)kernel, (c64 *const *)out, proc, st);
     default: return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "integer FFT convolution is not supported (documented broken upstream)");
     }
 }

@@ -12,6 +12,12 @@ template <typename T> struct DirectParams {
     int64_t max_rows, max_cols;
     int64_t tile_elems, w_elems;
     int64_t maps_off;        // byte offset of the int64 border maps in shared memory
+    int sw_ty, sw_nseg, sw_q;  // sliding-window tiling (rows, segments, swizzle pitch)
+    // batch: device arrays of per-instance pointers (null for one instance)
+    const T *const *xs;
+    const T *const *ks;
+    T *const *ys;
+    int64_t inst_base;
 };
 
 // x, k: device pointers (strided per g.ax[i].xs / ks); y: contiguous output.
@@ -19,5 +25,10 @@ template <typename T> struct DirectParams {
 template <typename T>
 cudaError_t direct_conv_launch(const T *x, const T *k, T *y, DirectParams<T> P, cudaStream_t st,
                                int force_naive);
+
+// n instances sharing the geometry; xs / ks / ys: device arrays of n device pointers.
+template <typename T>
+cudaError_t direct_conv_batch_launch(int64_t n, const T *const *xs, const T *const *ks, T *const *ys,
+                                     DirectParams<T> P, cudaStream_t st);
 
 }  // namespace ndconv

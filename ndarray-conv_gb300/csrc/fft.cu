@@ -129,19 +129,53 @@ bool make_plan(int L, FftPlanDev &pl) {
             r = 1;
         }
     }
+    uint32_t ns = 1;
+    for (int s = 0; s < pl.nst; s++) {
+        pl.ns[s] = make_fastdiv(ns);
+        ns *= (uint32_t)pl.rad[s];
+    }
     return true;
 }
 
+// Relative cost of one Stockham stage per element, by radix (each stage is
+// one shared-memory round trip; larger radices do more arithmetic).
+static double stage_cost(int r) {
+    switch (r) {
+    case 8: return 1.0;
+    case 4: return 0.75;
+    case 2: return 0.6;
+    case 3: return 0.8;
+    case 5: return 1.0;
+    case 7: return 1.3;
+    default: return 4.0;
+    }
+}
+
+// Cheapest 2^a 3^b 5^c 7^d >= n (even when asked; the real axis transforms
+// half of it), among sizes up to 1.35 n.
 int64_t smooth_size(int64_t n, bool even) {
-    // smallest 2^a 3^b 5^c 7^d >= n (and even when asked)
     if (n <= 1) return even ? 2 : 1;
     int64_t best = INT64_MAX;
-    for (int64_t p7 = 1; p7 < 2 * n + 8; p7 *= 7)
-        for (int64_t p5 = p7; p5 < 2 * n + 8; p5 *= 5)
-            for (int64_t p3 = p5; p3 < 2 * n + 8; p3 *= 3) {
+    double best_cost = 1e300;
+    const int64_t lim = n + n * 35 / 100 + 8;
+    for (int64_t p7 = 1; p7 <= 4 * lim; p7 *= 7)
+        for (int64_t p5 = p7; p5 <= 4 * lim; p5 *= 5)
+            for (int64_t p3 = p5; p3 <= 4 * lim; p3 *= 3) {
                 int64_t v = p3;
                 while (v < n || (even && (v & 1))) v *= 2;
-                if (v < best) best = v;
+                if (v > lim && best != INT64_MAX) continue;
+                FftPlanDev pl;
+                const int64_t L = even ? v / 2 : v;
+                double c = 1e300;
+                if (L < (1 << 30) && make_plan((int)L, pl)) {
+                    c = 0;
+                    for (int s = 0; s < pl.nst; s++) c += stage_cost(pl.rad[s]);
+                    c *= (double)L;
+                }
+                if (c < best_cost || (c == best_cost && v < best)) {
+                    best_cost = c;
+                    best = v;
+                }
             }
     return best;
 }
@@ -157,6 +191,10 @@ enum RowMode : int {
 };
 enum RowKind : int { RK_COMPLEX = 0, RK_REAL_EVEN = 1, RK_REAL_ODD = 2 };
 
+// One pass over rows of the contiguous axis.  Batched: blockIdx.y selects
+// the instance; its data / kernel / output pointers come from the device
+// arrays xs / ks / ys (or x / k / y for a single instance) and its spectra
+// sit inst * spec_is (kspec_is) elements further.
 template <typename T> struct RowArgs {
     using C = typename CplxT<typename Elem<T>::Real>::type;
     using R = typename Elem<T>::Real;
@@ -164,9 +202,10 @@ template <typename T> struct RowArgs {
     int64_t F;           // samples per row (real or complex)
     int64_t H;           // spectrum bins per row
     int64_t n_rows, n1;  // row r -> (r / n1, r % n1)
-    int64_t spec_s0, spec_s1;
+    int64_t spec_s0, spec_s1, spec_is;
     C *spec;
     const C *kspec;
+    int64_t kspec_is;
     const T *x;
     Geom3<T> g;
     const T *k;
@@ -175,6 +214,10 @@ template <typename T> struct RowArgs {
     int64_t y_s0, y_s1, out_n, crop_off, crop_step;
     const T *pin;
     T *pout;
+    const T *const *xs;
+    const T *const *ks;
+    T *const *ys;
+    int64_t inst_base;
     FftPlanDev pl;   // length M = F/2 (real even) or F
     const C *tw;     // table for pl.L
     const C *twF;    // table for F (real even)
@@ -208,38 +251,51 @@ template <typename T> __device__ __forceinline__ T make_elem(typename Elem<T>::R
     else return (T)re;
 }
 
-// sample j of row (i0, i1) for the forward loads
-template <typename T>
-__device__ __forceinline__ T row_sample(const RowArgs<T> &A, int64_t m0, int64_t m1, int64_t t0, int64_t t1,
-                                        int64_t row, int64_t j) {
-    if (A.mode == ROW_FWD_PLAIN) return A.pin[row * A.F + j];
-    if (A.mode == ROW_FWD_KERNEL) {
-        if (t0 < 0 || t1 < 0) return Elem<T>::zero();
+// per-row facts shared by the CTA
+struct RowInfo {
+    int64_t xoff;    // data: offset of the row's first input sample (interior rows)
+    int64_t soff;    // spectrum row offset
+    int64_t yoff;    // output row offset
+    int64_t m0, m1;  // data: border-mapped leading indices
+    int64_t t0, t1;  // kernel: tap indices of the leading axes (-1: zero row)
+    int valid, interior;
+};
+
+// sample j of a row for the forward loads (MODE is the RowMode)
+template <int MODE, typename T>
+__device__ __forceinline__ T row_sample(const RowArgs<T> &A, const T *__restrict__ x, const T *__restrict__ k,
+                                        const RowInfo &ri, int64_t row, int64_t j) {
+    if constexpr (MODE == ROW_FWD_PLAIN) {
+        return A.pin[row * A.F + j];
+    } else if constexpr (MODE == ROW_FWD_KERNEL) {
+        if (ri.t0 < 0 || ri.t1 < 0) return Elem<T>::zero();
         const int64_t t2 = kbuf_tap(A.g.ax[2], j, A.reverse);
         if (t2 < 0) return Elem<T>::zero();
-        return A.k[t0 * A.g.ax[0].ks + t1 * A.g.ax[1].ks + t2 * A.g.ax[2].ks];
+        return k[ri.t0 * A.g.ax[0].ks + ri.t1 * A.g.ax[1].ks + t2 * A.g.ax[2].ks];
+    } else {
+        // data (FWD_DATA / FUSED): zero beyond the padded extent
+        const AxisGeom &a2 = A.g.ax[2];
+        if (ri.interior && j >= a2.p0 && j < a2.p0 + a2.n) return x[ri.xoff + (j - a2.p0) * a2.xs];
+        if (j >= a2.L) return Elem<T>::zero();
+        return resolve_padded<T>(x, A.g, ri.m0, ri.m1, axis_map(a2, j));
     }
-    // data (FWD_DATA / FUSED): zero beyond the padded extent
-    if (j >= A.g.ax[2].L) return Elem<T>::zero();
-    return resolve_padded<T>(A.x, A.g, m0, m1, axis_map(A.g.ax[2], j));
 }
 
 // r2c post-processing: X[k] (k = 0..M) from Z = FFT_M(x[2m] + i x[2m+1])
 template <typename C>
-__device__ void r2c_post(const C *Z, C *X, int64_t M, int nb, int lognb, const C *__restrict__ twF) {
+__device__ void r2c_post(const C *Z, C *X, int M, int nb, int lognb, const C *__restrict__ twF) {
     using R = decltype(Z[0].re);
-    const int64_t total = (M + 1) << lognb;
-    for (int64_t u = threadIdx.x; u < total; u += blockDim.x) {
-        const int b = (int)(u & (nb - 1));
-        const int64_t k = u >> lognb;
-        const C a = Z[(k == M ? 0 : k) * nb + b];
-        const C c = cconj(Z[(k == 0 ? 0 : M - k) * nb + b]);
+    const int total = (M + 1) << lognb;
+    for (int u = threadIdx.x; u < total; u += blockDim.x) {
+        const int b = u & (nb - 1);
+        const int k = u >> lognb;
+        const C a = Z[sx<C>(((k == M ? 0 : k) << lognb) + b)];
+        const C c = cconj(Z[sx<C>(((k == 0 ? 0 : M - k) << lognb) + b)]);
         const C e = C{(R)0.5 * (a.re + c.re), (R)0.5 * (a.im + c.im)};
         const C d = C{(R)0.5 * (a.re - c.re), (R)0.5 * (a.im - c.im)};
         const C o = C{d.im, -d.re};  // -i * d
-        const C w = twF[k];
-        const C wo = cmul(w, o);
-        X[k * nb + b] = C{e.re + wo.re, e.im + wo.im};
+        const C wo = cmul(twF[k], o);
+        X[sx<C>(u)] = C{e.re + wo.re, e.im + wo.im};
     }
 }
 
@@ -247,12 +303,12 @@ __device__ void r2c_post(const C *Z, C *X, int64_t M, int nb, int lognb, const C
 // for the unnormalised length-2M inverse of the Hermitian spectrum X[0..M]
 // (imaginary parts of the DC and Nyquist bins ignored).
 template <typename C>
-__device__ void c2r_pre(const C *X, C *Z, int64_t M, int nb, int lognb, const C *__restrict__ twF) {
-    const int64_t total = M << lognb;
-    for (int64_t u = threadIdx.x; u < total; u += blockDim.x) {
-        const int b = (int)(u & (nb - 1));
-        const int64_t k = u >> lognb;
-        C a = X[k * nb + b], c = X[(M - k) * nb + b];
+__device__ void c2r_pre(const C *X, C *Z, int M, int nb, int lognb, const C *__restrict__ twF) {
+    const int total = M << lognb;
+    for (int u = threadIdx.x; u < total; u += blockDim.x) {
+        const int b = u & (nb - 1);
+        const int k = u >> lognb;
+        C a = X[sx<C>(u)], c = X[sx<C>(((M - k) << lognb) + b)];
         if (k == 0) {
             a.im = 0;
             c.im = 0;
@@ -261,62 +317,83 @@ __device__ void c2r_pre(const C *X, C *Z, int64_t M, int nb, int lognb, const C 
         const C e = cadd(a, c);
         const C d = csub(a, c);
         const C o = cmul(d, cconj(twF[k]));
-        Z[k * nb + b] = C{e.re - o.im, e.im + o.re};  // e + i*o
+        Z[sx<C>(u)] = C{e.re - o.im, e.im + o.re};  // e + i*o
     }
 }
 
-template <typename T>
+template <typename T, int MODE>
 __global__ void __launch_bounds__(256) row_kernel(RowArgs<T> A) {
     using C = typename RowArgs<T>::C;
     using R = typename RowArgs<T>::R;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nb = A.nb, lognb = A.lognb;
-    const int64_t M = A.pl.L;  // transform length
-    const int64_t cap = (A.kind == RK_REAL_EVEN ? M + 1 : M) * nb;
-    C *buf0 = reinterpret_cast<C *>(smem_raw);
+    const int M = A.pl.L;  // transform length
+    const int cap = (int)padded_slots<C>((int64_t)(A.kind == RK_REAL_EVEN ? M + 1 : M) << lognb);
+    RowInfo *rinfo = reinterpret_cast<RowInfo *>(smem_raw);
+    C *buf0 = reinterpret_cast<C *>(smem_raw + ((sizeof(RowInfo) * nb + 15) / 16) * 16);
     C *buf1 = buf0 + cap;
-    int64_t *rinfo = reinterpret_cast<int64_t *>(buf1 + cap);  // per row: m0, m1, t0, t1, i0, i1
+    const int inst = blockIdx.y;
+    const T *__restrict__ x = A.xs ? A.xs[A.inst_base + inst] : A.x;
+    const T *__restrict__ kp = A.ks ? A.ks[A.inst_base + inst] : A.k;
+    T *__restrict__ y = A.ys ? A.ys[A.inst_base + inst] : A.y;
+    C *spec = A.spec + inst * A.spec_is;
+    const C *kspec = A.kspec + inst * A.kspec_is;
     const int64_t rbase = (int64_t)blockIdx.x * nb;
 
     for (int b = threadIdx.x; b < nb; b += blockDim.x) {
         const int64_t r = rbase + b;
-        const int64_t i0 = r / A.n1, i1 = r % A.n1;
-        int64_t *ri = rinfo + 6 * b;
-        ri[4] = i0;
-        ri[5] = i1;
-        if (A.mode == ROW_FWD_DATA || A.mode == ROW_FUSED) {
-            ri[0] = axis_map(A.g.ax[0], i0);
-            ri[1] = axis_map(A.g.ax[1], i1);
-        } else if (A.mode == ROW_FWD_KERNEL) {
-            ri[2] = kbuf_tap(A.g.ax[0], i0, A.reverse);
-            ri[3] = kbuf_tap(A.g.ax[1], i1, A.reverse);
+        const int64_t i0 = r / A.n1, i1 = r - (r / A.n1) * A.n1;
+        RowInfo ri{};
+        ri.valid = r < A.n_rows;
+        ri.soff = i0 * A.spec_s0 + i1 * A.spec_s1;
+        ri.yoff = i0 * A.y_s0 + i1 * A.y_s1;
+        if constexpr (MODE == ROW_FWD_DATA || MODE == ROW_FUSED) {
+            ri.m0 = axis_map(A.g.ax[0], i0);
+            ri.m1 = axis_map(A.g.ax[1], i1);
+            ri.interior = ri.m0 >= 0 && ri.m1 >= 0;
+            ri.xoff = ri.interior ? ri.m0 * A.g.ax[0].xs + ri.m1 * A.g.ax[1].xs : 0;
+        } else if constexpr (MODE == ROW_FWD_KERNEL) {
+            ri.t0 = kbuf_tap(A.g.ax[0], i0, A.reverse);
+            ri.t1 = kbuf_tap(A.g.ax[1], i1, A.reverse);
         }
+        rinfo[b] = ri;
     }
     __syncthreads();
 
-    const bool fwd = (A.mode == ROW_FWD_DATA || A.mode == ROW_FWD_KERNEL || A.mode == ROW_FUSED ||
-                      A.mode == ROW_FWD_PLAIN);
+    constexpr bool fwd = (MODE == ROW_FWD_DATA || MODE == ROW_FWD_KERNEL || MODE == ROW_FUSED ||
+                          MODE == ROW_FWD_PLAIN);
     C *res;
-    if (fwd) {
-        // ---- load samples
-        const int64_t total = M << lognb;
-        for (int64_t u = threadIdx.x; u < total; u += blockDim.x) {
-            const int b = (int)(u / M);
-            const int64_t i = u - (int64_t)b * M;
-            const int64_t r = rbase + b;
-            C v = C{0, 0};
-            if (r < A.n_rows) {
-                const int64_t *ri = rinfo + 6 * b;
-                if (A.kind == RK_REAL_EVEN) {
-                    const T s0 = row_sample(A, ri[0], ri[1], ri[2], ri[3], r, 2 * i);
-                    const T s1 = row_sample(A, ri[0], ri[1], ri[2], ri[3], r, 2 * i + 1);
-                    v = C{RealPart<T>::re(s0), RealPart<T>::re(s1)};
-                } else {
-                    const T s = row_sample(A, ri[0], ri[1], ri[2], ri[3], r, i);
-                    v = C{RealPart<T>::re(s), RealPart<T>::im(s)};
+    if constexpr (fwd) {
+        // ---- load samples: element (b, i) -> buf0[i * nb + b], four independent loads per round
+        const int total = M << lognb;
+        const int T_ = blockDim.x;
+        for (int u0 = threadIdx.x; u0 < total; u0 += 4 * T_) {
+            C v[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int u = u0 + q * T_;
+                v[q] = C{0, 0};
+                if (u < total) {
+                    const int b = u & (nb - 1), i = u >> lognb;
+                    const RowInfo &ri = rinfo[b];
+                    if (ri.valid) {
+                        const int64_t r = rbase + b;
+                        if (A.kind == RK_REAL_EVEN) {
+                            const T s0 = row_sample<MODE>(A, x, kp, ri, r, 2 * (int64_t)i);
+                            const T s1 = row_sample<MODE>(A, x, kp, ri, r, 2 * (int64_t)i + 1);
+                            v[q] = C{RealPart<T>::re(s0), RealPart<T>::re(s1)};
+                        } else {
+                            const T s = row_sample<MODE>(A, x, kp, ri, r, i);
+                            v[q] = C{RealPart<T>::re(s), RealPart<T>::im(s)};
+                        }
+                    }
                 }
             }
-            buf0[i * nb + b] = v;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int u = u0 + q * T_;
+                if (u < total) buf0[sx<C>(u)] = v[q];
+            }
         }
         __syncthreads();
         res = block_fft<false>(buf0, buf1, nb, lognb, A.pl, A.tw);
@@ -328,27 +405,20 @@ __global__ void __launch_bounds__(256) row_kernel(RowArgs<T> A) {
             res = other;
             other = t;
         }
-        if (A.mode != ROW_FUSED) {
-            // store H bins per row
-            const int64_t tot = A.H << lognb;
-            for (int64_t u = threadIdx.x; u < tot; u += blockDim.x) {
-                const int b = (int)(u / A.H);
-                const int64_t k = u - (int64_t)b * A.H;
-                const int64_t r = rbase + b;
-                if (r >= A.n_rows) continue;
-                const int64_t *ri = rinfo + 6 * b;
-                A.spec[ri[4] * A.spec_s0 + ri[5] * A.spec_s1 + k] = res[k * nb + b];
+        const int H = (int)A.H;
+        if constexpr (MODE != ROW_FUSED) {
+            const int tot = H << lognb;
+            for (int u = threadIdx.x; u < tot; u += blockDim.x) {
+                const int b = u & (nb - 1), k = u >> lognb;
+                const RowInfo &ri = rinfo[b];
+                if (ri.valid) spec[ri.soff + k] = res[sx<C>(u)];
             }
             return;
         }
         // ---- fused: multiply by the kernel spectrum, back to the time domain
         {
-            const int64_t tot = A.H << lognb;
-            for (int64_t u = threadIdx.x; u < tot; u += blockDim.x) {
-                const int b = (int)(u & (nb - 1));
-                const int64_t k = u >> lognb;
-                res[k * nb + b] = cmul(res[k * nb + b], A.kspec[k]);
-            }
+            const int tot = H << lognb;
+            for (int u = threadIdx.x; u < tot; u += blockDim.x) res[sx<C>(u)] = cmul(res[sx<C>(u)], kspec[u >> lognb]);
             __syncthreads();
         }
         if (A.kind == RK_REAL_EVEN) {
@@ -360,28 +430,22 @@ __global__ void __launch_bounds__(256) row_kernel(RowArgs<T> A) {
         }
     } else {
         // ---- inverse: load spectrum rows
-        const int64_t tot = A.H << lognb;
+        const int H = (int)A.H;
+        const int tot = H << lognb;
         C *dst = (A.kind == RK_REAL_EVEN) ? buf1 : buf0;
-        for (int64_t u = threadIdx.x; u < tot; u += blockDim.x) {
-            const int b = (int)(u / A.H);
-            const int64_t k = u - (int64_t)b * A.H;
-            const int64_t r = rbase + b;
-            C v = C{0, 0};
-            if (r < A.n_rows) {
-                const int64_t *ri = rinfo + 6 * b;
-                v = A.spec[ri[4] * A.spec_s0 + ri[5] * A.spec_s1 + k];
-            }
-            dst[k * nb + b] = v;
+        for (int u = threadIdx.x; u < tot; u += blockDim.x) {
+            const int b = u & (nb - 1), k = u >> lognb;
+            const RowInfo &ri = rinfo[b];
+            dst[sx<C>(u)] = ri.valid ? spec[ri.soff + k] : C{0, 0};
         }
         __syncthreads();
         if (A.kind == RK_REAL_ODD) {
             // Hermitian extension to the full length (DC imaginary part ignored)
-            const int64_t tot2 = M << lognb;
-            for (int64_t u = threadIdx.x; u < tot2; u += blockDim.x) {
-                const int b = (int)(u & (nb - 1));
-                const int64_t k = u >> lognb;
-                if (k >= A.H) buf0[k * nb + b] = cconj(buf0[(M - k) * nb + b]);
-                else if (k == 0) buf0[b].im = 0;
+            const int tot2 = M << lognb;
+            for (int u = threadIdx.x; u < tot2; u += blockDim.x) {
+                const int b = u & (nb - 1), k = u >> lognb;
+                if (k >= H) buf0[sx<C>(u)] = cconj(buf0[sx<C>(((M - k) << lognb) + b)]);
+                else if (k == 0) buf0[sx<C>(u)].im = 0;
             }
             __syncthreads();
         }
@@ -392,48 +456,48 @@ __global__ void __launch_bounds__(256) row_kernel(RowArgs<T> A) {
         res = block_fft<true>(buf0, buf1, nb, lognb, A.pl, A.tw);
     }
     // ---- store time-domain samples (scaled; cropped + strided for INV_OUT / FUSED)
-    const bool plain = (A.mode == ROW_INV_PLAIN);
-    const int64_t n_out = plain ? A.F : A.out_n;
-    const int64_t tot = n_out << lognb;
-    for (int64_t u = threadIdx.x; u < tot; u += blockDim.x) {
-        const int b = (int)(u / n_out);
-        const int64_t o = u - (int64_t)b * n_out;
-        const int64_t r = rbase + b;
-        if (r >= A.n_rows) continue;
-        const int64_t p = plain ? o : (A.crop_off + o * A.crop_step);
+    constexpr bool plain = (MODE == ROW_INV_PLAIN);
+    const int n_out = (int)(plain ? A.F : A.out_n);
+    const int tot = n_out << lognb;
+    const int coff = (int)A.crop_off, cstep = (int)A.crop_step;
+    for (int u = threadIdx.x; u < tot; u += blockDim.x) {
+        const int b = u & (nb - 1), o = u >> lognb;
+        const RowInfo &ri = rinfo[b];
+        if (!ri.valid) continue;
+        const int p = plain ? o : (coff + o * cstep);
         R vr, vi;
         if (A.kind == RK_REAL_EVEN) {
-            const C z = res[(p >> 1) * nb + b];
+            const C z = res[sx<C>(((p >> 1) << lognb) + b)];
             vr = (p & 1) ? z.im : z.re;
             vi = 0;
         } else {
-            const C z = res[p * nb + b];
+            const C z = res[sx<C>((p << lognb) + b)];
             vr = z.re;
             vi = z.im;
         }
         const T v = make_elem<T>(vr * A.scale, vi * A.scale);
-        if (plain) {
-            A.pout[r * A.F + o] = v;
-        } else {
-            const int64_t *ri = rinfo + 6 * b;
-            A.y[ri[4] * A.y_s0 + ri[5] * A.y_s1 + o] = v;
-        }
+        if constexpr (plain) A.pout[(rbase + b) * A.F + o] = v;
+        else y[ri.yoff + o] = v;
     }
 }
 
 // ---------------------------------------------------------- column pass --
 enum ColMode : int { COL_FWD = 0, COL_INV = 1, COL_FUSED = 2 };
 
+// One pass over a strided axis: columns [h0, h0 + nb) of the contiguous
+// inner extent, outer index blockIdx.y (grid-strided), instance blockIdx.z
+// (buffers inst * src_is / dst_is / k_is elements further).
 template <typename C> struct ColArgs {
     int mode;
     const C *src;
     C *dst;
     int64_t n_inner, n_outer;
     int64_t src_outer, src_axis, dst_outer, dst_axis;
+    int64_t src_is, dst_is;
     int64_t valid_in;
     int64_t crop_off, crop_step, n_out;
     const C *kspec;
-    int64_t k_axis;
+    int64_t k_axis, k_is;
     FftPlanDev pl;
     const C *tw;
     int nb, lognb;
@@ -443,19 +507,31 @@ template <typename C>
 __global__ void __launch_bounds__(256) col_kernel(ColArgs<C> A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nb = A.nb, lognb = A.lognb;
-    const int64_t F = A.pl.L;
+    const int F = A.pl.L;
     C *buf0 = reinterpret_cast<C *>(smem_raw);
-    C *buf1 = buf0 + F * nb;
+    C *buf1 = buf0 + padded_slots<C>((int64_t)F << lognb);
     const int64_t h0 = (int64_t)blockIdx.x * nb;
+    const int inst = blockIdx.z;
+    const int nvalid = (int)(h0 + nb <= A.n_inner ? nb : A.n_inner - h0);
+    const int valid_in = (int)A.valid_in;
+    const int T_ = blockDim.x;
     for (int64_t outer = blockIdx.y; outer < A.n_outer; outer += gridDim.y) {
-        const C *src = A.src + outer * A.src_outer + h0;
-        const int64_t tot_in = F << lognb;
-        for (int64_t u = threadIdx.x; u < tot_in; u += blockDim.x) {
-            const int b = (int)(u & (nb - 1));
-            const int64_t i = u >> lognb;
-            C v = C{0, 0};
-            if (i < A.valid_in && h0 + b < A.n_inner) v = src[i * A.src_axis + b];
-            buf0[u] = v;
+        const C *__restrict__ src = A.src + inst * A.src_is + outer * A.src_outer + h0;
+        const int tot_in = F << lognb;
+        for (int u0 = threadIdx.x; u0 < tot_in; u0 += 4 * T_) {
+            C v[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int u = u0 + q * T_;
+                const int b = u & (nb - 1), i = u >> lognb;
+                v[q] = C{0, 0};
+                if (u < tot_in && i < valid_in && b < nvalid) v[q] = src[i * A.src_axis + b];
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int u = u0 + q * T_;
+                if (u < tot_in) buf0[sx<C>(u)] = v[q];
+            }
         }
         __syncthreads();
         C *res;
@@ -464,25 +540,25 @@ __global__ void __launch_bounds__(256) col_kernel(ColArgs<C> A) {
         } else {
             res = block_fft<false>(buf0, buf1, nb, lognb, A.pl, A.tw);
             if (A.mode == COL_FUSED) {
-                for (int64_t u = threadIdx.x; u < tot_in; u += blockDim.x) {
-                    const int b = (int)(u & (nb - 1));
-                    const int64_t k = u >> lognb;
-                    if (h0 + b < A.n_inner) res[u] = cmul(res[u], A.kspec[k * A.k_axis + h0 + b]);
+                const C *__restrict__ kp = A.kspec + inst * A.k_is + h0;
+                for (int u = threadIdx.x; u < tot_in; u += T_) {
+                    const int b = u & (nb - 1), k = u >> lognb;
+                    if (b < nvalid) res[sx<C>(u)] = cmul(res[sx<C>(u)], kp[k * A.k_axis + b]);
                 }
                 __syncthreads();
                 C *other = (res == buf0) ? buf1 : buf0;
                 res = block_fft<true>(res, other, nb, lognb, A.pl, A.tw);
             }
         }
-        C *dst = A.dst + outer * A.dst_outer + h0;
-        const int64_t n_out = (A.mode == COL_FWD) ? F : A.n_out;
-        const int64_t tot_out = n_out << lognb;
-        for (int64_t u = threadIdx.x; u < tot_out; u += blockDim.x) {
-            const int b = (int)(u & (nb - 1));
-            const int64_t o = u >> lognb;
-            if (h0 + b >= A.n_inner) continue;
-            const int64_t p = (A.mode == COL_FWD) ? o : (A.crop_off + o * A.crop_step);
-            dst[o * A.dst_axis + b] = res[p * nb + b];
+        C *dst = A.dst + inst * A.dst_is + outer * A.dst_outer + h0;
+        const int n_out = (A.mode == COL_FWD) ? F : (int)A.n_out;
+        const int tot_out = n_out << lognb;
+        const int coff = (int)A.crop_off, cstep = (int)A.crop_step;
+        for (int u = threadIdx.x; u < tot_out; u += T_) {
+            const int b = u & (nb - 1), o = u >> lognb;
+            if (b >= nvalid) continue;
+            const int p = (A.mode == COL_FWD) ? o : (coff + o * cstep);
+            dst[o * A.dst_axis + b] = res[sx<C>((p << lognb) + b)];
         }
         __syncthreads();
     }
@@ -516,18 +592,15 @@ int ilog2(int v) {
 }
 
 template <typename K> int ensure_smem(K fn) {
-    static int done = 0;  // one per instantiation
-    if (!done) {
-        NDCONV_CUDA_OK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFftSmemMax));
-        done = 1;
-    }
+    const cudaError_t e = ndconv_allow_smem((const void *)fn, (int)kFftSmemMax);
+    if (e != cudaSuccess) return ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e));
     return NDCONV_OK;
 }
 
 template <typename T> size_t row_smem(const RowArgs<T> &A) {
     using C = typename RowArgs<T>::C;
-    const int64_t cap = (A.kind == RK_REAL_EVEN ? A.pl.L + 1 : A.pl.L) * A.nb;
-    return sizeof(C) * 2 * cap + sizeof(int64_t) * 6 * A.nb;
+    const int64_t cap = padded_slots<C>((A.kind == RK_REAL_EVEN ? A.pl.L + 1 : A.pl.L) * A.nb);
+    return ((sizeof(RowInfo) * A.nb + 15) / 16) * 16 + sizeof(C) * 2 * cap;
 }
 
 // rows per CTA: enough to give each CTA ~2K samples, at least 1
@@ -539,39 +612,55 @@ int pick_nb(int64_t len, int64_t rows, size_t per_row_bytes) {
     return nb;
 }
 
-template <typename T> int launch_row(RowArgs<T> A, cudaStream_t st) {
-    using C = typename RowArgs<T>::C;
-    if (A.n_rows <= 0) return NDCONV_OK;
-    const size_t per_row = sizeof(C) * 2 * (A.pl.L + 1) + sizeof(int64_t) * 6;
-    A.nb = pick_nb(A.pl.L, A.n_rows, per_row);
-    A.lognb = ilog2(A.nb);
-    const size_t sm = row_smem(A);
-    if (sm > kFftSmemMax) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "FFT row length exceeds shared memory");
-    int st_ = ensure_smem(row_kernel<T>);
+// n_inst instances (grid.y); A.spec_is etc. describe their spacing
+template <typename T, int MODE> int launch_row_mode(const RowArgs<T> &A, size_t sm, unsigned grid, int n_inst,
+                                                    cudaStream_t st) {
+    int st_ = ensure_smem(row_kernel<T, MODE>);
     if (st_) return st_;
-    const int64_t grid = (A.n_rows + A.nb - 1) / A.nb;
-    if (grid > 0x7fffffff) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "too many FFT rows");
-    row_kernel<T><<<(unsigned)grid, kThreads, sm, st>>>(A);
+    row_kernel<T, MODE><<<dim3(grid, (unsigned)n_inst), kThreads, sm, st>>>(A);
     ndconv_count_launch();
     NDCONV_CUDA_OK(cudaGetLastError());
     return NDCONV_OK;
 }
 
-template <typename C> int launch_col(ColArgs<C> A, cudaStream_t st) {
-    if (A.n_outer <= 0 || A.n_inner <= 0) return NDCONV_OK;
+// n_inst instances (grid.y); A.spec_is etc. describe their spacing
+template <typename T> int launch_row(RowArgs<T> A, cudaStream_t st, int n_inst = 1) {
+    using C = typename RowArgs<T>::C;
+    if (A.n_rows <= 0 || n_inst <= 0) return NDCONV_OK;
+    const size_t per_row = sizeof(C) * 2 * padded_slots<C>(A.pl.L + 1) + sizeof(RowInfo);
+    A.nb = pick_nb(A.pl.L, A.n_rows, per_row);
+    A.lognb = ilog2(A.nb);
+    const size_t sm = row_smem(A);
+    if (sm > kFftSmemMax) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "FFT row length exceeds shared memory");
+    if (((int64_t)(A.pl.L + 1) << A.lognb) >= (int64_t)1 << 29)
+        return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "FFT row too long");
+    const int64_t grid = (A.n_rows + A.nb - 1) / A.nb;
+    if (grid > 0x7fffffff || n_inst > 65535) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "too many FFT rows");
+    switch (A.mode) {
+    case ROW_FWD_DATA: return launch_row_mode<T, ROW_FWD_DATA>(A, sm, (unsigned)grid, n_inst, st);
+    case ROW_FWD_KERNEL: return launch_row_mode<T, ROW_FWD_KERNEL>(A, sm, (unsigned)grid, n_inst, st);
+    case ROW_INV_OUT: return launch_row_mode<T, ROW_INV_OUT>(A, sm, (unsigned)grid, n_inst, st);
+    case ROW_FUSED: return launch_row_mode<T, ROW_FUSED>(A, sm, (unsigned)grid, n_inst, st);
+    case ROW_FWD_PLAIN: return launch_row_mode<T, ROW_FWD_PLAIN>(A, sm, (unsigned)grid, n_inst, st);
+    default: return launch_row_mode<T, ROW_INV_PLAIN>(A, sm, (unsigned)grid, n_inst, st);
+    }
+}
+
+template <typename C> int launch_col(ColArgs<C> A, cudaStream_t st, int n_inst = 1) {
+    if (A.n_outer <= 0 || A.n_inner <= 0 || n_inst <= 0) return NDCONV_OK;
     const int64_t F = A.pl.L;
     int nb = 1;
     while (nb < 32 && (int64_t)nb * 2 <= A.n_inner + 1 && sizeof(C) * 2 * F * nb * 2 <= 96 * 1024) nb *= 2;
     A.nb = nb;
     A.lognb = ilog2(nb);
-    const size_t sm = sizeof(C) * 2 * F * nb;
+    const size_t sm = sizeof(C) * 2 * padded_slots<C>(F * nb);
     if (sm > kFftSmemMax) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "FFT column length exceeds shared memory");
     int st_ = ensure_smem(col_kernel<C>);
     if (st_) return st_;
     const int64_t gx = (A.n_inner + nb - 1) / nb;
     const int64_t gy = A.n_outer < 65535 ? A.n_outer : 65535;
-    if (gx > 0x7fffffff) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "too many FFT columns");
-    col_kernel<C><<<dim3((unsigned)gx, (unsigned)gy), kThreads, sm, st>>>(A);
+    if (gx > 0x7fffffff || n_inst > 65535) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "too many FFT columns");
+    col_kernel<C><<<dim3((unsigned)gx, (unsigned)gy, (unsigned)n_inst), kThreads, sm, st>>>(A);
     ndconv_count_launch();
     NDCONV_CUDA_OK(cudaGetLastError());
     return NDCONV_OK;
@@ -655,130 +744,160 @@ int Workspace::get(size_t bytes, void **out) {
 }  // namespace
 
 // ------------------------------------------------------------ conv_fft --
-template <typename T>
-int conv_fft_run(const Geom3<T> &g, int reverse, const T *x, const T *k, T *y,
-                 ndconv_fft_processor *proc, cudaStream_t st, void *scratch, size_t scratch_bytes) {
+namespace {
+// Shared plan of one conv_fft geometry.
+template <typename T> struct FftConvPlan {
     using R = typename Elem<T>::Real;
     using C = typename CplxT<R>::type;
+    int64_t P[3], F[3], H;
+    int astar;
+    RowArgs<T> rk;  // row plan (kind, pl, tw, twF, F, H)
+    FftPlanDev pl0, pl1;
+    const C *tw0, *tw1;
+    size_t nK, nS;  // complex elements of Kh and S per instance
+};
+
+template <typename T> int make_conv_plan(const Geom3<T> &g, FftConvPlan<T> &cp) {
+    using C = typename FftConvPlan<T>::C;
     const bool real = !Elem<T>::kComplex;
-    const AxisGeom &A0 = g.ax[0], &A1 = g.ax[1], &A2 = g.ax[2];
-    int64_t P[3] = {A0.L, A1.L, A2.L}, F[3];
-    for (int a = 0; a < 3; a++) F[a] = (P[a] == 1) ? 1 : smooth_size(P[a], real && a == 2);
-    const int astar = F[0] > 1 ? 0 : (F[1] > 1 ? 1 : 2);
-
-    RowArgs<T> rk{};
-    int s = row_plan<T>(F[2], real, rk);
-    if (s) return s;
-    const int64_t H = rk.H;
-    FftPlanDev pl0{}, pl1{};
-    const C *tw0 = nullptr, *tw1 = nullptr;
-    if (F[0] > 1 && (s = plan_with_tw<C>(F[0], pl0, &tw0))) return s;
-    if (F[1] > 1 && (s = plan_with_tw<C>(F[1], pl1, &tw1))) return s;
-
-    // buffers: kernel spectrum Kh[F0][F1][H], data spectrum S[P0][F1][H]
-    const size_t nK = (size_t)F[0] * F[1] * H;
-    const size_t nS = (astar == 2) ? 0 : (size_t)P[0] * F[1] * H;
-    const size_t bytes = sizeof(C) * (nK + nS) + 256;
-    Workspace ws{proc, st};
-    void *base = scratch;
-    if (base) {
-        if (scratch_bytes < bytes) return ndconv_fail(NDCONV_ERR_NO_MEMORY, "scratch too small");
-    } else if ((s = ws.get(bytes, &base))) {
-        return s;
+    for (int a = 0; a < 3; a++) {
+        cp.P[a] = g.ax[a].L;
+        cp.F[a] = (cp.P[a] == 1) ? 1 : smooth_size(cp.P[a], real && a == 2);
     }
-    C *Kh = reinterpret_cast<C *>(base);
-    C *S = Kh + nK;
+    cp.astar = cp.F[0] > 1 ? 0 : (cp.F[1] > 1 ? 1 : 2);
+    cp.rk = RowArgs<T>{};
+    int s = row_plan<T>(cp.F[2], real, cp.rk);
+    if (s) return s;
+    cp.H = cp.rk.H;
+    cp.pl0 = FftPlanDev{};
+    cp.pl1 = FftPlanDev{};
+    cp.tw0 = cp.tw1 = nullptr;
+    if (cp.F[0] > 1 && (s = plan_with_tw<C>(cp.F[0], cp.pl0, &cp.tw0))) return s;
+    if (cp.F[1] > 1 && (s = plan_with_tw<C>(cp.F[1], cp.pl1, &cp.tw1))) return s;
+    cp.nK = (size_t)cp.F[0] * cp.F[1] * cp.H;
+    cp.nS = (cp.astar == 2) ? 0 : (size_t)cp.P[0] * cp.F[1] * cp.H;
+    return NDCONV_OK;
+}
+
+// Instances [base, base + cnt) through all passes; Kh / S hold cnt
+// instances' spectra back to back.  Pointers come from the device arrays
+// xs / ks / ys when given, else x / k / y (cnt == 1).
+template <typename T>
+int conv_fft_wave(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, const T *x, const T *k, T *y,
+                  const T *const *xs, const T *const *ks, T *const *ys, int64_t base, int cnt,
+                  typename FftConvPlan<T>::C *Kh, typename FftConvPlan<T>::C *S, cudaStream_t st) {
+    using R = typename Elem<T>::Real;
+    using C = typename FftConvPlan<T>::C;
+    const AxisGeom &A0 = g.ax[0], &A1 = g.ax[1], &A2 = g.ax[2];
+    const int64_t *P = cp.P, *F = cp.F, H = cp.H;
+    const int64_t K_is = (int64_t)cp.nK, S_is = (int64_t)cp.nS;
+    int s;
 
     // ---- kernel spectrum
-    RowArgs<T> kr = rk;
+    RowArgs<T> kr = cp.rk;
     kr.mode = ROW_FWD_KERNEL;
     kr.g = g;
     kr.k = k;
+    kr.ks = ks;
+    kr.inst_base = base;
     kr.reverse = reverse;
     kr.n1 = A1.keff;
     kr.n_rows = A0.keff * A1.keff;
     kr.spec = Kh;
     kr.spec_s0 = F[1] * H;
     kr.spec_s1 = H;
+    kr.spec_is = K_is;
     kr.scale = 1;
-    if ((s = launch_row(kr, st))) return s;
+    if ((s = launch_row(kr, st, cnt))) return s;
     if (F[1] > 1) {
         ColArgs<C> c{};
         c.mode = COL_FWD;
         c.src = c.dst = Kh;
+        c.src_is = c.dst_is = K_is;
         c.n_inner = H;
         c.n_outer = A0.keff;
         c.src_outer = c.dst_outer = F[1] * H;
         c.src_axis = c.dst_axis = H;
         c.valid_in = A1.keff;
-        c.pl = pl1;
-        c.tw = tw1;
-        if ((s = launch_col(c, st))) return s;
+        c.pl = cp.pl1;
+        c.tw = cp.tw1;
+        if ((s = launch_col(c, st, cnt))) return s;
     }
     if (F[0] > 1) {
         ColArgs<C> c{};
         c.mode = COL_FWD;
         c.src = c.dst = Kh;
+        c.src_is = c.dst_is = K_is;
         c.n_inner = F[1] * H;
         c.n_outer = 1;
         c.src_axis = c.dst_axis = F[1] * H;
         c.valid_in = A0.keff;
-        c.pl = pl0;
-        c.tw = tw0;
-        if ((s = launch_col(c, st))) return s;
+        c.pl = cp.pl0;
+        c.tw = cp.tw0;
+        if ((s = launch_col(c, st, cnt))) return s;
     }
     const R scale = (R)(1.0 / ((double)F[0] * (double)F[1] * (double)F[2]));
 
-    if (astar == 2) {
-        RowArgs<T> fr = rk;
+    if (cp.astar == 2) {
+        RowArgs<T> fr = cp.rk;
         fr.mode = ROW_FUSED;
         fr.g = g;
         fr.x = x;
+        fr.xs = xs;
+        fr.y = y;
+        fr.ys = ys;
+        fr.inst_base = base;
         fr.n1 = 1;
         fr.n_rows = 1;
         fr.kspec = Kh;
-        fr.y = y;
+        fr.kspec_is = K_is;
         fr.y_s0 = 0;
         fr.y_s1 = 0;
         fr.out_n = A2.out;
         fr.crop_off = A2.keff - 1;
         fr.crop_step = A2.s;
         fr.scale = scale;
-        return launch_row(fr, st);
+        return launch_row(fr, st, cnt);
     }
 
     // ---- data: forward row pass into S
-    RowArgs<T> dr = rk;
+    RowArgs<T> dr = cp.rk;
     dr.mode = ROW_FWD_DATA;
     dr.g = g;
     dr.x = x;
+    dr.xs = xs;
+    dr.inst_base = base;
     dr.n1 = P[1];
     dr.n_rows = P[0] * P[1];
     dr.spec = S;
     dr.spec_s0 = F[1] * H;
     dr.spec_s1 = H;
+    dr.spec_is = S_is;
     dr.scale = 1;
-    if ((s = launch_row(dr, st))) return s;
-    if (astar == 0 && F[1] > 1) {
+    if ((s = launch_row(dr, st, cnt))) return s;
+    if (cp.astar == 0 && F[1] > 1) {
         ColArgs<C> c{};
         c.mode = COL_FWD;
         c.src = c.dst = S;
+        c.src_is = c.dst_is = S_is;
         c.n_inner = H;
         c.n_outer = P[0];
         c.src_outer = c.dst_outer = F[1] * H;
         c.src_axis = c.dst_axis = H;
         c.valid_in = P[1];
-        c.pl = pl1;
-        c.tw = tw1;
-        if ((s = launch_col(c, st))) return s;
+        c.pl = cp.pl1;
+        c.tw = cp.tw1;
+        if ((s = launch_col(c, st, cnt))) return s;
     }
     {
         ColArgs<C> c{};
         c.mode = COL_FUSED;
         c.src = c.dst = S;
+        c.src_is = c.dst_is = S_is;
         c.n_outer = 1;
         c.kspec = Kh;
-        if (astar == 0) {
+        c.k_is = K_is;
+        if (cp.astar == 0) {
             c.n_inner = F[1] * H;
             c.src_axis = c.dst_axis = F[1] * H;
             c.valid_in = P[0];
@@ -786,8 +905,8 @@ int conv_fft_run(const Geom3<T> &g, int reverse, const T *x, const T *k, T *y,
             c.crop_off = A0.keff - 1;
             c.crop_step = A0.s;
             c.n_out = A0.out;
-            c.pl = pl0;
-            c.tw = tw0;
+            c.pl = cp.pl0;
+            c.tw = cp.tw0;
         } else {
             c.n_inner = H;
             c.src_axis = c.dst_axis = H;
@@ -796,15 +915,16 @@ int conv_fft_run(const Geom3<T> &g, int reverse, const T *x, const T *k, T *y,
             c.crop_off = A1.keff - 1;
             c.crop_step = A1.s;
             c.n_out = A1.out;
-            c.pl = pl1;
-            c.tw = tw1;
+            c.pl = cp.pl1;
+            c.tw = cp.tw1;
         }
-        if ((s = launch_col(c, st))) return s;
+        if ((s = launch_col(c, st, cnt))) return s;
     }
-    if (astar == 0 && F[1] > 1) {
+    if (cp.astar == 0 && F[1] > 1) {
         ColArgs<C> c{};
         c.mode = COL_INV;
         c.src = c.dst = S;
+        c.src_is = c.dst_is = S_is;
         c.n_inner = H;
         c.n_outer = A0.out;
         c.src_outer = c.dst_outer = F[1] * H;
@@ -813,25 +933,85 @@ int conv_fft_run(const Geom3<T> &g, int reverse, const T *x, const T *k, T *y,
         c.crop_off = A1.keff - 1;
         c.crop_step = A1.s;
         c.n_out = A1.out;
-        c.pl = pl1;
-        c.tw = tw1;
-        if ((s = launch_col(c, st))) return s;
+        c.pl = cp.pl1;
+        c.tw = cp.tw1;
+        if ((s = launch_col(c, st, cnt))) return s;
     }
-    RowArgs<T> ir = rk;
+    RowArgs<T> ir = cp.rk;
     ir.mode = ROW_INV_OUT;
     ir.n1 = A1.out;
     ir.n_rows = A0.out * A1.out;
     ir.spec = S;
     ir.spec_s0 = F[1] * H;
     ir.spec_s1 = H;
+    ir.spec_is = S_is;
     ir.y = y;
+    ir.ys = ys;
+    ir.inst_base = base;
     ir.y_s0 = A1.out * A2.out;
     ir.y_s1 = A2.out;
     ir.out_n = A2.out;
     ir.crop_off = A2.keff - 1;
     ir.crop_step = A2.s;
     ir.scale = scale;
-    return launch_row(ir, st);
+    return launch_row(ir, st, cnt);
+}
+
+// bytes of spectra a wave may keep so that they stay in L2 between passes
+size_t wave_budget_bytes() {
+    static size_t v = 0;
+    if (!v) {
+        const char *e = getenv("NDCONV_WAVE_MB");
+        v = (size_t)((e && atoi(e) > 0) ? atoi(e) : 48) << 20;
+    }
+    return v;
+}
+}  // namespace
+
+template <typename T>
+int conv_fft_run(const Geom3<T> &g, int reverse, const T *x, const T *k, T *y,
+                 ndconv_fft_processor *proc, cudaStream_t st, void *scratch, size_t scratch_bytes) {
+    using C = typename FftConvPlan<T>::C;
+    FftConvPlan<T> cp;
+    int s = make_conv_plan(g, cp);
+    if (s) return s;
+    const size_t bytes = sizeof(C) * (cp.nK + cp.nS) + 256;
+    Workspace ws{proc, st};
+    void *base = scratch;
+    if (base) {
+        if (scratch_bytes < bytes) return ndconv_fail(NDCONV_ERR_NO_MEMORY, "scratch too small");
+    } else if ((s = ws.get(bytes, &base))) {
+        return s;
+    }
+    C *Kh = reinterpret_cast<C *>(base);
+    C *S = Kh + cp.nK;
+    return conv_fft_wave<T>(g, reverse, cp, x, k, y, nullptr, nullptr, nullptr, 0, 1, Kh, S, st);
+}
+
+template <typename T>
+int conv_fft_batch_run(const Geom3<T> &g, int reverse, int64_t n, const T *const *xs, const T *const *ks,
+                       T *const *ys, ndconv_fft_processor *proc, cudaStream_t st) {
+    using C = typename FftConvPlan<T>::C;
+    if (n <= 0) return NDCONV_OK;
+    FftConvPlan<T> cp;
+    int s = make_conv_plan(g, cp);
+    if (s) return s;
+    const size_t per = sizeof(C) * (cp.nK + cp.nS);
+    int64_t W = (int64_t)(wave_budget_bytes() / (per ? per : 1));
+    if (W < 1) W = 1;
+    if (W > n) W = n;
+    if (W > 65535) W = 65535;
+    Workspace ws{proc, st};
+    void *base = nullptr;
+    if ((s = ws.get(per * W + 256, &base))) return s;
+    C *Kh = reinterpret_cast<C *>(base);
+    C *S = Kh + cp.nK * W;
+    for (int64_t b = 0; b < n; b += W) {
+        const int cnt = (int)(n - b < W ? n - b : W);
+        if ((s = conv_fft_wave<T>(g, reverse, cp, nullptr, nullptr, nullptr, xs, ks, ys, b, cnt, Kh, S, st)))
+            return s;
+    }
+    return NDCONV_OK;
 }
 
 template <typename T> size_t conv_fft_scratch_bytes(const Geom3<T> &g) {
@@ -840,7 +1020,7 @@ template <typename T> size_t conv_fft_scratch_bytes(const Geom3<T> &g) {
     const bool real = !Elem<T>::kComplex;
     int64_t P[3] = {g.ax[0].L, g.ax[1].L, g.ax[2].L}, F[3];
     for (int a = 0; a < 3; a++) F[a] = (P[a] == 1) ? 1 : smooth_size(P[a], real && a == 2);
-    const int64_t H = real ? (F[2] % 2 == 0 ? F[2] / 2 + 1 : F[2] / 2 + 1) : F[2];
+    const int64_t H = real ? F[2] / 2 + 1 : F[2];
     const int astar = F[0] > 1 ? 0 : (F[1] > 1 ? 1 : 2);
     const size_t nK = (size_t)F[0] * F[1] * H;
     const size_t nS = (astar == 2) ? 0 : (size_t)P[0] * F[1] * H;
@@ -850,6 +1030,9 @@ template <typename T> size_t conv_fft_scratch_bytes(const Geom3<T> &g) {
 #define NDCONV_INST_FFT(T)                                                                          \
     template int conv_fft_run<T>(const Geom3<T> &, int, const T *, const T *, T *,                \
                                  ndconv_fft_processor *, cudaStream_t, void *, size_t);          \
+    template int conv_fft_batch_run<T>(const Geom3<T> &, int, int64_t, const T *const *,          \
+                                       const T *const *, T *const *, ndconv_fft_processor *,      \
+                                       cudaStream_t);                                              \
     template size_t conv_fft_scratch_bytes<T>(const Geom3<T> &);
 NDCONV_INST_FFT(float)
 NDCONV_INST_FFT(double)

@@ -12,6 +12,11 @@ template <typename T>
 int conv_fft_run(const Geom3<T> &g, int reverse, const T *x, const T *k, T *y,
                  ndconv_fft_processor *proc, cudaStream_t st, void *scratch, size_t scratch_bytes);
 template <typename T> size_t conv_fft_scratch_bytes(const Geom3<T> &g);
+// n instances sharing the geometry; xs / ks / ys are device arrays of n
+// device pointers.  Runs in waves whose spectra fit a share of L2.
+template <typename T>
+int conv_fft_batch_run(const Geom3<T> &g, int reverse, int64_t n, const T *const *xs, const T *const *ks,
+                       T *const *ys, ndconv_fft_processor *proc, cudaStream_t st);
 
 template <typename T>
 int proc_forward(ndconv_fft_processor *proc, int rank, const int64_t *shape, const T *in,

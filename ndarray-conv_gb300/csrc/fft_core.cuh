@@ -1,7 +1,7 @@
 // Shared-memory FFT building blocks (sm_103a).
 //
 // A CTA transforms nb transforms of length L held in shared memory with
-// element (b, i) at buf[i * nb + b] (nb a power of two).  Each stage is a
+// element (b, i) at slot sx(i * nb + b) (nb a power of two).  Each stage is a
 // Stockham autosort radix-R step (no bit reversal), ping-ponging between
 // two buffers: butterfly j reads buf[j + r L/R], applies the twiddles
 // w^(r * (j mod Ns)) with w = exp(-+2 pi i / (Ns R)), does a radix-R DFT in
@@ -20,11 +20,42 @@ template <> struct CplxT<double> { using type = c64; };
 constexpr int kMaxStages = 40;
 constexpr int kMaxGenericRadix = 64;
 
+// n / d for n < 2^31 with a precomputed multiplier: q = umulhi(n, m) >> s
+// (m = ceil(2^(31+t) / d), s = t - 1, t = ceil(log2 d) >= 1; d == 1 is the
+// identity).  Exact for all n < 2^31 because d <= 2^t.
+struct FastDiv {
+    uint32_t d, m, s;
+};
+inline FastDiv make_fastdiv(uint32_t d) {
+    FastDiv f{d, 0, 0};
+    if (d <= 1) return f;
+    uint32_t t = 0;
+    while ((1ull << t) < d) t++;
+    f.m = (uint32_t)(((1ull << (31 + t)) + d - 1) / d);
+    f.s = t - 1;
+    return f;
+}
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
+    return f.d == 1 ? n : (__umulhi(n, f.m) >> f.s);
+}
+
 struct FftPlanDev {
     int L;
     int nst;
     int rad[kMaxStages];
+    FastDiv ns[kMaxStages];  // Ns (product of the previous radices) per stage
 };
+
+// Shared-memory slot of logical element u: one padding slot after every
+// 128-byte wavefront (16 c32 or 8 c64 values), so the stride-R stores of
+// the first Stockham stages spread over all banks.
+template <typename C> __host__ __device__ __forceinline__ int sx(int u) {
+    return u + (u >> (sizeof(C) <= 8 ? 4 : 3));
+}
+// slots needed for n logical elements
+template <typename C> __host__ __device__ __forceinline__ int64_t padded_slots(int64_t n) {
+    return n + (n >> (sizeof(C) <= 8 ? 4 : 3)) + 1;
+}
 
 template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
     return C{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
@@ -76,6 +107,28 @@ template <bool INV, typename C> __device__ __forceinline__ void dft5(C *v) {
     v[2] = cadd(t2, u2);
     v[3] = csub(t2, u2);
 }
+template <bool INV, typename C> __device__ __forceinline__ void dft7(C *v) {
+    using R = decltype(v[0].re);
+    // cos / sin of 2 pi k / 7, k = 1..3
+    const R c1 = (R)0.62348980185873353053, c2 = (R)-0.22252093395631440429, c3 = (R)-0.90096886790241912624;
+    const R s1 = (R)0.78183148246802980871, s2 = (R)0.97492791218182360702, s3 = (R)0.43388373911755812048;
+    const C a0 = v[0];
+    const C b1 = cadd(v[1], v[6]), b2 = cadd(v[2], v[5]), b3 = cadd(v[3], v[4]);
+    const C d1 = csub(v[1], v[6]), d2 = csub(v[2], v[5]), d3 = csub(v[3], v[4]);
+    const C t1 = C{a0.re + c1 * b1.re + c2 * b2.re + c3 * b3.re, a0.im + c1 * b1.im + c2 * b2.im + c3 * b3.im};
+    const C t2 = C{a0.re + c2 * b1.re + c3 * b2.re + c1 * b3.re, a0.im + c2 * b1.im + c3 * b2.im + c1 * b3.im};
+    const C t3 = C{a0.re + c3 * b1.re + c1 * b2.re + c2 * b3.re, a0.im + c3 * b1.im + c1 * b2.im + c2 * b3.im};
+    const C u1 = mul_mi<INV>(C{s1 * d1.re + s2 * d2.re + s3 * d3.re, s1 * d1.im + s2 * d2.im + s3 * d3.im});
+    const C u2 = mul_mi<INV>(C{s2 * d1.re - s3 * d2.re - s1 * d3.re, s2 * d1.im - s3 * d2.im - s1 * d3.im});
+    const C u3 = mul_mi<INV>(C{s3 * d1.re - s1 * d2.re + s2 * d3.re, s3 * d1.im - s1 * d2.im + s2 * d3.im});
+    v[0] = cadd(a0, cadd(b1, cadd(b2, b3)));
+    v[1] = cadd(t1, u1);
+    v[6] = csub(t1, u1);
+    v[2] = cadd(t2, u2);
+    v[5] = csub(t2, u2);
+    v[3] = cadd(t3, u3);
+    v[4] = csub(t3, u3);
+}
 template <bool INV, typename C> __device__ __forceinline__ void dft8(C *v) {
     using R = decltype(v[0].re);
     const R r2 = (R)0.70710678118654752440;
@@ -98,44 +151,49 @@ template <bool INV, typename C> __device__ __forceinline__ void dft8(C *v) {
 }
 
 template <bool INV, typename C>
-__device__ __forceinline__ C twiddle(const C *__restrict__ tw, int64_t e) {
+__device__ __forceinline__ C twiddle(const C *__restrict__ tw, int e) {
     C w = tw[e];
     return INV ? cconj(w) : w;
 }
 
 // One radix-R Stockham stage over nb interleaved transforms.
 template <bool INV, int RAD, typename C>
-__device__ __forceinline__ void stockham_stage(const C *src, C *dst, int L, int nb, int lognb, int Ns,
-                                               const C *__restrict__ tw) {
+__device__ __forceinline__ void stockham_stage(const C *src, C *dst, int L, int nb, int lognb,
+                                               const FastDiv &nsd, const C *__restrict__ tw) {
+    const int Ns = (int)nsd.d;
     const int nr = L / RAD;
     const int twstep = L / (Ns * RAD);
     const int total = nr << lognb;
+#pragma unroll 2
     for (int u = threadIdx.x; u < total; u += blockDim.x) {
         const int b = u & (nb - 1);
         const int j = u >> lognb;
-        const int t = j % Ns;
+        const int q = (int)fdiv((uint32_t)j, nsd);
+        const int t = j - q * Ns;
         C v[RAD];
 #pragma unroll
-        for (int r = 0; r < RAD; r++) v[r] = src[(j + r * nr) * nb + b];
+        for (int r = 0; r < RAD; r++) v[r] = src[sx<C>(((j + r * nr) << lognb) + b)];
         if (t) {
 #pragma unroll
-            for (int r = 1; r < RAD; r++) v[r] = cmul(v[r], twiddle<INV>(tw, (int64_t)t * r * twstep));
+            for (int r = 1; r < RAD; r++) v[r] = cmul(v[r], twiddle<INV>(tw, t * r * twstep));
         }
         if constexpr (RAD == 2) dft2<INV>(v);
         else if constexpr (RAD == 3) dft3<INV>(v);
         else if constexpr (RAD == 4) dft4<INV>(v[0], v[1], v[2], v[3]);
         else if constexpr (RAD == 5) dft5<INV>(v);
+        else if constexpr (RAD == 7) dft7<INV>(v);
         else if constexpr (RAD == 8) dft8<INV>(v);
-        const int base = (j / Ns) * Ns * RAD + t;
+        const int base = q * Ns * RAD + t;
 #pragma unroll
-        for (int r = 0; r < RAD; r++) dst[(base + r * Ns) * nb + b] = v[r];
+        for (int r = 0; r < RAD; r++) dst[sx<C>(((base + r * Ns) << lognb) + b)] = v[r];
     }
 }
 
 // Generic odd-prime radix (O(p^2), runtime p <= kMaxGenericRadix).
 template <bool INV, typename C>
-__device__ void stockham_stage_generic(const C *src, C *dst, int L, int nb, int lognb, int Ns, int RAD,
-                                       const C *__restrict__ tw) {
+__device__ void stockham_stage_generic(const C *src, C *dst, int L, int nb, int lognb, const FastDiv &nsd,
+                                       int RAD, const C *__restrict__ tw) {
+    const int Ns = (int)nsd.d;
     const int nr = L / RAD;
     const int twstep = L / (Ns * RAD);
     const int wstep = L / RAD;  // tw index step for the radix's own roots
@@ -143,41 +201,41 @@ __device__ void stockham_stage_generic(const C *src, C *dst, int L, int nb, int 
     for (int u = threadIdx.x; u < total; u += blockDim.x) {
         const int b = u & (nb - 1);
         const int j = u >> lognb;
-        const int t = j % Ns;
+        const int q = (int)fdiv((uint32_t)j, nsd);
+        const int t = j - q * Ns;
         C v[kMaxGenericRadix];
         for (int r = 0; r < RAD; r++) {
-            C x = src[(j + r * nr) * nb + b];
-            if (t && r) x = cmul(x, twiddle<INV>(tw, (int64_t)t * r * twstep));
+            C x = src[sx<C>(((j + r * nr) << lognb) + b)];
+            if (t && r) x = cmul(x, twiddle<INV>(tw, t * r * twstep));
             v[r] = x;
         }
-        const int base = (j / Ns) * Ns * RAD + t;
+        const int base = q * Ns * RAD + t;
         for (int k = 0; k < RAD; k++) {
             C acc = v[0];
-            for (int m = 1; m < RAD; m++) acc = cadd(acc, cmul(v[m], twiddle<INV>(tw, (int64_t)((m * k) % RAD) * wstep)));
-            dst[(base + k * Ns) * nb + b] = acc;
+            for (int m = 1; m < RAD; m++) acc = cadd(acc, cmul(v[m], twiddle<INV>(tw, ((m * k) % RAD) * wstep)));
+            dst[sx<C>(((base + k * Ns) << lognb) + b)] = acc;
         }
     }
 }
 
 // Full transform of nb interleaved length-L sequences starting in `a`, using
 // `b` as the second buffer.  Returns the buffer holding the result.  Must be
-// called by all threads of the CTA; ends with a barrier.
+// called by all threads of the CTA; ends with a barrier after every stage.
 template <bool INV, typename C>
 __device__ C *block_fft(C *a, C *b, int nb, int lognb, const FftPlanDev &pl, const C *__restrict__ tw) {
     C *src = a, *dst = b;
-    int Ns = 1;
     for (int s = 0; s < pl.nst; s++) {
         const int R = pl.rad[s];
         switch (R) {
-        case 2: stockham_stage<INV, 2>(src, dst, pl.L, nb, lognb, Ns, tw); break;
-        case 3: stockham_stage<INV, 3>(src, dst, pl.L, nb, lognb, Ns, tw); break;
-        case 4: stockham_stage<INV, 4>(src, dst, pl.L, nb, lognb, Ns, tw); break;
-        case 5: stockham_stage<INV, 5>(src, dst, pl.L, nb, lognb, Ns, tw); break;
-        case 8: stockham_stage<INV, 8>(src, dst, pl.L, nb, lognb, Ns, tw); break;
-        default: stockham_stage_generic<INV>(src, dst, pl.L, nb, lognb, Ns, R, tw); break;
+        case 2: stockham_stage<INV, 2>(src, dst, pl.L, nb, lognb, pl.ns[s], tw); break;
+        case 3: stockham_stage<INV, 3>(src, dst, pl.L, nb, lognb, pl.ns[s], tw); break;
+        case 4: stockham_stage<INV, 4>(src, dst, pl.L, nb, lognb, pl.ns[s], tw); break;
+        case 5: stockham_stage<INV, 5>(src, dst, pl.L, nb, lognb, pl.ns[s], tw); break;
+        case 7: stockham_stage<INV, 7>(src, dst, pl.L, nb, lognb, pl.ns[s], tw); break;
+        case 8: stockham_stage<INV, 8>(src, dst, pl.L, nb, lognb, pl.ns[s], tw); break;
+        default: stockham_stage_generic<INV>(src, dst, pl.L, nb, lognb, pl.ns[s], R, tw); break;
         }
         __syncthreads();
-        Ns *= R;
         C *tmp = src;
         src = dst;
         dst = tmp;

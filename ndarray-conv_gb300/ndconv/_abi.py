@@ -79,6 +79,8 @@ def lib():
         "ndconv_conv": (ctypes.c_int, [pp, vp, vp, vp, vp]),
         "ndconv_conv_fft": (ctypes.c_int, [pp, vp, vp, vp, vp, vp]),
         "ndconv_conv_fft_noalloc": (ctypes.c_int, [pp, vp, vp, vp, vp]),
+        "ndconv_conv_batch": (ctypes.c_int, [pp, ctypes.c_int64, vp, vp, vp, vp]),
+        "ndconv_conv_fft_batch": (ctypes.c_int, [pp, ctypes.c_int64, vp, vp, vp, vp, vp]),
         "ndconv_fft_processor_create": (ctypes.c_int, [i32, ctypes.POINTER(vp)]),
         "ndconv_fft_processor_destroy": (ctypes.c_int, [vp]),
         "ndconv_fft_forward": (ctypes.c_int, [vp, i32, i64p, vp, vp, i64p, vp]),

@@ -152,3 +152,51 @@ def get_fft_processor(dtype=torch.float32):
     """get_fft_processor::<T, InElem>() (src/lib.rs:75-77): real dtype -> real
     processor, complex dtype -> complex processor."""
     return FftProcessor(dtype)
+
+
+def _ptr_array(tensors):
+    return torch.tensor([t.data_ptr() for t in tensors], dtype=torch.int64, device=tensors[0].device)
+
+
+def _run_batch(algo, datas, kernels, conv_mode, padding_mode, processor=None, stream=None):
+    """One submission over instances that share shapes, dilation and modes."""
+    L = _abi.lib()
+    if len(datas) != len(kernels) or not datas:
+        raise ValueError("need equally many data and kernel arrays (at least one)")
+    kwd0 = into_kernel_with_dilation(kernels[0])
+    xs = [_to_device(d)[0].contiguous() for d in datas]
+    ks = [_to_device(into_kernel_with_dilation(k).kernel)[0].contiguous() for k in kernels]
+    from .api import KernelWithDilation
+    p = build_problem(dtype_code(xs[0].dtype), tuple(xs[0].shape),
+                      KernelWithDilation(ks[0], kwd0.dilation, kwd0.reverse_flag), conv_mode, padding_mode)
+    for x, k in zip(xs, ks):
+        if tuple(x.shape) != tuple(xs[0].shape) or tuple(k.shape) != tuple(ks[0].shape) or x.dtype != xs[0].dtype:
+            raise ValueError("batched instances must share shapes and element type")
+    shape = (ctypes.c_int64 * 3)()
+    raise_for_status(L.ndconv_output_shape(ctypes.byref(p), algo, shape), p, algo)
+    ys = [torch.empty([shape[i] for i in range(p.rank)], dtype=xs[0].dtype, device=xs[0].device)
+          for _ in xs]
+    px, pk, py = _ptr_array(xs), _ptr_array(ks), _ptr_array(ys)
+    sp = _stream_ptr(stream)
+    n = len(xs)
+    if algo == 0:
+        st = L.ndconv_conv_batch(ctypes.byref(p), n, ctypes.c_void_p(px.data_ptr()), ctypes.c_void_p(pk.data_ptr()),
+                                 ctypes.c_void_p(py.data_ptr()), sp)
+    else:
+        h = processor._handle if processor is not None else None
+        st = L.ndconv_conv_fft_batch(ctypes.byref(p), n, ctypes.c_void_p(px.data_ptr()),
+                                     ctypes.c_void_p(pk.data_ptr()), ctypes.c_void_p(py.data_ptr()), h, sp)
+    raise_for_status(st, p, algo)
+    torch.cuda.current_stream().synchronize() if stream is None else stream.synchronize()
+    return ys
+
+
+def conv_batch(datas, kernels, conv_mode, padding_mode, stream=None):
+    """conv over many instances with one geometry (kernels may carry the
+    same dilation / no_reverse)."""
+    return _run_batch(0, datas, kernels, conv_mode, padding_mode, stream=stream)
+
+
+def conv_fft_batch(datas, kernels, conv_mode, padding_mode, processor=None, stream=None):
+    """conv_fft over many instances with one geometry, L2-sized waves."""
+    return _run_batch(1, datas, kernels, conv_mode, padding_mode, processor=processor, stream=stream)

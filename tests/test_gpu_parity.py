@@ -302,3 +302,49 @@ def test_c2_i32_bitexact():
     assert st == 0
     y = ndconv.conv(x, kw, mode, pm)
     assert np.array_equal(y, yo)
+
+
+# ---- batched submissions equal per-instance calls -------------------------------------------
+@pytest.mark.parametrize("algo", ["direct", "fft"])
+@pytest.mark.parametrize("cfg", [
+    ((64, 300), (5, 9), 2, ConvMode.Same, PaddingMode.Custom([BorderType.Reflect, BorderType.Circular]), "float32"),
+    ((6, 30, 40), (3, 4, 5), 1, ConvMode.Full, PaddingMode.Replicate, "complex64"),
+    ((5000,), (31,), 1, ConvMode.Full, PaddingMode.Zeros, "float32"),
+    ((50, 60), (7, 7), 1, ConvMode.Custom([2, 3], [2, 3]), PaddingMode.Circular, "float64"),
+])
+def test_batch_equals_single(algo, cfg):
+    import torch
+    xs_, ks_, dil, mode, pm, dt = cfg
+    tdt = getattr(torch, dt)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    n = 7
+    if tdt.is_complex:
+        xs = [torch.randn(xs_, generator=g, device="cuda", dtype=tdt) for _ in range(n)]
+        ks = [torch.randn(ks_, generator=g, device="cuda", dtype=tdt) for _ in range(n)]
+    else:
+        xs = [torch.rand(xs_, generator=g, device="cuda", dtype=tdt) for _ in range(n)]
+        ks = [torch.rand(ks_, generator=g, device="cuda", dtype=tdt) for _ in range(n)]
+    kws = [with_dilation(k, dil) for k in ks]
+    fb = ndconv.conv_batch if algo == "direct" else ndconv.conv_fft_batch
+    f1 = ndconv.conv if algo == "direct" else ndconv.conv_fft
+    yb = fb(xs, kws, mode, pm)
+    for i in range(n):
+        y1 = f1(xs[i], kws[i], mode, pm)
+        assert torch.equal(yb[i], y1), i
+    # and one instance against the f64 oracle
+    x0, k0 = xs[0].cpu().numpy(), ks[0].cpu().numpy()
+    y64 = _oracle64(x0, with_dilation(k0, dil), mode, pm)
+    assert normwise_err(yb[0].cpu().numpy(), y64) <= TOL32
+
+
+def test_batch_i32_bitexact():
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(9)
+    xs = [torch.randint(-100, 101, (200, 500), generator=g, device="cuda", dtype=torch.int32) for _ in range(5)]
+    ks = [torch.randint(-100, 101, (11, 31), generator=g, device="cuda", dtype=torch.int32) for _ in range(5)]
+    mode, pm = ConvMode.Same, PaddingMode.Custom([BorderType.Reflect, BorderType.Circular])
+    ys = ndconv.conv_batch(xs, [with_dilation(k, 2) for k in ks], mode, pm)
+    for x, k, y in zip(xs, ks, ys):
+        p = problem(I32, x.cpu().numpy(), with_dilation(k.cpu().numpy(), 2), mode, pm)
+        st, yo = O.conv(p, x.cpu().numpy(), k.cpu().numpy())
+        assert st == 0 and np.array_equal(y.cpu().numpy(), yo)
