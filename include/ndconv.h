@@ -101,6 +101,7 @@ typedef struct ndconv_problem {
 } ndconv_problem;
 
 typedef struct ndconv_fft_processor ndconv_fft_processor;
+typedef struct ndconv_batch_plan ndconv_batch_plan;
 
 /* Output shape and argument checks, host only (no device work).
  * algo: 0 = direct (ConvExt::conv), 1 = FFT (ConvFFTExt::conv_fft); the two
@@ -133,6 +134,28 @@ int ndconv_conv_batch(const ndconv_problem *p, int64_t n, const void *const *dat
 int ndconv_conv_fft_batch(const ndconv_problem *p, int64_t n, const void *const *data,
                           const void *const *kernel, void *const *out, ndconv_fft_processor *proc,
                           void *stream);
+
+/* Heterogeneous batch: n independent problems (any shapes, kernels, modes,
+ * element types), each run by the direct (algo[i] = 0) or FFT (1)
+ * algorithm.  No counterpart in the reference (its calls are one instance
+ * at a time).  data / kernel / out are HOST arrays of n device pointers,
+ * bound at creation.  f32 instances become tasks of one persistent kernel
+ * driven by a device-side work queue; others run as ordinary launches in
+ * the same submission.  The plan owns all spectra (allocated once). */
+int ndconv_batch_create(const ndconv_problem *problems, int64_t n, const int32_t *algo,
+                        const void *const *data, const void *const *kernel, void *const *out,
+                        ndconv_batch_plan **plan);
+/* Run the batch on stream; use_graph = 1 captures the submission into a
+ * CUDA graph on first use and replays it afterwards. */
+int ndconv_batch_run(ndconv_batch_plan *plan, int32_t use_graph, void *stream);
+/* The same instances, one per-instance entry point call each (the plain
+ * drop-in path), for comparison. */
+int ndconv_batch_run_plain(ndconv_batch_plan *plan, void *stream);
+/* Synchronises stream; NDCONV_ERR_TIMEOUT if a queue wait ran out. */
+int ndconv_batch_status(ndconv_batch_plan *plan, void *stream);
+/* tasks, grid, shared bytes, #FFT, #direct, #standalone, workspace bytes, counters */
+int ndconv_batch_info(const ndconv_batch_plan *plan, int64_t info[8]);
+int ndconv_batch_destroy(ndconv_batch_plan *plan);
 
 /* ndconv_conv_fft for callers that cannot allocate device memory (inside
  * a CUDA graph being captured, hosts that forbid allocation after start-up,
@@ -171,6 +194,13 @@ int ndconv_fft_backward(ndconv_fft_processor *proc, int32_t rank, const int64_t 
 /* Number of CUDA kernels this library has launched in this process.
  * Diagnostics only; no counterpart in the reference. */
 uint64_t ndconv_kernel_launches(void);
+
+/* Planning facts for one problem (host only): out[0] modelled direct time
+ * (s), out[1] modelled FFT time (s, 1e30 when the FFT passes do not fit a
+ * persistent-kernel CTA), out[2] direct MACs, out[3] algorithmic bytes,
+ * out[4..6] FFT lengths, out[7] 1 if the FFT fits.  No counterpart in the
+ * reference; used by dispatchers. */
+int ndconv_plan_info(const ndconv_problem *p, double out[8]);
 
 /* Message for the last non-OK status returned on this thread. */
 const char *ndconv_last_error(void);

@@ -251,13 +251,26 @@ extern "C" int ndconv_conv_fft(const ndconv_problem *p, const void *data, const 
     if (s) return s;
     if (!data || !kernel || !out) return ndconv_fail(NDCONV_ERR_INVALID, "null pointer");
     cudaStream_t st = (cudaStream_t)stream;
+    int s2 = NDCONV_OK;
     switch (P.dtype) {
-    case NDCONV_F32: return conv_fft_run<float>(P.geom<float>(), P.reverse, (const float *)data, (const float *)kernel, (float *)out, proc, st, nullptr, 0);
-    case NDCONV_F64: return conv_fft_run<double>(P.geom<double>(), P.reverse, (const double *)data, (const double *)kernel, (double *)out, proc, st, nullptr, 0);
-    case NDCONV_C32: return conv_fft_run<c32>(P.geom<c32>(), P.reverse, (const c32 *)data, (const c32 *)kernel, (c32 *)out, proc, st, nullptr, 0);
-    case NDCONV_C64: return conv_fft_run<c64>(P.geom<c64>(), P.reverse, (const c64 *)data, (const c64 *)kernel, (c64 *)out, proc, st, nullptr, 0);
+    case NDCONV_F32: s2 = conv_fft_run<float>(P.geom<float>(), P.reverse, (const float *)data, (const float *)kernel, (float *)out, proc, st, nullptr, 0); break;
+    case NDCONV_F64: s2 = conv_fft_run<double>(P.geom<double>(), P.reverse, (const double *)data, (const double *)kernel, (double *)out, proc, st, nullptr, 0); break;
+    case NDCONV_C32: s2 = conv_fft_run<c32>(P.geom<c32>(), P.reverse, (const c32 *)data, (const c32 *)kernel, (c32 *)out, proc, st, nullptr, 0); break;
+    case NDCONV_C64: s2 = conv_fft_run<c64>(P.geom<c64>(), P.reverse, (const c64 *)data, (const c64 *)kernel, (c64 *)out, proc, st, nullptr, 0); break;
     default: return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "integer FFT convolution is not supported (documented broken upstream)");
     }
+    if (s2 != NDCONV_ERR_UNSUPPORTED) return s2;
+    // FFT lengths beyond one CTA's shared memory: the same convolution by the
+    // direct kernel (results within the FFT path's tolerance)
+    cudaError_t e = cudaSuccess;
+    switch (P.dtype) {
+    case NDCONV_F32: e = direct_conv_launch<float>((const float *)data, (const float *)kernel, (float *)out, P.direct<float>(), st, 0); break;
+    case NDCONV_F64: e = direct_conv_launch<double>((const double *)data, (const double *)kernel, (double *)out, P.direct<double>(), st, 0); break;
+    case NDCONV_C32: e = direct_conv_launch<c32>((const c32 *)data, (const c32 *)kernel, (c32 *)out, P.direct<c32>(), st, 0); break;
+    default: e = direct_conv_launch<c64>((const c64 *)data, (const c64 *)kernel, (c64 *)out, P.direct<c64>(), st, 0); break;
+    }
+    if (e != cudaSuccess) return ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e));
+    return NDCONV_OK;
 }
 
 extern "C" int ndconv_conv_batch(const ndconv_problem *p, int64_t n, const void *const *data,

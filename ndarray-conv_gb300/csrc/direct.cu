@@ -11,402 +11,11 @@
 // (src/dilation/mod.rs:47-50); the skip is warp-uniform.
 #include "common.cuh"
 #include "direct.h"
+#include "direct_blocks.cuh"
 
 namespace ndconv {
 
-template <typename T, int RX>
-__global__ void __launch_bounds__(256) direct_tile_kernel(const T *__restrict__ x0,
-                                                          const T *__restrict__ k0,
-                                                          T *__restrict__ y0, DirectParams<T> P) {
-    using E = Elem<T>;
-    using Acc = typename E::Acc;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    // grid.z enumerates (instance, output plane)
-    const int64_t inst = blockIdx.z / P.g.ax[0].out;
-    const T *__restrict__ x = P.xs ? P.xs[P.inst_base + inst] : x0;
-    const T *__restrict__ k = P.ks ? P.ks[P.inst_base + inst] : k0;
-    T *__restrict__ y = P.ys ? P.ys[P.inst_base + inst] : y0;
-    const Geom3<T> &g = P.g;
-    const AxisGeom &A0 = g.ax[0], &A1 = g.ax[1], &A2 = g.ax[2];
-    const int BX = blockDim.x, BY = blockDim.y;
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int tid = ty * BX + tx, nthr = BX * BY;
-    const int TX = BX * RX;
-
-    T *tile = reinterpret_cast<T *>(smem_raw);
-    T *wsm = tile + P.tile_elems;
-    int64_t *mrow = reinterpret_cast<int64_t *>(smem_raw + P.maps_off);
-    int64_t *mcol = mrow + P.max_rows;
-
-    const int64_t oz = blockIdx.z - inst * A0.out;
-    const int64_t oy0 = (int64_t)blockIdx.y * BY;
-    const int64_t ox0 = (int64_t)blockIdx.x * TX;
-
-    Acc acc[RX];
-#pragma unroll
-    for (int r = 0; r < RX; r++) acc[r] = E::zero();
-
-    const int64_t s1 = A1.s, s2 = A2.s, d1 = A1.d, d2 = A2.d;
-    for (int64_t kz = 0; kz < A0.K; kz++) {
-        const int64_t mz = axis_map(A0, oz * A0.s + kz * A0.d);
-        const int64_t kzs = tap_source(kz, A0.K, P.reverse);
-        for (int64_t ky0 = 0; ky0 < A1.K; ky0 += P.cky) {
-            const int cky = (int)(P.cky < A1.K - ky0 ? P.cky : A1.K - ky0);
-            const int64_t row0 = oy0 * s1 + ky0 * d1;
-            const int nrows = (int)((BY - 1) * s1 + (cky - 1) * d1 + 1);
-            for (int64_t kx0 = 0; kx0 < A2.K; kx0 += P.ckx) {
-                const int ckx = (int)(P.ckx < A2.K - kx0 ? P.ckx : A2.K - kx0);
-                const int64_t col0 = ox0 * s2 + kx0 * d2;
-                const int ncols = (int)((TX - 1) * s2 + (ckx - 1) * d2 + 1);
-                __syncthreads();  // previous chunk's compute is done with smem
-                for (int i = tid; i < nrows; i += nthr) mrow[i] = axis_map(A1, row0 + i);
-                for (int i = tid; i < ncols; i += nthr) mcol[i] = axis_map(A2, col0 + i);
-                for (int i = tid; i < cky * ckx; i += nthr) {
-                    const int a = i / ckx, b = i - a * ckx;
-                    const int64_t ys = tap_source(ky0 + a, A1.K, P.reverse);
-                    const int64_t xs_ = tap_source(kx0 + b, A2.K, P.reverse);
-                    wsm[i] = k[kzs * A0.ks + ys * A1.ks + xs_ * A2.ks];
-                }
-                __syncthreads();
-                const int W = ncols;
-                for (int i = tid; i < nrows * ncols; i += nthr) {
-                    const int r = i / ncols, c = i - r * ncols;
-                    tile[r * W + c] = resolve_padded<T>(x, g, mz, mrow[r], mcol[c]);
-                }
-                __syncthreads();
-                const int is1 = (int)s1, id1 = (int)d1, is2 = (int)s2, id2 = (int)d2;
-                for (int a = 0; a < cky; a++) {
-                    const T *trow = tile + (ty * is1 + a * id1) * W + tx * is2;
-                    for (int b = 0; b < ckx; b++) {
-                        const T w = wsm[a * ckx + b];
-                        if (E::is_zero(w)) continue;
-                        const T *tp = trow + b * id2;
-#pragma unroll
-                        for (int r = 0; r < RX; r++) E::mac(acc[r], tp[r * BX * is2], w);
-                    }
-                }
-            }
-        }
-    }
-    const int64_t oy = oy0 + ty;
-    if (oy < A1.out) {
-        T *yrow = y + (oz * A1.out + oy) * A2.out;
-#pragma unroll
-        for (int r = 0; r < RX; r++) {
-            const int64_t ox = ox0 + tx + (int64_t)r * BX;
-            if (ox < A2.out) yrow[ox] = E::out(acc[r]);
-        }
-    }
-}
-
-// Sliding-window variant for unit stride along the contiguous axis
-// (s_x == 1, any dilation d_x <= 8).  Output ox = X0 + phi + j d_x reads
-// input X0 + phi + (j + t) d_x for tap t, so each phase phi of the row is an
-// undilated 1-D correlation over the decimated sequence D_phi[m] =
-// row[phi + m d_x].  A warp owns one (output row, phase, segment) line of
-// 32 * RX outputs; lane l owns RX consecutive phase outputs j = l*RX + r and
-// slides a register window over D_phi, so each shared-memory load feeds up
-// to CKX FMAs.  D_phi is stored swizzled (element m at (m % RX) * Q + m / RX)
-// so the lanes' window loads hit consecutive banks.
-template <typename T, int RX, int CKX>
-__global__ void __launch_bounds__(256) direct_sw_kernel(const T *__restrict__ x0, const T *__restrict__ k0,
-                                                        T *__restrict__ y0, DirectParams<T> P) {
-    using E = Elem<T>;
-    using Acc = typename E::Acc;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const AxisGeom &A0 = P.g.ax[0], &A1 = P.g.ax[1], &A2 = P.g.ax[2];
-    const int64_t inst = blockIdx.z / A0.out;
-    const T *__restrict__ x = P.xs ? P.xs[P.inst_base + inst] : x0;
-    const T *__restrict__ k = P.ks ? P.ks[P.inst_base + inst] : k0;
-    T *__restrict__ y = P.ys ? P.ys[P.inst_base + inst] : y0;
-    const int D = (int)A2.d;            // phases
-    const int TY = P.sw_ty, NSEG = P.sw_nseg;
-    const int SEGW = 32 * RX;           // phase outputs per line
-    const int Q = P.sw_q;               // swizzle pitch
-    const int PH = RX * Q;              // smem elements per phase of one row
-    const int ROWE = D * PH;            // smem elements per staged row
-    T *tile = reinterpret_cast<T *>(smem_raw);
-    T *wsm = tile + P.tile_elems;
-    int64_t *mrow = reinterpret_cast<int64_t *>(smem_raw + P.maps_off);
-    int64_t *mcol = mrow + P.max_rows;
-    int64_t *rowoff = mcol + P.max_cols;
-    int *zrow = reinterpret_cast<int *>(rowoff + P.max_rows);
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int nlines = TY * NSEG * D;
-    const int ty = warp / (NSEG * D);
-    const int sg = (warp / D) % NSEG;
-    const int phi = warp % D;
-    const int64_t oz = blockIdx.z - inst * A0.out;
-    const int64_t oy0 = (int64_t)blockIdx.y * TY;
-    const int64_t TXo = (int64_t)NSEG * D * SEGW;
-    const int64_t X0 = (int64_t)blockIdx.x * TXo;
-    const int s1 = (int)A1.s, d1 = (int)A1.d;
-
-    Acc acc[RX];
-#pragma unroll
-    for (int r = 0; r < RX; r++) acc[r] = E::zero();
-
-    for (int64_t kz = 0; kz < A0.K; kz++) {
-        const int64_t mz = axis_map(A0, oz * A0.s + kz * A0.d);
-        const int64_t kzs = tap_source(kz, A0.K, P.reverse);
-        for (int64_t ky0 = 0; ky0 < A1.K; ky0 += P.cky) {
-            const int cky = (int)(P.cky < A1.K - ky0 ? P.cky : A1.K - ky0);
-            const int64_t row0 = oy0 * s1 + ky0 * d1;
-            const int nrows = (TY - 1) * s1 + (cky - 1) * d1 + 1;
-            for (int64_t kx0 = 0; kx0 < A2.K; kx0 += P.ckx) {
-                const int ckx = (int)(P.ckx < A2.K - kx0 ? P.ckx : A2.K - kx0);
-                const int64_t col0 = X0 + kx0 * D;
-                const int mlen = NSEG * SEGW + ckx - 1;  // decimated elements per phase
-                const int ncols = D * mlen;
-                __syncthreads();
-                // per staged row: data offset of an interior row, or -1 (then the
-                // general border resolution is used); per column: mapped index
-                for (int i = tid; i < nrows; i += blockDim.x) {
-                    const int64_t my = axis_map(A1, row0 + i);
-                    mrow[i] = my;
-                    rowoff[i] = (mz >= 0 && my >= 0) ? mz * A0.xs + my * A1.xs : -1;
-                }
-                for (int i = tid; i < ncols; i += blockDim.x) mcol[i] = axis_map(A2, col0 + i);
-                for (int i = tid; i < cky; i += blockDim.x) zrow[i] = 0;
-                __syncthreads();
-                for (int i = tid; i < cky * ckx; i += blockDim.x) {
-                    const int a = i / ckx, b = i - a * ckx;
-                    const T w = k[kzs * A0.ks + tap_source(ky0 + a, A1.K, P.reverse) * A1.ks +
-                                  tap_source(kx0 + b, A2.K, P.reverse) * A2.ks];
-                    wsm[i] = w;
-                    if (E::is_zero(w)) zrow[a] = 1;  // this kernel row has taps to skip
-                }
-                __syncthreads();
-                const int64_t xs2 = A2.xs;
-                for (int rr = 0; rr < nrows; rr++) {
-                    const int64_t ro = rowoff[rr];
-                    T *trow = tile + rr * ROWE;
-                    for (int cc = tid; cc < ncols; cc += blockDim.x) {
-                        const int64_t mc = mcol[cc];
-                        const T v = (ro >= 0 && mc >= 0) ? x[ro + mc * xs2]
-                                                         : resolve_padded<T>(x, P.g, mz, mrow[rr], mc);
-                        const int ph = (D == 1) ? 0 : cc % D;
-                        const int m = (D == 1) ? cc : cc / D;
-                        trow[ph * PH + (m & (RX - 1)) * Q + m / RX] = v;
-                    }
-                }
-                __syncthreads();
-                if (warp < nlines) {
-                    // lane's first decimated element is a multiple of RX, and so is
-                    // every chunk start t0, so element jbase + t0 + q sits at
-                    // (q % RX) * Q + (jbase + t0) / RX + q / RX
-                    const int lbase = sg * (SEGW / RX) + lane;
-                    for (int a = 0; a < cky; a++) {
-                        const T *prow = tile + (ty * s1 + a * d1) * ROWE + phi * PH + lbase;
-                        const T *wrow = wsm + a * ckx;
-                        for (int t0 = 0; t0 < ckx; t0 += CKX) {
-                            T win[RX + CKX - 1];
-                            const T *pw = prow + t0 / RX;
-#pragma unroll
-                            for (int q = 0; q < RX + CKX - 1; q++)
-                                win[q] = (t0 + q < ckx + RX - 1) ? pw[(q % RX) * Q + q / RX] : E::zero();
-                            if (t0 + CKX <= ckx && !zrow[a]) {
-                                // full chunk without zero taps: no per-tap branches
-#pragma unroll
-                                for (int t = 0; t < CKX; t++) {
-                                    const T w = wrow[t0 + t];
-#pragma unroll
-                                    for (int r = 0; r < RX; r++) E::mac(acc[r], win[r + t], w);
-                                }
-                            } else {
-#pragma unroll
-                                for (int t = 0; t < CKX; t++) {
-                                    if (t0 + t < ckx) {
-                                        const T w = wrow[t0 + t];
-                                        if (!E::is_zero(w)) {
-#pragma unroll
-                                            for (int r = 0; r < RX; r++) E::mac(acc[r], win[r + t], w);
-                                        }
-                                    }
-                                }
-                            }
-                        }
-                    }
-                }
-            }
-        }
-    }
-    if (warp < nlines) {
-        const int64_t oy = oy0 + ty;
-        if (oy < A1.out) {
-            T *yrow = y + (oz * A1.out + oy) * A2.out;
-#pragma unroll
-            for (int r = 0; r < RX; r++) {
-                const int64_t ox = X0 + phi + (int64_t)(sg * SEGW + lane * RX + r) * D;
-                if (ox < A2.out) yrow[ox] = E::out(acc[r]);
-            }
-        }
-    }
-}
-
-// One thread per output, reading the data through the border map with no
-// staging.  Used when a tile would not fit in shared memory (very large
-// strides); correct for every geometry.
-template <typename T>
-__global__ void __launch_bounds__(256) direct_naive_kernel(const T *__restrict__ x0,
-                                                           const T *__restrict__ k0,
-                                                           T *__restrict__ y0, DirectParams<T> P) {
-    using E = Elem<T>;
-    using Acc = typename E::Acc;
-    const int64_t inst = blockIdx.y;
-    const T *__restrict__ x = P.xs ? P.xs[P.inst_base + inst] : x0;
-    const T *__restrict__ k = P.ks ? P.ks[P.inst_base + inst] : k0;
-    T *__restrict__ y = P.ys ? P.ys[P.inst_base + inst] : y0;
-    const Geom3<T> &g = P.g;
-    const AxisGeom &A0 = g.ax[0], &A1 = g.ax[1], &A2 = g.ax[2];
-    const int64_t total = A0.out * A1.out * A2.out;
-    for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < total;
-         o += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t ox = o % A2.out, oy = (o / A2.out) % A1.out, oz = o / (A2.out * A1.out);
-        Acc acc = E::zero();
-        for (int64_t kz = 0; kz < A0.K; kz++) {
-            const int64_t mz = axis_map(A0, oz * A0.s + kz * A0.d);
-            const int64_t kzs = tap_source(kz, A0.K, P.reverse);
-            for (int64_t ky = 0; ky < A1.K; ky++) {
-                const int64_t my = axis_map(A1, oy * A1.s + ky * A1.d);
-                const int64_t kys = tap_source(ky, A1.K, P.reverse);
-                for (int64_t kx = 0; kx < A2.K; kx++) {
-                    const T w = k[kzs * A0.ks + kys * A1.ks + tap_source(kx, A2.K, P.reverse) * A2.ks];
-                    if (E::is_zero(w)) continue;
-                    const int64_t mx = axis_map(A2, ox * A2.s + kx * A2.d);
-                    E::mac(acc, resolve_padded<T>(x, g, mz, my, mx), w);
-                }
-            }
-        }
-        y[o] = E::out(acc);
-    }
-}
-
-namespace {
-constexpr int kMaxCols = 2048;
-constexpr size_t kSmemBudget = 96 * 1024;
-
-template <typename T> size_t smem_bytes(const DirectParams<T> &P) {
-    // row maps, column maps, row data offsets and per-row zero-tap flags
-    // (the last two used by the sliding-window kernel)
-    return (size_t)P.maps_off + sizeof(int64_t) * (2 * P.max_rows + P.max_cols) + sizeof(int) * P.cky;
-}
-
-// Pick block shape and tap chunks so the staged window fits in shared
-// memory; returns false when no tile fits (naive kernel then).
-template <typename T> bool plan_tile(DirectParams<T> &P, int RX, int &BX, int &BY) {
-    const AxisGeom &A1 = P.g.ax[1], &A2 = P.g.ax[2];
-    // rows of output per CTA: few when the plane has few rows
-    static const int shapes[4][2] = {{32, 8}, {64, 4}, {128, 2}, {256, 1}};
-    int pick = 3;
-    if (A1.out >= 8) pick = 0;
-    else if (A1.out >= 4) pick = 1;
-    else if (A1.out >= 2) pick = 2;
-    for (; pick < 4; pick++) {
-        BX = shapes[pick][0];
-        BY = shapes[pick][1];
-        const int64_t TX = (int64_t)BX * RX;
-        const int64_t base_cols = (TX - 1) * A2.s + 1;
-        if (base_cols > kMaxCols) continue;
-        int64_t ckx = A2.K;
-        if (base_cols + (ckx - 1) * A2.d > kMaxCols) ckx = (kMaxCols - base_cols) / A2.d + 1;
-        if (ckx < 1) continue;
-        const int64_t W = base_cols + (ckx - 1) * A2.d;
-        const int64_t base_rows = (int64_t)(BY - 1) * A1.s + 1;
-        // largest cky whose window fits the budget
-        int64_t cky = A1.K;
-        auto bytes = [&](int64_t c) {
-            const int64_t rows = base_rows + (c - 1) * A1.d;
-            return sizeof(T) * (rows * W + c * ckx) + 16 + sizeof(int64_t) * (rows + W);
-        };
-        while (cky > 1 && bytes(cky) > kSmemBudget) cky = (cky + 1) / 2;
-        if (bytes(cky) > kSmemBudget) continue;
-        P.cky = cky;
-        P.ckx = ckx;
-        P.max_rows = base_rows + (cky - 1) * A1.d;
-        P.max_cols = W;
-        P.tile_elems = P.max_rows * W;
-        P.w_elems = cky * ckx;
-        P.maps_off = ((int64_t)sizeof(T) * (P.tile_elems + P.w_elems) + 15) / 16 * 16;
-        return true;
-    }
-    return false;
-}
-
-// Sliding-window tiling: warps = TY rows x NSEG segments x D phases (<= 8).
-template <typename T> bool plan_sw(DirectParams<T> &P, int RX) {
-    const AxisGeom &A1 = P.g.ax[1], &A2 = P.g.ax[2];
-    if (A2.s != 1 || A2.d > 8) return false;
-    const int D = (int)A2.d;
-    const int lines = 8 / D;
-    int TY = 1;
-    while (TY * 2 <= lines && TY * 2 <= A1.out) TY *= 2;
-    const int SEGW = 32 * RX;
-    int NSEG = lines / TY;
-    const int64_t segs_needed = (A2.out + (int64_t)D * SEGW - 1) / ((int64_t)D * SEGW);
-    if (NSEG > segs_needed) NSEG = (int)(segs_needed < 1 ? 1 : segs_needed);
-    auto geom = [&](int64_t ckx, int64_t cky, int &Q, int64_t &rows, int64_t &cols, int64_t &rowe) {
-        Q = (int)((NSEG * SEGW + ckx - 1 + RX - 1) / RX);
-        rowe = (int64_t)D * RX * Q;
-        rows = (TY - 1) * A1.s + (cky - 1) * A1.d + 1;
-        cols = (int64_t)D * (NSEG * SEGW + ckx - 1);
-        return sizeof(T) * (rows * rowe + cky * ckx) + 16 + sizeof(int64_t) * (2 * rows + cols) +
-               sizeof(int) * cky;
-    };
-    int Q;
-    int64_t rows, cols, rowe;
-    // taps per staged chunk along x: all of them if a single kernel row fits
-    int64_t ckx = A2.K;
-    while (ckx > 1 && geom(ckx, 1, Q, rows, cols, rowe) > kSmemBudget) ckx = (ckx + 1) / 2;
-    if (geom(ckx, 1, Q, rows, cols, rowe) > kSmemBudget) return false;
-    int64_t cky = A1.K;
-    while (cky > 1 && geom(ckx, cky, Q, rows, cols, rowe) > kSmemBudget) cky = (cky + 1) / 2;
-    geom(ckx, cky, Q, rows, cols, rowe);
-    P.sw_ty = TY;
-    P.sw_nseg = NSEG;
-    P.sw_q = Q;
-    P.cky = cky;
-    P.ckx = ckx;
-    P.max_rows = rows;
-    P.max_cols = cols;
-    P.tile_elems = rows * rowe;
-    P.w_elems = cky * ckx;
-    P.maps_off = ((int64_t)sizeof(T) * (P.tile_elems + P.w_elems) + 15) / 16 * 16;
-    return true;
-}
-
-template <typename T, int RX, int CKX>
-cudaError_t launch_sw(const T *x, const T *k, T *y, const DirectParams<T> &P, cudaStream_t st, int64_t n_inst) {
-    static_assert(CKX % RX == 0, "tap chunks must start on window blocks");
-    const size_t sm = smem_bytes(P);
-    auto fn = direct_sw_kernel<T, RX, CKX>;
-    cudaError_t e = ndconv_allow_smem((const void *)fn, (int)kSmemBudget + 4096);
-    if (e != cudaSuccess) return e;
-    const AxisGeom &A0 = P.g.ax[0], &A1 = P.g.ax[1], &A2 = P.g.ax[2];
-    const int64_t TXo = (int64_t)P.sw_nseg * A2.d * 32 * RX;
-    dim3 grid((unsigned)((A2.out + TXo - 1) / TXo), (unsigned)((A1.out + P.sw_ty - 1) / P.sw_ty),
-              (unsigned)(A0.out * n_inst));
-    fn<<<grid, 256, sm, st>>>(x, k, y, P);
-    ndconv_count_launch();
-    return cudaGetLastError();
-}
-
-template <typename T, int RX> cudaError_t launch_tile(const T *x, const T *k, T *y, const DirectParams<T> &P,
-                                                      int BX, int BY, cudaStream_t st, int64_t n_inst) {
-    const size_t sm = smem_bytes(P);
-    auto fn = direct_tile_kernel<T, RX>;
-    cudaError_t e = ndconv_allow_smem((const void *)fn, (int)kSmemBudget + 4096);
-    if (e != cudaSuccess) return e;
-    const AxisGeom &A0 = P.g.ax[0], &A1 = P.g.ax[1], &A2 = P.g.ax[2];
-    const int64_t TX = (int64_t)BX * RX;
-    dim3 grid((unsigned)((A2.out + TX - 1) / TX), (unsigned)((A1.out + BY - 1) / BY),
-              (unsigned)(A0.out * n_inst));
-    fn<<<grid, dim3(BX, BY), sm, st>>>(x, k, y, P);
-    ndconv_count_launch();
-    return cudaGetLastError();
-}
-}  // namespace
-
+// CTA (bx, by, bz) of the tiled kernel; block shape (BX, BY) comes from P.
 namespace {
 bool sw_disabled() {
     static int v = -1;

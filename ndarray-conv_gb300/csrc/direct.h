@@ -13,11 +13,17 @@ template <typename T> struct DirectParams {
     int64_t tile_elems, w_elems;
     int64_t maps_off;        // byte offset of the int64 border maps in shared memory
     int sw_ty, sw_nseg, sw_q;  // sliding-window tiling (rows, segments, swizzle pitch)
+    int tile_bx, tile_by;      // tiled kernel block shape
     // batch: device arrays of per-instance pointers (null for one instance)
     const T *const *xs;
     const T *const *ks;
     T *const *ys;
     int64_t inst_base;
+    // one instance whose pointers travel in the parameters (persistent batch
+    // kernel); null when the kernel arguments carry them
+    const T *x1;
+    const T *k1;
+    T *y1;
 };
 
 // x, k: device pointers (strided per g.ax[i].xs / ks); y: contiguous output.

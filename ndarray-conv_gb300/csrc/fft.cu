@@ -16,7 +16,9 @@
 // are the smallest 2^a 3^b 5^c 7^d >= pds (even on the real axis): any
 // length >= pds gives the same cropped result as the reference's good_size
 // (the circular wrap only touches indices < k_eff - 1).
+#include <algorithm>
 #include <map>
+#include <string>
 #include <mutex>
 #include <vector>
 
@@ -321,24 +323,24 @@ __device__ void c2r_pre(const C *X, C *Z, int M, int nb, int lognb, const C *__r
     }
 }
 
+// One CTA's share of a row pass: rows [bx * nb, bx * nb + nb) of instance by.
 template <typename T, int MODE>
-__global__ void __launch_bounds__(256) row_kernel(RowArgs<T> A) {
+__device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsigned by, unsigned char *smem_raw) {
     using C = typename RowArgs<T>::C;
     using R = typename RowArgs<T>::R;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nb = A.nb, lognb = A.lognb;
     const int M = A.pl.L;  // transform length
     const int cap = (int)padded_slots<C>((int64_t)(A.kind == RK_REAL_EVEN ? M + 1 : M) << lognb);
     RowInfo *rinfo = reinterpret_cast<RowInfo *>(smem_raw);
     C *buf0 = reinterpret_cast<C *>(smem_raw + ((sizeof(RowInfo) * nb + 15) / 16) * 16);
     C *buf1 = buf0 + cap;
-    const int inst = blockIdx.y;
+    const int inst = (int)by;
     const T *__restrict__ x = A.xs ? A.xs[A.inst_base + inst] : A.x;
     const T *__restrict__ kp = A.ks ? A.ks[A.inst_base + inst] : A.k;
     T *__restrict__ y = A.ys ? A.ys[A.inst_base + inst] : A.y;
     C *spec = A.spec + inst * A.spec_is;
     const C *kspec = A.kspec + inst * A.kspec_is;
-    const int64_t rbase = (int64_t)blockIdx.x * nb;
+    const int64_t rbase = (int64_t)bx * nb;
 
     for (int b = threadIdx.x; b < nb; b += blockDim.x) {
         const int64_t r = rbase + b;
@@ -418,7 +420,7 @@ __global__ void __launch_bounds__(256) row_kernel(RowArgs<T> A) {
         // ---- fused: multiply by the kernel spectrum, back to the time domain
         {
             const int tot = H << lognb;
-            for (int u = threadIdx.x; u < tot; u += blockDim.x) res[sx<C>(u)] = cmul(res[sx<C>(u)], kspec[u >> lognb]);
+            for (int u = threadIdx.x; u < tot; u += blockDim.x) res[sx<C>(u)] = cmul(res[sx<C>(u)], ldcg_c(kspec + (u >> lognb)));
             __syncthreads();
         }
         if (A.kind == RK_REAL_EVEN) {
@@ -436,7 +438,7 @@ __global__ void __launch_bounds__(256) row_kernel(RowArgs<T> A) {
         for (int u = threadIdx.x; u < tot; u += blockDim.x) {
             const int b = u & (nb - 1), k = u >> lognb;
             const RowInfo &ri = rinfo[b];
-            dst[sx<C>(u)] = ri.valid ? spec[ri.soff + k] : C{0, 0};
+            dst[sx<C>(u)] = ri.valid ? ldcg_c(spec + ri.soff + k) : C{0, 0};
         }
         __syncthreads();
         if (A.kind == RK_REAL_ODD) {
@@ -481,6 +483,12 @@ __global__ void __launch_bounds__(256) row_kernel(RowArgs<T> A) {
     }
 }
 
+template <typename T, int MODE>
+__global__ void __launch_bounds__(256) row_kernel(const __grid_constant__ RowArgs<T> A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    row_block<T, MODE>(A, blockIdx.x, blockIdx.y, smem_raw);
+}
+
 // ---------------------------------------------------------- column pass --
 enum ColMode : int { COL_FWD = 0, COL_INV = 1, COL_FUSED = 2 };
 
@@ -503,19 +511,21 @@ template <typename C> struct ColArgs {
     int nb, lognb;
 };
 
+// One CTA's share of a column pass: column tile bx, outer indices by,
+// by + ystep, ... of instance bz.
 template <typename C>
-__global__ void __launch_bounds__(256) col_kernel(ColArgs<C> A) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void col_block(const ColArgs<C> &A, unsigned bx, int64_t by, int64_t ystep, unsigned bz,
+                                          unsigned char *smem_raw) {
     const int nb = A.nb, lognb = A.lognb;
     const int F = A.pl.L;
     C *buf0 = reinterpret_cast<C *>(smem_raw);
     C *buf1 = buf0 + padded_slots<C>((int64_t)F << lognb);
-    const int64_t h0 = (int64_t)blockIdx.x * nb;
-    const int inst = blockIdx.z;
+    const int64_t h0 = (int64_t)bx * nb;
+    const int inst = (int)bz;
     const int nvalid = (int)(h0 + nb <= A.n_inner ? nb : A.n_inner - h0);
     const int valid_in = (int)A.valid_in;
     const int T_ = blockDim.x;
-    for (int64_t outer = blockIdx.y; outer < A.n_outer; outer += gridDim.y) {
+    for (int64_t outer = by; outer < A.n_outer; outer += ystep) {
         const C *__restrict__ src = A.src + inst * A.src_is + outer * A.src_outer + h0;
         const int tot_in = F << lognb;
         for (int u0 = threadIdx.x; u0 < tot_in; u0 += 4 * T_) {
@@ -525,7 +535,7 @@ __global__ void __launch_bounds__(256) col_kernel(ColArgs<C> A) {
                 const int u = u0 + q * T_;
                 const int b = u & (nb - 1), i = u >> lognb;
                 v[q] = C{0, 0};
-                if (u < tot_in && i < valid_in && b < nvalid) v[q] = src[i * A.src_axis + b];
+                if (u < tot_in && i < valid_in && b < nvalid) v[q] = ldcg_c(src + i * A.src_axis + b);
             }
 #pragma unroll
             for (int q = 0; q < 4; q++) {
@@ -543,7 +553,7 @@ __global__ void __launch_bounds__(256) col_kernel(ColArgs<C> A) {
                 const C *__restrict__ kp = A.kspec + inst * A.k_is + h0;
                 for (int u = threadIdx.x; u < tot_in; u += T_) {
                     const int b = u & (nb - 1), k = u >> lognb;
-                    if (b < nvalid) res[sx<C>(u)] = cmul(res[sx<C>(u)], kp[k * A.k_axis + b]);
+                    if (b < nvalid) res[sx<C>(u)] = cmul(res[sx<C>(u)], ldcg_c(kp + k * A.k_axis + b));
                 }
                 __syncthreads();
                 C *other = (res == buf0) ? buf1 : buf0;
@@ -562,6 +572,12 @@ __global__ void __launch_bounds__(256) col_kernel(ColArgs<C> A) {
         }
         __syncthreads();
     }
+}
+
+template <typename C>
+__global__ void __launch_bounds__(256) col_kernel(const __grid_constant__ ColArgs<C> A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    col_block<C>(A, blockIdx.x, blockIdx.y, gridDim.y, blockIdx.z, smem_raw);
 }
 
 // ----------------------------------------------------------- transpose --
@@ -623,19 +639,28 @@ template <typename T, int MODE> int launch_row_mode(const RowArgs<T> &A, size_t 
     return NDCONV_OK;
 }
 
-// n_inst instances (grid.y); A.spec_is etc. describe their spacing
-template <typename T> int launch_row(RowArgs<T> A, cudaStream_t st, int n_inst = 1) {
+// Fill nb / lognb and the launch shape of a row pass over n_inst instances.
+template <typename T> int prep_row(RowArgs<T> &A, int n_inst, int64_t &grid, size_t &sm) {
     using C = typename RowArgs<T>::C;
-    if (A.n_rows <= 0 || n_inst <= 0) return NDCONV_OK;
     const size_t per_row = sizeof(C) * 2 * padded_slots<C>(A.pl.L + 1) + sizeof(RowInfo);
     A.nb = pick_nb(A.pl.L, A.n_rows, per_row);
     A.lognb = ilog2(A.nb);
-    const size_t sm = row_smem(A);
+    sm = row_smem(A);
     if (sm > kFftSmemMax) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "FFT row length exceeds shared memory");
     if (((int64_t)(A.pl.L + 1) << A.lognb) >= (int64_t)1 << 29)
         return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "FFT row too long");
-    const int64_t grid = (A.n_rows + A.nb - 1) / A.nb;
+    grid = (A.n_rows + A.nb - 1) / A.nb;
     if (grid > 0x7fffffff || n_inst > 65535) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "too many FFT rows");
+    return NDCONV_OK;
+}
+
+// n_inst instances (grid.y); A.spec_is etc. describe their spacing
+template <typename T> int launch_row(RowArgs<T> A, cudaStream_t st, int n_inst = 1) {
+    if (A.n_rows <= 0 || n_inst <= 0) return NDCONV_OK;
+    int64_t grid;
+    size_t sm;
+    int s = prep_row(A, n_inst, grid, sm);
+    if (s) return s;
     switch (A.mode) {
     case ROW_FWD_DATA: return launch_row_mode<T, ROW_FWD_DATA>(A, sm, (unsigned)grid, n_inst, st);
     case ROW_FWD_KERNEL: return launch_row_mode<T, ROW_FWD_KERNEL>(A, sm, (unsigned)grid, n_inst, st);
@@ -646,20 +671,30 @@ template <typename T> int launch_row(RowArgs<T> A, cudaStream_t st, int n_inst =
     }
 }
 
-template <typename C> int launch_col(ColArgs<C> A, cudaStream_t st, int n_inst = 1) {
-    if (A.n_outer <= 0 || A.n_inner <= 0 || n_inst <= 0) return NDCONV_OK;
+// Fill nb / lognb and the launch shape of a column pass.
+template <typename C> int prep_col(ColArgs<C> &A, int64_t &gx, int64_t &gy, size_t &sm) {
     const int64_t F = A.pl.L;
     int nb = 1;
     while (nb < 32 && (int64_t)nb * 2 <= A.n_inner + 1 && sizeof(C) * 2 * F * nb * 2 <= 96 * 1024) nb *= 2;
     A.nb = nb;
     A.lognb = ilog2(nb);
-    const size_t sm = sizeof(C) * 2 * padded_slots<C>(F * nb);
+    sm = sizeof(C) * 2 * padded_slots<C>(F * nb);
     if (sm > kFftSmemMax) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "FFT column length exceeds shared memory");
+    gx = (A.n_inner + nb - 1) / nb;
+    gy = A.n_outer < 65535 ? A.n_outer : 65535;
+    if (gx > 0x7fffffff) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "too many FFT columns");
+    return NDCONV_OK;
+}
+
+template <typename C> int launch_col(ColArgs<C> A, cudaStream_t st, int n_inst = 1) {
+    if (A.n_outer <= 0 || A.n_inner <= 0 || n_inst <= 0) return NDCONV_OK;
+    int64_t gx, gy;
+    size_t sm;
+    int s = prep_col(A, gx, gy, sm);
+    if (s) return s;
+    if (n_inst > 65535) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "too many FFT instances");
     int st_ = ensure_smem(col_kernel<C>);
     if (st_) return st_;
-    const int64_t gx = (A.n_inner + nb - 1) / nb;
-    const int64_t gy = A.n_outer < 65535 ? A.n_outer : 65535;
-    if (gx > 0x7fffffff || n_inst > 65535) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "too many FFT columns");
     col_kernel<C><<<dim3((unsigned)gx, (unsigned)gy, (unsigned)n_inst), kThreads, sm, st>>>(A);
     ndconv_count_launch();
     NDCONV_CUDA_OK(cudaGetLastError());
@@ -779,13 +814,15 @@ template <typename T> int make_conv_plan(const Geom3<T> &g, FftConvPlan<T> &cp) 
     return NDCONV_OK;
 }
 
-// Instances [base, base + cnt) through all passes; Kh / S hold cnt
+// The passes of instances [base, base + cnt), in order, handed to emit_row /
+// emit_col (launch them, or record them as tasks).  Kh / S hold cnt
 // instances' spectra back to back.  Pointers come from the device arrays
 // xs / ks / ys when given, else x / k / y (cnt == 1).
-template <typename T>
-int conv_fft_wave(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, const T *x, const T *k, T *y,
-                  const T *const *xs, const T *const *ks, T *const *ys, int64_t base, int cnt,
-                  typename FftConvPlan<T>::C *Kh, typename FftConvPlan<T>::C *S, cudaStream_t st) {
+template <typename T, typename EmitRow, typename EmitCol>
+int conv_fft_passes(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, const T *x, const T *k, T *y,
+                    const T *const *xs, const T *const *ks, T *const *ys, int64_t base, int cnt,
+                    typename FftConvPlan<T>::C *Kh, typename FftConvPlan<T>::C *S, EmitRow &&emit_row,
+                    EmitCol &&emit_col) {
     using R = typename Elem<T>::Real;
     using C = typename FftConvPlan<T>::C;
     const AxisGeom &A0 = g.ax[0], &A1 = g.ax[1], &A2 = g.ax[2];
@@ -808,7 +845,7 @@ int conv_fft_wave(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, cons
     kr.spec_s1 = H;
     kr.spec_is = K_is;
     kr.scale = 1;
-    if ((s = launch_row(kr, st, cnt))) return s;
+    if ((s = emit_row(kr, cnt))) return s;
     if (F[1] > 1) {
         ColArgs<C> c{};
         c.mode = COL_FWD;
@@ -821,7 +858,7 @@ int conv_fft_wave(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, cons
         c.valid_in = A1.keff;
         c.pl = cp.pl1;
         c.tw = cp.tw1;
-        if ((s = launch_col(c, st, cnt))) return s;
+        if ((s = emit_col(c, cnt))) return s;
     }
     if (F[0] > 1) {
         ColArgs<C> c{};
@@ -834,7 +871,7 @@ int conv_fft_wave(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, cons
         c.valid_in = A0.keff;
         c.pl = cp.pl0;
         c.tw = cp.tw0;
-        if ((s = launch_col(c, st, cnt))) return s;
+        if ((s = emit_col(c, cnt))) return s;
     }
     const R scale = (R)(1.0 / ((double)F[0] * (double)F[1] * (double)F[2]));
 
@@ -857,7 +894,7 @@ int conv_fft_wave(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, cons
         fr.crop_off = A2.keff - 1;
         fr.crop_step = A2.s;
         fr.scale = scale;
-        return launch_row(fr, st, cnt);
+        return emit_row(fr, cnt);
     }
 
     // ---- data: forward row pass into S
@@ -874,7 +911,7 @@ int conv_fft_wave(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, cons
     dr.spec_s1 = H;
     dr.spec_is = S_is;
     dr.scale = 1;
-    if ((s = launch_row(dr, st, cnt))) return s;
+    if ((s = emit_row(dr, cnt))) return s;
     if (cp.astar == 0 && F[1] > 1) {
         ColArgs<C> c{};
         c.mode = COL_FWD;
@@ -887,7 +924,7 @@ int conv_fft_wave(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, cons
         c.valid_in = P[1];
         c.pl = cp.pl1;
         c.tw = cp.tw1;
-        if ((s = launch_col(c, st, cnt))) return s;
+        if ((s = emit_col(c, cnt))) return s;
     }
     {
         ColArgs<C> c{};
@@ -918,7 +955,7 @@ int conv_fft_wave(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, cons
             c.pl = cp.pl1;
             c.tw = cp.tw1;
         }
-        if ((s = launch_col(c, st, cnt))) return s;
+        if ((s = emit_col(c, cnt))) return s;
     }
     if (cp.astar == 0 && F[1] > 1) {
         ColArgs<C> c{};
@@ -935,7 +972,7 @@ int conv_fft_wave(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, cons
         c.n_out = A1.out;
         c.pl = cp.pl1;
         c.tw = cp.tw1;
-        if ((s = launch_col(c, st, cnt))) return s;
+        if ((s = emit_col(c, cnt))) return s;
     }
     RowArgs<T> ir = cp.rk;
     ir.mode = ROW_INV_OUT;
@@ -954,7 +991,18 @@ int conv_fft_wave(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, cons
     ir.crop_off = A2.keff - 1;
     ir.crop_step = A2.s;
     ir.scale = scale;
-    return launch_row(ir, st, cnt);
+    return emit_row(ir, cnt);
+}
+
+template <typename T>
+int conv_fft_wave(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, const T *x, const T *k, T *y,
+                  const T *const *xs, const T *const *ks, T *const *ys, int64_t base, int cnt,
+                  typename FftConvPlan<T>::C *Kh, typename FftConvPlan<T>::C *S, cudaStream_t st) {
+    using C = typename FftConvPlan<T>::C;
+    return conv_fft_passes<T>(
+        g, reverse, cp, x, k, y, xs, ks, ys, base, cnt, Kh, S,
+        [&](RowArgs<T> &A, int n) { return launch_row<T>(A, st, n); },
+        [&](ColArgs<C> &A, int n) { return launch_col<C>(A, st, n); });
 }
 
 // bytes of spectra a wave may keep so that they stay in L2 between passes
@@ -1213,3 +1261,627 @@ extern "C" int ndconv_fft_processor_destroy(ndconv_fft_processor *p) {
 
 int64_t ndconv_proc_origin_len(const ndconv_fft_processor *p) { return p->rp_origin_len; }
 int32_t ndconv_proc_dtype(const ndconv_fft_processor *p) { return p->dtype; }
+
+// ======================================================== batch plan ====
+// A heterogeneous batch (instances with different shapes, kernels, modes,
+// algorithms) executed by one persistent kernel.  Every instance becomes
+// CTA-sized tasks: direct-convolution tiles, or the passes of its FFT
+// convolution (one "level" per pass).  Tasks are stored in ticket order:
+// all FFT tasks level-major across instances, then the direct tiles.  A CTA
+// takes the next ticket, waits (bounded) until the previous level of the
+// same instance has completed, runs the task and bumps its level counter.
+// A task only waits for tasks with smaller tickets, which running CTAs have
+// already claimed, so the queue always makes progress.
+#include "direct_blocks.cuh"
+#include "geometry.h"
+
+namespace ndconv {
+namespace batch {
+
+enum TaskKind : int32_t {
+    TK_DIRECT_SW = 1,
+    TK_DIRECT_TILE4 = 2,
+    TK_DIRECT_TILE1 = 3,
+    TK_DIRECT_NAIVE = 4,
+    TK_ROW_FWD_DATA = 10,
+    TK_ROW_FWD_KERNEL = 11,
+    TK_ROW_INV_OUT = 12,
+    TK_ROW_FUSED = 13,
+    TK_COL = 20,
+};
+
+struct Task {
+    int32_t kind, arg;
+    int32_t bx, by, bz;
+    int32_t done_ctr;   // counter bumped when done (-1: none)
+    int32_t wait_ctr;   // counter to wait for (-1: none)
+    int32_t wait_need;  // value it must reach
+};
+
+constexpr int kSpinLimit = 1 << 24;  // ~1-2 s of polling before giving up
+
+__device__ __forceinline__ int ld_acquire(const int *p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__global__ void __launch_bounds__(256) persistent_kernel(const Task *__restrict__ tasks, int ntasks,
+                                                         const RowArgs<float> *__restrict__ rargs,
+                                                         const ColArgs<c32> *__restrict__ cargs,
+                                                         const DirectParams<float> *__restrict__ dargs,
+                                                         int *ctrs, int *ticket, int *status) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_ticket;
+    for (;;) {
+        if (threadIdx.x == 0) s_ticket = atomicAdd(ticket, 1);
+        __syncthreads();
+        const int t = s_ticket;
+        __syncthreads();
+        if (t >= ntasks) return;
+        const Task tk = tasks[t];
+        if (tk.wait_ctr >= 0) {
+            if (threadIdx.x == 0) {
+                int it = 0;
+                while (ld_acquire(ctrs + tk.wait_ctr) < tk.wait_need) {
+                    if (++it > kSpinLimit) {
+                        atomicOr(status, 1);  // dependency never completed: report, do not hang
+                        break;
+                    }
+                    __nanosleep(64);
+                }
+            }
+            __syncthreads();
+        }
+        switch (tk.kind) {
+        case TK_DIRECT_SW: {
+            const DirectParams<float> &P = dargs[tk.arg];
+            direct_sw_block<float, 8, 16>(nullptr, nullptr, nullptr, P, tk.bx, tk.by, tk.bz, smem_raw);
+            break;
+        }
+        case TK_DIRECT_TILE4: {
+            const DirectParams<float> &P = dargs[tk.arg];
+            direct_tile_block<float, 4>(nullptr, nullptr, nullptr, P, tk.bx, tk.by, tk.bz, smem_raw);
+            break;
+        }
+        case TK_DIRECT_TILE1: {
+            const DirectParams<float> &P = dargs[tk.arg];
+            direct_tile_block<float, 1>(nullptr, nullptr, nullptr, P, tk.bx, tk.by, tk.bz, smem_raw);
+            break;
+        }
+        case TK_DIRECT_NAIVE: {
+            const DirectParams<float> &P = dargs[tk.arg];
+            direct_naive_range<float>(P, (int64_t)tk.bx * 256 + threadIdx.x);
+            break;
+        }
+        case TK_ROW_FWD_DATA: row_block<float, ROW_FWD_DATA>(rargs[tk.arg], tk.bx, 0, smem_raw); break;
+        case TK_ROW_FWD_KERNEL: row_block<float, ROW_FWD_KERNEL>(rargs[tk.arg], tk.bx, 0, smem_raw); break;
+        case TK_ROW_INV_OUT: row_block<float, ROW_INV_OUT>(rargs[tk.arg], tk.bx, 0, smem_raw); break;
+        case TK_ROW_FUSED: row_block<float, ROW_FUSED>(rargs[tk.arg], tk.bx, 0, smem_raw); break;
+        case TK_COL: {
+            const ColArgs<c32> &A = cargs[tk.arg];
+            col_block<c32>(A, tk.bx, tk.by, A.n_outer, 0, smem_raw);
+            break;
+        }
+        default: break;
+        }
+        __threadfence();  // this CTA's results visible GPU-wide before the counter moves
+        __syncthreads();
+        if (threadIdx.x == 0 && tk.done_ctr >= 0) atomicAdd(ctrs + tk.done_ctr, 1);
+    }
+}
+
+// work estimate of one instance (for ordering direct tiles, longest first)
+struct HostInst {
+    int algo;        // 0 direct, 1 FFT
+    int standalone;  // runs as ordinary launches before the persistent kernel
+    Plan3 P;
+    const void *x, *k;
+    void *y;
+    size_t ws_off;   // spectra offset (FFT)
+    FftConvPlan<float> cp;
+};
+
+}  // namespace batch
+}  // namespace ndconv
+
+struct ndconv_batch_plan {
+    int device = 0;
+    int64_t n = 0;
+    std::vector<ndconv::batch::HostInst> inst;
+    std::vector<ndconv::batch::Task> tasks;
+    std::vector<ndconv::RowArgs<float>> rargs;
+    std::vector<ndconv::ColArgs<c32>> cargs;
+    std::vector<ndconv::DirectParams<float>> dargs;
+    int nctrs = 0;
+    size_t smem = 0;
+    int grid = 0;
+    void *d_tasks = nullptr, *d_rargs = nullptr, *d_cargs = nullptr, *d_dargs = nullptr;
+    int *d_ctrs = nullptr;  // nctrs counters, then ticket, then status
+    void *ws = nullptr;
+    size_t ws_bytes = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int64_t n_fft = 0, n_direct = 0, n_standalone = 0;
+};
+
+namespace ndconv {
+namespace batch {
+
+constexpr size_t kBatchSmem = 100 * 1024;  // persistent kernel's shared memory (2 CTAs per SM)
+
+template <typename V> int upload(const std::vector<V> &v, void **d) {
+    const size_t bytes = sizeof(V) * (v.empty() ? 1 : v.size());
+    NDCONV_CUDA_OK(cudaMalloc(d, bytes));
+    if (!v.empty()) NDCONV_CUDA_OK(cudaMemcpy(*d, v.data(), sizeof(V) * v.size(), cudaMemcpyHostToDevice));
+    return NDCONV_OK;
+}
+
+// Direct tiles of instance i as tasks; returns the shared memory a task needs.
+size_t direct_tasks(ndconv_batch_plan *B, HostInst &h, std::vector<Task> &out) {
+    DirectParams<float> D = h.P.direct<float>();
+    D.xs = nullptr;
+    D.ks = nullptr;
+    D.ys = nullptr;
+    D.x1 = static_cast<const float *>(h.x);
+    D.k1 = static_cast<const float *>(h.k);
+    D.y1 = static_cast<float *>(h.y);
+    const AxisGeom &A0 = D.g.ax[0], &A1 = D.g.ax[1], &A2 = D.g.ax[2];
+    int kind = 0;
+    int64_t gx = 0, gy = 0;
+    if (A2.s == 1 && A2.d <= 8 && plan_sw(D, 8) && smem_bytes(D) <= kBatchSmem) {
+        kind = TK_DIRECT_SW;
+        const int64_t TXo = (int64_t)D.sw_nseg * A2.d * 32 * 8;
+        gx = (A2.out + TXo - 1) / TXo;
+        gy = (A1.out + D.sw_ty - 1) / D.sw_ty;
+    } else {
+        int BX, BY;
+        if (plan_tile(D, 4, BX, BY) && smem_bytes(D) <= kBatchSmem) {
+            kind = TK_DIRECT_TILE4;
+            gx = (A2.out + (int64_t)BX * 4 - 1) / ((int64_t)BX * 4);
+        } else if (plan_tile(D, 1, BX, BY) && smem_bytes(D) <= kBatchSmem) {
+            kind = TK_DIRECT_TILE1;
+            gx = (A2.out + BX - 1) / BX;
+        } else {
+            kind = TK_DIRECT_NAIVE;
+        }
+        if (kind != TK_DIRECT_NAIVE) gy = (A1.out + BY - 1) / BY;
+    }
+    const int arg = (int)B->dargs.size();
+    B->dargs.push_back(D);
+    if (kind == TK_DIRECT_NAIVE) {
+        const int64_t total = A0.out * A1.out * A2.out;
+        for (int64_t b = 0; b * 256 < total; b++) out.push_back(Task{kind, arg, (int32_t)b, 0, 0, -1, -1, 0});
+        return 0;
+    }
+    for (int64_t z = 0; z < A0.out; z++)
+        for (int64_t yy = 0; yy < gy; yy++)
+            for (int64_t xx = 0; xx < gx; xx++)
+                out.push_back(Task{kind, arg, (int32_t)xx, (int32_t)yy, (int32_t)z, -1, -1, 0});
+    return smem_bytes(D);
+}
+
+}  // namespace batch
+}  // namespace ndconv
+
+namespace ndconv {
+namespace batch {
+
+// Build the plan: per-instance tasks, spectra, device copies of everything.
+int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const void *const *data,
+           const void *const *kernel, void *const *out, ndconv_batch_plan **outp) {
+    auto *B = new ndconv_batch_plan();
+    cudaGetDevice(&B->device);
+    B->n = n;
+    B->inst.resize((size_t)n);
+    auto fail = [&](int st) {
+        delete B;
+        return st;
+    };
+    // ---- pass 1: plans, algorithms, spectra sizes
+    size_t ws = 0;
+    for (int64_t i = 0; i < n; i++) {
+        HostInst &h = B->inst[(size_t)i];
+        h.algo = algo ? algo[i] : 1;
+        if (h.algo != 0 && h.algo != 1) return fail(ndconv_fail(NDCONV_ERR_INVALID, "algo must be 0 (direct) or 1 (FFT)"));
+        int s = plan_problem(&probs[i], h.algo, &h.P);
+        if (s) {
+            std::string m = "instance " + std::to_string(i) + ": " + ndconv_last_error();
+            return fail(ndconv_fail(s, m.c_str()));
+        }
+        if (h.algo == 1 && (h.P.dtype == NDCONV_I32))
+            return fail(ndconv_fail(NDCONV_ERR_UNSUPPORTED, "integer FFT convolution is not supported"));
+        h.x = data[i];
+        h.k = kernel[i];
+        h.y = out[i];
+        h.standalone = (h.P.dtype != NDCONV_F32);
+        h.ws_off = 0;
+        if (h.algo == 1 && !h.standalone) {
+            if ((s = make_conv_plan<float>(h.P.geom<float>(), h.cp))) return fail(s);
+            h.ws_off = ws;
+            ws += (sizeof(c32) * (h.cp.nK + h.cp.nS) + 255) / 256 * 256;
+        }
+    }
+    // standalone FFT instances of other types get their own slice as scratch
+    for (int64_t i = 0; i < n; i++) {
+        HostInst &h = B->inst[(size_t)i];
+        if (h.algo == 1 && h.standalone) {
+            h.ws_off = ws;
+            size_t b = 0;
+            int s = NDCONV_OK;
+            // plans now, so their twiddle tables exist before any graph capture
+            switch (h.P.dtype) {
+            case NDCONV_F64: {
+                FftConvPlan<double> cp;
+                s = make_conv_plan<double>(h.P.geom<double>(), cp);
+                b = conv_fft_scratch_bytes<double>(h.P.geom<double>());
+                break;
+            }
+            case NDCONV_C32: {
+                FftConvPlan<c32> cp;
+                s = make_conv_plan<c32>(h.P.geom<c32>(), cp);
+                b = conv_fft_scratch_bytes<c32>(h.P.geom<c32>());
+                break;
+            }
+            default: {
+                FftConvPlan<c64> cp;
+                s = make_conv_plan<c64>(h.P.geom<c64>(), cp);
+                b = conv_fft_scratch_bytes<c64>(h.P.geom<c64>());
+                break;
+            }
+            }
+            if (s) return fail(s);
+            ws += (b + 255) / 256 * 256;
+        }
+    }
+    B->ws_bytes = ws;
+    if (ws) {
+        cudaError_t e = cudaMalloc(&B->ws, ws);
+        if (e != cudaSuccess) return fail(ndconv_fail(NDCONV_ERR_NO_MEMORY, cudaGetErrorString(e)));
+    }
+    // ---- pass 2: FFT passes as tasks (level-major across instances)
+    struct Level {
+        int64_t inst;
+        int ctr;
+        std::vector<Task> tasks;
+    };
+    std::vector<std::vector<Level>> per_inst((size_t)n);
+    int max_levels = 0;
+    for (int64_t i = 0; i < n; i++) {
+        HostInst &h = B->inst[(size_t)i];
+        if (h.algo != 1 || h.standalone) continue;
+        c32 *Kh = reinterpret_cast<c32 *>(static_cast<unsigned char *>(B->ws) + h.ws_off);
+        c32 *S = Kh + h.cp.nK;
+        std::vector<Level> &lv = per_inst[(size_t)i];
+        bool too_big = false;
+        size_t inst_smem = 0;
+        auto new_level = [&]() -> Level & {
+            lv.push_back(Level{i, B->nctrs++, {}});
+            return lv.back();
+        };
+        auto emit_row = [&](RowArgs<float> &A, int cnt) -> int {
+            (void)cnt;
+            if (A.n_rows <= 0) return NDCONV_OK;
+            int64_t grid;
+            size_t sm;
+            int s2 = prep_row(A, 1, grid, sm);
+            if (s2) return s2;
+            if (sm > kBatchSmem) too_big = true;
+            inst_smem = std::max(inst_smem, sm);
+            const int arg = (int)B->rargs.size();
+            B->rargs.push_back(A);
+            int kind = TK_ROW_FWD_DATA;
+            switch (A.mode) {
+            case ROW_FWD_DATA: kind = TK_ROW_FWD_DATA; break;
+            case ROW_FWD_KERNEL: kind = TK_ROW_FWD_KERNEL; break;
+            case ROW_INV_OUT: kind = TK_ROW_INV_OUT; break;
+            default: kind = TK_ROW_FUSED; break;
+            }
+            Level &L = new_level();
+            for (int64_t b = 0; b < grid; b++) L.tasks.push_back(Task{kind, arg, (int32_t)b, 0, 0, L.ctr, -1, 0});
+            return NDCONV_OK;
+        };
+        auto emit_col = [&](ColArgs<c32> &A, int cnt) -> int {
+            (void)cnt;
+            if (A.n_outer <= 0 || A.n_inner <= 0) return NDCONV_OK;
+            int64_t gx, gy;
+            size_t sm;
+            int s2 = prep_col(A, gx, gy, sm);
+            if (s2) return s2;
+            if (sm > kBatchSmem) too_big = true;
+            inst_smem = std::max(inst_smem, sm);
+            const int arg = (int)B->cargs.size();
+            B->cargs.push_back(A);
+            Level &L = new_level();
+            for (int64_t o = 0; o < A.n_outer; o++)
+                for (int64_t b = 0; b < gx; b++)
+                    L.tasks.push_back(Task{TK_COL, arg, (int32_t)b, (int32_t)o, 0, L.ctr, -1, 0});
+            return NDCONV_OK;
+        };
+        const Geom3<float> g = h.P.geom<float>();
+        int s = conv_fft_passes<float>(g, h.P.reverse, h.cp, static_cast<const float *>(h.x),
+                                       static_cast<const float *>(h.k), static_cast<float *>(h.y), nullptr,
+                                       nullptr, nullptr, 0, 1, Kh, S, emit_row, emit_col);
+        if (s) return fail(s);
+        if (too_big) {
+            // does not fit the persistent kernel's shared memory: ordinary launches
+            h.standalone = 1;
+            lv.clear();
+            continue;
+        }
+        B->smem = std::max(B->smem, inst_smem);
+        for (size_t l = 1; l < lv.size(); l++)
+            for (Task &t : lv[l].tasks) {
+                t.wait_ctr = lv[l - 1].ctr;
+                t.wait_need = (int32_t)lv[l - 1].tasks.size();
+            }
+        max_levels = std::max(max_levels, (int)lv.size());
+        B->n_fft++;
+    }
+    for (int l = 0; l < max_levels; l++)
+        for (int64_t i = 0; i < n; i++) {
+            std::vector<Level> &lv = per_inst[(size_t)i];
+            if ((int)lv.size() > l) B->tasks.insert(B->tasks.end(), lv[l].tasks.begin(), lv[l].tasks.end());
+        }
+    // ---- direct tiles, largest instances first
+    std::vector<std::pair<double, int64_t>> order;
+    for (int64_t i = 0; i < n; i++) {
+        HostInst &h = B->inst[(size_t)i];
+        if (h.algo != 0 || h.standalone) continue;
+        const AxisGeom *A = h.P.ax;
+        const double work = (double)(A[0].out * A[1].out * A[2].out) * (double)(A[0].K * A[1].K * A[2].K);
+        order.push_back({-work, i});
+    }
+    std::sort(order.begin(), order.end());
+    for (auto &o : order) {
+        HostInst &h = B->inst[(size_t)o.second];
+        B->smem = std::max(B->smem, direct_tasks(B, h, B->tasks));
+        B->n_direct++;
+    }
+    for (auto &h : B->inst) B->n_standalone += h.standalone;
+    // ---- device copies
+    int s;
+    if ((s = upload(B->tasks, &B->d_tasks)) || (s = upload(B->rargs, &B->d_rargs)) ||
+        (s = upload(B->cargs, &B->d_cargs)) || (s = upload(B->dargs, &B->d_dargs)))
+        return fail(s);
+    {
+        cudaError_t e = cudaMalloc((void **)&B->d_ctrs, sizeof(int) * (size_t)(B->nctrs + 2));
+        if (e != cudaSuccess) return fail(ndconv_fail(NDCONV_ERR_NO_MEMORY, cudaGetErrorString(e)));
+    }
+    if (B->smem < 16) B->smem = 16;
+    if (B->smem > kBatchSmem) return fail(ndconv_fail(NDCONV_ERR_INVALID, "batch task shared memory above the cap"));
+    {
+        cudaError_t e = ndconv_allow_smem((const void *)persistent_kernel, (int)kBatchSmem);
+        if (e != cudaSuccess) return fail(ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e)));
+        int per_sm = 0, sms = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_kernel, 256, B->smem);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, B->device);
+        if (e != cudaSuccess) return fail(ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e)));
+        B->grid = std::max(1, per_sm) * sms;
+        if ((int64_t)B->grid > (int64_t)B->tasks.size()) B->grid = (int)std::max<size_t>(1, B->tasks.size());
+    }
+    *outp = B;
+    return NDCONV_OK;
+}
+
+// Instances that run as ordinary launches (other element types, or FFT
+// passes too large for the persistent kernel), on stream st.
+int run_standalone(ndconv_batch_plan *B, cudaStream_t st) {
+    for (auto &h : B->inst) {
+        if (!h.standalone) continue;
+        unsigned char *scr = static_cast<unsigned char *>(B->ws) + h.ws_off;
+        int s = NDCONV_OK;
+        if (h.algo == 0) {
+            cudaError_t e = cudaSuccess;
+            switch (h.P.dtype) {
+            case NDCONV_F32: e = direct_conv_launch<float>((const float *)h.x, (const float *)h.k, (float *)h.y, h.P.direct<float>(), st, 0); break;
+            case NDCONV_F64: e = direct_conv_launch<double>((const double *)h.x, (const double *)h.k, (double *)h.y, h.P.direct<double>(), st, 0); break;
+            case NDCONV_I32: e = direct_conv_launch<int32_t>((const int32_t *)h.x, (const int32_t *)h.k, (int32_t *)h.y, h.P.direct<int32_t>(), st, 0); break;
+            case NDCONV_C32: e = direct_conv_launch<c32>((const c32 *)h.x, (const c32 *)h.k, (c32 *)h.y, h.P.direct<c32>(), st, 0); break;
+            default: e = direct_conv_launch<c64>((const c64 *)h.x, (const c64 *)h.k, (c64 *)h.y, h.P.direct<c64>(), st, 0); break;
+            }
+            if (e != cudaSuccess) return ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e));
+            continue;
+        }
+        switch (h.P.dtype) {
+        case NDCONV_F32: {
+            const size_t b = sizeof(c32) * (h.cp.nK + h.cp.nS) + 256;
+            s = conv_fft_run<float>(h.P.geom<float>(), h.P.reverse, (const float *)h.x, (const float *)h.k, (float *)h.y, nullptr, st, scr, b);
+            break;
+        }
+        case NDCONV_F64: s = conv_fft_run<double>(h.P.geom<double>(), h.P.reverse, (const double *)h.x, (const double *)h.k, (double *)h.y, nullptr, st, scr, conv_fft_scratch_bytes<double>(h.P.geom<double>())); break;
+        case NDCONV_C32: s = conv_fft_run<c32>(h.P.geom<c32>(), h.P.reverse, (const c32 *)h.x, (const c32 *)h.k, (c32 *)h.y, nullptr, st, scr, conv_fft_scratch_bytes<c32>(h.P.geom<c32>())); break;
+        default: s = conv_fft_run<c64>(h.P.geom<c64>(), h.P.reverse, (const c64 *)h.x, (const c64 *)h.k, (c64 *)h.y, nullptr, st, scr, conv_fft_scratch_bytes<c64>(h.P.geom<c64>())); break;
+        }
+        if (s) return s;
+    }
+    return NDCONV_OK;
+}
+
+// One execution: reset the queue, standalone instances, persistent kernel.
+int enqueue(ndconv_batch_plan *B, cudaStream_t st) {
+    NDCONV_CUDA_OK(cudaMemsetAsync(B->d_ctrs, 0, sizeof(int) * (size_t)(B->nctrs + 2), st));
+    int s = run_standalone(B, st);
+    if (s) return s;
+    if (!B->tasks.empty()) {
+        persistent_kernel<<<B->grid, 256, B->smem, st>>>(
+            (const Task *)B->d_tasks, (int)B->tasks.size(), (const RowArgs<float> *)B->d_rargs,
+            (const ColArgs<c32> *)B->d_cargs, (const DirectParams<float> *)B->d_dargs, B->d_ctrs,
+            B->d_ctrs + B->nctrs, B->d_ctrs + B->nctrs + 1);
+        ndconv_count_launch();
+        NDCONV_CUDA_OK(cudaGetLastError());
+    }
+    return NDCONV_OK;
+}
+
+}  // namespace batch
+}  // namespace ndconv
+
+extern "C" int ndconv_batch_create(const ndconv_problem *problems, int64_t n, const int32_t *algo,
+                                   const void *const *data, const void *const *kernel, void *const *out,
+                                   ndconv_batch_plan **plan) {
+    if (!problems || !data || !kernel || !out || !plan || n < 0)
+        return ndconv_fail(NDCONV_ERR_INVALID, "null argument or negative count");
+    return ndconv::batch::create(problems, n, algo, data, kernel, out, plan);
+}
+
+extern "C" int ndconv_batch_run(ndconv_batch_plan *B, int32_t use_graph, void *stream) {
+    if (!B) return ndconv_fail(NDCONV_ERR_INVALID, "null plan");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!use_graph) return ndconv::batch::enqueue(B, st);
+    if (!B->exec) {
+        // capture once on a private stream, replay with cudaGraphLaunch
+        cudaStream_t cs;
+        NDCONV_CUDA_OK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        int s = NDCONV_OK;
+        if (e == cudaSuccess) s = ndconv::batch::enqueue(B, cs);
+        cudaGraph_t g = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+        cudaStreamDestroy(cs);
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e != cudaSuccess ? e : e2));
+        }
+        if (s) {
+            cudaGraphDestroy(g);
+            return s;
+        }
+        e = cudaGraphInstantiate(&B->exec, g, 0);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            return ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e));
+        }
+        B->graph = g;
+    }
+    NDCONV_CUDA_OK(cudaGraphLaunch(B->exec, st));
+    return NDCONV_OK;
+}
+
+extern "C" int ndconv_batch_run_plain(ndconv_batch_plan *B, void *stream) {
+    // the plain drop-in: every instance through its own per-instance entry point
+    if (!B) return ndconv_fail(NDCONV_ERR_INVALID, "null plan");
+    cudaStream_t st = (cudaStream_t)stream;
+    for (auto &h : B->inst) {
+        unsigned char *scr = static_cast<unsigned char *>(B->ws) + h.ws_off;
+        if (h.algo == 0) {
+            cudaError_t e = cudaSuccess;
+            switch (h.P.dtype) {
+            case NDCONV_F32: e = ndconv::direct_conv_launch<float>((const float *)h.x, (const float *)h.k, (float *)h.y, h.P.direct<float>(), st, 0); break;
+            case NDCONV_F64: e = ndconv::direct_conv_launch<double>((const double *)h.x, (const double *)h.k, (double *)h.y, h.P.direct<double>(), st, 0); break;
+            case NDCONV_I32: e = ndconv::direct_conv_launch<int32_t>((const int32_t *)h.x, (const int32_t *)h.k, (int32_t *)h.y, h.P.direct<int32_t>(), st, 0); break;
+            case NDCONV_C32: e = ndconv::direct_conv_launch<c32>((const c32 *)h.x, (const c32 *)h.k, (c32 *)h.y, h.P.direct<c32>(), st, 0); break;
+            default: e = ndconv::direct_conv_launch<c64>((const c64 *)h.x, (const c64 *)h.k, (c64 *)h.y, h.P.direct<c64>(), st, 0); break;
+            }
+            if (e != cudaSuccess) return ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e));
+            continue;
+        }
+        int s;
+        switch (h.P.dtype) {
+        case NDCONV_F32: s = ndconv::conv_fft_run<float>(h.P.geom<float>(), h.P.reverse, (const float *)h.x, (const float *)h.k, (float *)h.y, nullptr, st, scr, ndconv::conv_fft_scratch_bytes<float>(h.P.geom<float>())); break;
+        case NDCONV_F64: s = ndconv::conv_fft_run<double>(h.P.geom<double>(), h.P.reverse, (const double *)h.x, (const double *)h.k, (double *)h.y, nullptr, st, scr, ndconv::conv_fft_scratch_bytes<double>(h.P.geom<double>())); break;
+        case NDCONV_C32: s = ndconv::conv_fft_run<c32>(h.P.geom<c32>(), h.P.reverse, (const c32 *)h.x, (const c32 *)h.k, (c32 *)h.y, nullptr, st, scr, ndconv::conv_fft_scratch_bytes<c32>(h.P.geom<c32>())); break;
+        default: s = ndconv::conv_fft_run<c64>(h.P.geom<c64>(), h.P.reverse, (const c64 *)h.x, (const c64 *)h.k, (c64 *)h.y, nullptr, st, scr, ndconv::conv_fft_scratch_bytes<c64>(h.P.geom<c64>())); break;
+        }
+        if (s) return s;
+    }
+    return NDCONV_OK;
+}
+
+extern "C" int ndconv_batch_status(ndconv_batch_plan *B, void *stream) {
+    if (!B) return ndconv_fail(NDCONV_ERR_INVALID, "null plan");
+    int v = 0;
+    NDCONV_CUDA_OK(cudaMemcpyAsync(&v, B->d_ctrs + B->nctrs + 1, sizeof(int), cudaMemcpyDeviceToHost,
+                                   (cudaStream_t)stream));
+    NDCONV_CUDA_OK(cudaStreamSynchronize((cudaStream_t)stream));
+    if (v) return ndconv_fail(NDCONV_ERR_TIMEOUT, "a batch task waited too long for its predecessors");
+    return NDCONV_OK;
+}
+
+extern "C" int ndconv_batch_info(const ndconv_batch_plan *B, int64_t info[8]) {
+    if (!B || !info) return ndconv_fail(NDCONV_ERR_INVALID, "null argument");
+    info[0] = (int64_t)B->tasks.size();
+    info[1] = B->grid;
+    info[2] = (int64_t)B->smem;
+    info[3] = B->n_fft;
+    info[4] = B->n_direct;
+    info[5] = B->n_standalone;
+    info[6] = (int64_t)B->ws_bytes;
+    info[7] = B->nctrs;
+    return NDCONV_OK;
+}
+
+extern "C" int ndconv_batch_destroy(ndconv_batch_plan *B) {
+    if (!B) return NDCONV_OK;
+    cudaDeviceSynchronize();
+    if (B->exec) cudaGraphExecDestroy(B->exec);
+    if (B->graph) cudaGraphDestroy(B->graph);
+    cudaFree(B->d_tasks);
+    cudaFree(B->d_rargs);
+    cudaFree(B->d_cargs);
+    cudaFree(B->d_dargs);
+    cudaFree(B->d_ctrs);
+    cudaFree(B->ws);
+    delete B;
+    return NDCONV_OK;
+}
+
+// ------------------------------------------------ plan facts / cost model --
+// Modelled cost of one instance under each algorithm, used by the default
+// dispatcher and as features of the learned one.  Rates are round numbers
+// for one GB300 (FP32 FMA ~40 T/s, shared memory ~40 TB/s, HBM ~6.8 TB/s);
+// the autotuner's measurements replace them where available.
+extern "C" int ndconv_plan_info(const ndconv_problem *p, double out[8]) {
+    using namespace ndconv;
+    if (!out) return ndconv_fail(NDCONV_ERR_INVALID, "null output");
+    for (int i = 0; i < 8; i++) out[i] = 0;
+    Plan3 P;
+    int s = plan_problem(p, 0, &P);
+    if (s) return s;
+    const AxisGeom *A = P.ax;
+    const double nout = (double)(A[0].out * A[1].out * A[2].out);
+    const double nx = (double)(A[0].n * A[1].n * A[2].n);
+    const double taps = (double)(A[0].K * A[1].K * A[2].K);
+    const int es = (P.dtype == NDCONV_F64 || P.dtype == NDCONV_C32) ? 8 : (P.dtype == NDCONV_C64 ? 16 : 4);
+    const double bytes = es * (nx + taps + nout);
+    const double macs = nout * taps * ((P.dtype == NDCONV_C32 || P.dtype == NDCONV_C64) ? 4 : 1);
+    out[0] = macs / 40e12 + bytes / 6.8e12 + 4e-6;  // direct, seconds
+    out[2] = macs;
+    out[3] = bytes;
+    // FFT: sizes, shared-memory fit, smem-traffic model
+    const bool real = !(P.dtype == NDCONV_C32 || P.dtype == NDCONV_C64);
+    int64_t F[3];
+    for (int a = 0; a < 3; a++) F[a] = (A[a].L == 1) ? 1 : smooth_size(A[a].L, real && a == 2);
+    out[4] = (double)F[0];
+    out[5] = (double)F[1];
+    out[6] = (double)F[2];
+    const int csz = (P.dtype == NDCONV_F64 || P.dtype == NDCONV_C64) ? 16 : 8;
+    const double budget = 100.0 * 1024;  // persistent kernel share
+    bool fits = true;
+    const int64_t M = real ? F[2] / 2 : F[2];
+    if ((double)csz * 2 * (M + 1) * 1.07 > budget) fits = false;
+    for (int a = 0; a < 2; a++)
+        if (F[a] > 1 && (double)csz * 2 * F[a] * 1.07 > budget) fits = false;
+    if (P.dtype == NDCONV_I32) fits = false;
+    if (!fits) {
+        out[1] = 1e30;
+        out[7] = 0;
+        return NDCONV_OK;
+    }
+    auto stages = [](int64_t L) {
+        FftPlanDev pl;
+        if (L <= 1 || !make_plan((int)L, pl)) return 0.0;
+        double c = 0;
+        for (int i = 0; i < pl.nst; i++) c += 1.0;
+        return c;
+    };
+    const double H = real ? (double)(F[2] / 2 + 1) : (double)F[2];
+    const double vol = (double)F[0] * F[1] * H;  // spectrum elements
+    // kernel + data forward, inverse: ~3 transforms, each stage a smem round trip (16 B/elem)
+    const double st = stages(M) + stages(F[1]) + stages(F[0]) + 1;
+    const double smem_bytes = 3.0 * vol * st * 16.0;
+    const double dram = bytes + 4.0 * vol * csz;
+    out[1] = smem_bytes / 40e12 + dram / 6.8e12 + 12e-6;
+    out[7] = 1;
+    return NDCONV_OK;
+}

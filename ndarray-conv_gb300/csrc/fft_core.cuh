@@ -57,6 +57,18 @@ template <typename C> __host__ __device__ __forceinline__ int64_t padded_slots(i
     return n + (n >> (sizeof(C) <= 8 ? 4 : 3)) + 1;
 }
 
+// Load a complex value past L1 (other CTAs of the same launch may have
+// written it).
+template <typename C> __device__ __forceinline__ C ldcg_c(const C *p) {
+    if constexpr (sizeof(C) == 8) {
+        const float2 v = __ldcg(reinterpret_cast<const float2 *>(p));
+        return C{v.x, v.y};
+    } else {
+        const double2 v = __ldcg(reinterpret_cast<const double2 *>(p));
+        return C{v.x, v.y};
+    }
+}
+
 template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
     return C{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
 }

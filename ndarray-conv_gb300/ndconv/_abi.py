@@ -88,6 +88,13 @@ def lib():
         "ndconv_last_error": (ctypes.c_char_p, []),
         "ndconv_version": (ctypes.c_char_p, []),
         "ndconv_kernel_launches": (ctypes.c_uint64, []),
+        "ndconv_batch_create": (ctypes.c_int, [pp, ctypes.c_int64, vp, vp, vp, vp, ctypes.POINTER(vp)]),
+        "ndconv_batch_run": (ctypes.c_int, [vp, i32, vp]),
+        "ndconv_batch_run_plain": (ctypes.c_int, [vp, vp]),
+        "ndconv_batch_status": (ctypes.c_int, [vp, vp]),
+        "ndconv_batch_info": (ctypes.c_int, [vp, i64p]),
+        "ndconv_batch_destroy": (ctypes.c_int, [vp]),
+        "ndconv_plan_info": (ctypes.c_int, [pp, ctypes.POINTER(ctypes.c_double)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

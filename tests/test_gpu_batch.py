@@ -1,0 +1,86 @@
+"""Heterogeneous batches: the persistent work-queue kernel (with and without
+CUDA-graph replay) and the plain per-instance submission must give exactly
+the per-instance entry points' results; one instance is also checked
+against the f64 oracle."""
+import numpy as np
+import pytest
+
+import ndconv
+from helpers import F64, normwise_err, problem, with_dilation
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    import __graft_entry__ as g
+    g.build()
+
+
+def _batch(n, seed, **kw):
+    from ndconv import workloads as W
+    specs = W.uneven_batch(n, seed=seed, **kw)
+    xs, ks = W.make_tensors(specs, seed=seed)
+    kws = [with_dilation(k, s.dilation) for k, s in zip(ks, specs)]
+    modes = [(s.conv_mode(), s.padding_mode()) for s in specs]
+    return specs, xs, ks, kws, modes
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_batch_matches_per_instance(seed):
+    import torch
+    from ndconv.batch import BatchPlan
+    specs, xs, ks, kws, modes = _batch(60, seed, max_log2=14, kmax=31)
+    rng = np.random.default_rng(seed)
+    algos = [int(a) for a in rng.integers(0, 2, len(specs))]
+    plan = BatchPlan(modes, xs, kws, algos=algos)
+    info = plan.info()
+    assert info["tasks"] > 0 and info["n_direct"] + info["n_fft"] + info["n_standalone"] == len(specs)
+    refs = []
+    for i, s in enumerate(specs):
+        f = ndconv.conv if algos[i] == 0 else ndconv.conv_fft
+        refs.append(f(xs[i], kws[i], *modes[i]))
+    for form in ("queue", "graph", "graph2", "plain"):
+        for y in plan.outs:
+            y.fill_(float("nan"))
+        if form == "plain":
+            plan.run_plain()
+        else:
+            plan.run(graph=form != "queue")
+        plan.check()
+        torch.cuda.synchronize()
+        for i in range(len(specs)):
+            assert torch.equal(plan.outs[i], refs[i]), (form, i, specs[i], algos[i])
+    # one instance against the f64 oracle
+    i = int(np.argmax([np.prod(s.shape) for s in specs]))
+    x, k = xs[i].cpu().numpy(), ks[i].cpu().numpy()
+    p = problem(F64, x, with_dilation(k, specs[i].dilation), *modes[i])
+    st, y64 = O.conv(p, x.astype(np.float64), k.astype(np.float64))
+    assert st == 0
+    assert normwise_err(plan.outs[i].cpu().numpy(), y64) <= 1e-5
+    plan.close()
+
+
+def test_batch_mixed_types_standalone():
+    import torch
+    from ndconv import BorderType, ConvMode, PaddingMode
+    from ndconv.batch import BatchPlan
+    g = torch.Generator(device="cuda").manual_seed(3)
+    xs = [torch.rand((30, 40), generator=g, device="cuda", dtype=torch.float64),
+          torch.randint(-9, 9, (50,), generator=g, device="cuda", dtype=torch.int32),
+          torch.rand((8, 9, 10), generator=g, device="cuda")]
+    ks = [torch.rand((3, 5), generator=g, device="cuda", dtype=torch.float64),
+          torch.randint(-9, 9, (7,), generator=g, device="cuda", dtype=torch.int32),
+          torch.rand((3, 3, 3), generator=g, device="cuda")]
+    modes = [(ConvMode.Same, PaddingMode.Reflect), (ConvMode.Full, PaddingMode.Zeros),
+             (ConvMode.Valid, PaddingMode.Custom([BorderType.Zeros] * 3))]
+    algos = [1, 0, 1]
+    plan = BatchPlan(modes, xs, ks, algos=algos)
+    assert plan.info()["n_standalone"] == 2
+    plan.run(graph=True)
+    plan.check()
+    for i in range(3):
+        f = ndconv.conv if algos[i] == 0 else ndconv.conv_fft
+        assert torch.equal(plan.outs[i], f(xs[i], ks[i], *modes[i]))
+    plan.close()
