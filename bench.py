@@ -168,6 +168,185 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def flat_views(shapes, dtype, device):
+    """One flat buffer and per-instance views into it."""
+    import math
+    import torch
+    sizes = [math.prod(s) for s in shapes]
+    buf = torch.empty(sum(sizes), dtype=dtype, device=device)
+    views, off = [], 0
+    for s, n in zip(shapes, sizes):
+        views.append(buf[off:off + n].view(*s))
+        off += n
+    return buf, views
+
+
+def bench_uneven(args, world, rank, local_rank):
+    """Config 4: an uneven batch of independent instances in one persistent
+    launch (device work queue, CUDA graph), against the same instances
+    through the per-instance entry points (the plain drop-in)."""
+    import torch
+    import __graft_entry__ as g
+    g.build()
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from ndconv import _abi, with_dilation
+    from ndconv import workloads as W
+    from ndconv.batch import BatchPlan
+    from ndconv.dispatch import ModelDispatcher
+    L = _abi.lib()
+    specs = W.uneven_batch(args.n_instances, seed=4000 + rank)
+    gen = torch.Generator(device="cuda").manual_seed(4000 + rank)
+    xbuf, xs = flat_views([s.shape for s in specs], torch.float32, "cuda")
+    kbuf, ks = flat_views([s.kshape for s in specs], torch.float32, "cuda")
+    ybuf, ys = flat_views([tuple(s.out_shape()) for s in specs], torch.float32, "cuda")
+    xbuf.uniform_(-1, 1, generator=gen)
+    kbuf.uniform_(-1, 1, generator=gen)
+    algos = ModelDispatcher().choose(specs)
+    plan = BatchPlan([(s.conv_mode(), s.padding_mode()) for s in specs], xs,
+                     [with_dilation(k, s.dilation) for k, s in zip(ks, specs)], outs=ys, algos=algos)
+    info = plan.info()
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    plan.run(graph=False)  # first run outside capture (kernel attributes, tables)
+    for _ in range(args.warmup):
+        plan.run(graph=True)
+    plan.check()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n0 = L.ndconv_kernel_launches()
+    with ClockSampler(local_rank) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            plan.run(graph=True)
+        e1.record(stream)
+        barrier()
+    launches = L.ndconv_kernel_launches() - n0
+    ms = e0.elapsed_time(e1) / args.steps
+    plan.check()
+    # plain per-instance entry points, same algorithms
+    plan.run_plain()
+    barrier()
+    e0.record(stream)
+    nplain = max(1, args.steps // 2)
+    for _ in range(nplain):
+        plan.run_plain()
+    e1.record(stream)
+    barrier()
+    plain_ms = e0.elapsed_time(e1) / nplain
+    # end to end: inputs from pinned host memory, outputs back to it
+    hx, hk = xbuf.cpu().pin_memory(), kbuf.cpu().pin_memory()
+    hy = torch.empty_like(ybuf, device="cpu").pin_memory()
+    for _ in range(2):
+        xbuf.copy_(hx, non_blocking=True)
+        kbuf.copy_(hk, non_blocking=True)
+        plan.run(graph=True)
+        hy.copy_(ybuf, non_blocking=True)
+    barrier()
+    e0.record(stream)
+    for _ in range(args.steps):
+        xbuf.copy_(hx, non_blocking=True)
+        kbuf.copy_(hk, non_blocking=True)
+        plan.run(graph=True)
+        hy.copy_(ybuf, non_blocking=True)
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    if dist:
+        t = torch.tensor([ms, plain_ms, e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms, plain_ms, e2e_ms = [float(v) for v in t.tolist()]
+    bytes_step = sum(s.bytes() for s in specs)
+    peak, peak_kind = peaks()
+    value = bytes_step * world / (ms * 1e-3) / 1e9
+    # parity spot checks against the f64 oracle (largest direct and FFT instances that stay cheap)
+    from oracle import oracle as O
+    from ndconv import build_problem
+    errs = []
+    for want in (0, 1):
+        cand = [i for i, s in enumerate(specs) if algos[i] == want]
+        cand.sort(key=lambda i: specs[i].out_shape()[0] * 0 + int(np.prod(specs[i].out_shape())) *
+                  int(np.prod(specs[i].kshape)))
+        for i in cand[len(cand) // 2: len(cand) // 2 + 2]:
+            s = specs[i]
+            x0, k0 = xs[i].cpu().numpy().astype(np.float64), ks[i].cpu().numpy().astype(np.float64)
+            p = build_problem(_abi.F64, s.shape, with_dilation(k0, s.dilation), s.conv_mode(), s.padding_mode())
+            st, y64 = O.conv(p, x0, k0)
+            if st == 0:
+                y = ys[i].cpu().numpy().astype(np.float64)
+                errs.append(float(np.linalg.norm(y - y64) / max(np.linalg.norm(y64), 1e-300)))
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            cpu = cpu_baseline_uneven(specs, args.cpu_seconds)
+        line = {
+            "metric": "conv GB/s (algorithmic bytes 4*(|x|+|k|+|y|)), uneven batch",
+            "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded; config-4 distribution)",
+            "config": {"workload": f"config4: {len(specs)} uneven instances (rank 1/2/3 = 60/35/5%, "
+                                   "2^8..2^20 elements, odd kernels 3..127, dilation/stride 1|2, "
+                                   "Zeros/Reflect/Replicate/Circular), one persistent launch + CUDA graph",
+                       "instances_per_gpu": len(specs), "algos": {"direct": int(sum(a == 0 for a in algos)),
+                                                                  "fft": int(sum(a == 1 for a in algos))},
+                       "dispatcher": "cost model", "plan": info,
+                       "plain_per_instance_gbs": bytes_step * world / (plain_ms * 1e-3) / 1e9,
+                       "batched_over_plain": plain_ms / ms,
+                       "l2": f"inputs {xbuf.numel() * 4 / 1e9:.2f} GB per GPU, larger than L2, no flush"},
+            "roofline": {"bound": "hbm", "achieved": bytes_step / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": bytes_step / (ms * 1e-3) / 1e9 / peak, "traffic": None,
+                         "kernel": "persistent batch kernel (one launch per step, plus standalone launches)",
+                         "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": bytes_step * world / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s",
+                    "h2d_bytes_per_step": int((xbuf.numel() + kbuf.numel()) * 4),
+                    "d2h_bytes_per_step": int(ybuf.numel() * 4)},
+            "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+            "normwise_err_vs_f64": max(errs) if errs else None,
+        }
+        print(json.dumps(line), flush=True)
+    plan.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def cpu_baseline_uneven(specs, seconds):
+    """The oracle port of conv_fft_par on host cores over a seeded sample of
+    the batch's instances, for ~`seconds`."""
+    from oracle import oracle as O
+    from ndconv import _abi, build_problem, with_dilation
+    nth = os.cpu_count() or 1
+    rng = np.random.default_rng(7)
+    order = rng.permutation(len(specs))
+    done_bytes, n, t0 = 0, 0, time.perf_counter()
+    for i in order:
+        s = specs[i]
+        if np.prod(s.shape) * np.prod([k * s.dilation for k in s.kshape]) > 5e9:
+            continue  # keep the sample bounded
+        x = rng.uniform(-1, 1, s.shape).astype(np.float32)
+        k = rng.uniform(-1, 1, s.kshape).astype(np.float32)
+        p = build_problem(_abi.F32, s.shape, with_dilation(k, s.dilation), s.conv_mode(), s.padding_mode())
+        st, _ = O.conv_fft(p, x, k, nth)
+        if st == 0:
+            done_bytes += s.bytes()
+            n += 1
+        if time.perf_counter() - t0 > seconds:
+            break
+    el = time.perf_counter() - t0
+    return {"value": done_bytes / el / 1e9, "unit": "GB/s", "cores": nth, "kind": "port",
+            "sample": f"{n} random instances of the uneven batch (conv_fft_par port, f32) in {el:.1f} s"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -180,6 +359,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-instances", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--config", default="c2", choices=["c2", "c4"])
+    ap.add_argument("--n-instances", type=int, default=4096)
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -191,6 +372,8 @@ def main():
         O.build()
         return run_reference(args, rank, world)
 
+    if args.config == "c4":
+        return bench_uneven(args, world, rank, local_rank)
     import torch
     import __graft_entry__ as g
     g.build()

@@ -13,9 +13,20 @@
 #include "direct.h"
 #include "direct_blocks.cuh"
 
+#include <type_traits>
+
 namespace ndconv {
 
 // CTA (bx, by, bz) of the tiled kernel; block shape (BX, BY) comes from P.
+template <typename T>
+__global__ void __launch_bounds__(256) dead_tap_fixup_kernel(const T *__restrict__ k0, T *__restrict__ y0,
+                                                             const __grid_constant__ DirectParams<T> P) {
+    const int64_t inst = blockIdx.y;
+    const T *k = P.ks ? P.ks[P.inst_base + inst] : k0;
+    T *y = P.ys ? P.ys[P.inst_base + inst] : y0;
+    dead_tap_fixup_block<T>(k, y, P, blockIdx.x, gridDim.x);
+}
+
 namespace {
 bool sw_disabled() {
     static int v = -1;
@@ -27,10 +38,9 @@ bool sw_disabled() {
 }
 
 template <typename T>
-cudaError_t launch_any(const T *x, const T *k, T *y, DirectParams<T> P, cudaStream_t st, int force_naive,
-                       int64_t n_inst) {
+cudaError_t launch_main(const T *x, const T *k, T *y, DirectParams<T> &P, cudaStream_t st, int force_naive,
+                        int64_t n_inst) {
     const AxisGeom &A0 = P.g.ax[0], &A1 = P.g.ax[1], &A2 = P.g.ax[2];
-    if (A0.out <= 0 || A1.out <= 0 || A2.out <= 0 || n_inst <= 0) return cudaSuccess;
     int BX = 0, BY = 0;
     const bool grid_ok = A0.out * n_inst < 65536 && (A1.out + 7) / 8 < 65536;
     if (!force_naive && grid_ok && A1.out < 65536 && !sw_disabled()) {
@@ -47,6 +57,26 @@ cudaError_t launch_any(const T *x, const T *k, T *y, DirectParams<T> P, cudaStre
     if (blocks > 152 * 64) blocks = 152 * 64;
     if (n_inst > 65535) return cudaErrorInvalidConfiguration;
     direct_naive_kernel<T><<<dim3((unsigned)blocks, (unsigned)n_inst), 256, 0, st>>>(x, k, y, P);
+    ndconv_count_launch();
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_any(const T *x, const T *k, T *y, DirectParams<T> P, cudaStream_t st, int force_naive,
+                       int64_t n_inst) {
+    const AxisGeom &A0 = P.g.ax[0], &A1 = P.g.ax[1], &A2 = P.g.ax[2];
+    if (A0.out <= 0 || A1.out <= 0 || A2.out <= 0 || n_inst <= 0) return cudaSuccess;
+    if (!force_naive) {
+        restrict_live_taps(P);
+        permute_axes_for_tiles(P);
+    }
+    cudaError_t e = launch_main<T>(x, k, y, P, st, force_naive, n_inst);
+    if (e != cudaSuccess || !taps_restricted(P) || std::is_same<T, int32_t>::value) return e;
+    // skipped taps with a non-finite weight: every output is NaN, as in the reference
+    const int64_t nk = A0.K * A1.K * A2.K;
+    int64_t parts = (nk + 4095) / 4096;
+    if (parts > 64) parts = 64;
+    dead_tap_fixup_kernel<T><<<dim3((unsigned)parts, (unsigned)n_inst), 256, 0, st>>>(k, y, P);
     ndconv_count_launch();
     return cudaGetLastError();
 }

@@ -24,6 +24,10 @@ template <typename T> struct DirectParams {
     const T *x1;
     const T *k1;
     T *y1;
+    // live taps per axis: the kernels loop over [t_lo, t_lo + t_n)
+    int64_t t_lo[3], t_n[3];
+    // output element strides per (possibly permuted) axis
+    int64_t ys_[3];
 };
 
 // x, k: device pointers (strided per g.ax[i].xs / ks); y: contiguous output.

@@ -1,6 +1,9 @@
 // Direct-convolution CTA bodies and their tile planners, shared by the
 // standalone kernels (direct.cu) and the persistent batch kernel.
 #pragma once
+#include <type_traits>
+#include <vector>
+
 #include "common.cuh"
 #include "direct.h"
 
@@ -38,15 +41,17 @@ __device__ __forceinline__ void direct_tile_block(const T *__restrict__ x0, cons
     for (int r = 0; r < RX; r++) acc[r] = E::zero();
 
     const int64_t s1 = A1.s, s2 = A2.s, d1 = A1.d, d2 = A2.d;
-    for (int64_t kz = 0; kz < A0.K; kz++) {
+    // live taps only (taps outside [t_lo, t_lo + t_n) read padding zeros for every output)
+    const int64_t kz_end = P.t_lo[0] + P.t_n[0], ky_end = P.t_lo[1] + P.t_n[1], kx_end = P.t_lo[2] + P.t_n[2];
+    for (int64_t kz = P.t_lo[0]; kz < kz_end; kz++) {
         const int64_t mz = axis_map(A0, oz * A0.s + kz * A0.d);
         const int64_t kzs = tap_source(kz, A0.K, P.reverse);
-        for (int64_t ky0 = 0; ky0 < A1.K; ky0 += P.cky) {
-            const int cky = (int)(P.cky < A1.K - ky0 ? P.cky : A1.K - ky0);
+        for (int64_t ky0 = P.t_lo[1]; ky0 < ky_end; ky0 += P.cky) {
+            const int cky = (int)(P.cky < ky_end - ky0 ? P.cky : ky_end - ky0);
             const int64_t row0 = oy0 * s1 + ky0 * d1;
             const int nrows = (int)((BY - 1) * s1 + (cky - 1) * d1 + 1);
-            for (int64_t kx0 = 0; kx0 < A2.K; kx0 += P.ckx) {
-                const int ckx = (int)(P.ckx < A2.K - kx0 ? P.ckx : A2.K - kx0);
+            for (int64_t kx0 = P.t_lo[2]; kx0 < kx_end; kx0 += P.ckx) {
+                const int ckx = (int)(P.ckx < kx_end - kx0 ? P.ckx : kx_end - kx0);
                 const int64_t col0 = ox0 * s2 + kx0 * d2;
                 const int ncols = (int)((TX - 1) * s2 + (ckx - 1) * d2 + 1);
                 __syncthreads();  // previous chunk's compute is done with smem
@@ -81,11 +86,11 @@ __device__ __forceinline__ void direct_tile_block(const T *__restrict__ x0, cons
     }
     const int64_t oy = oy0 + ty;
     if (oy < A1.out) {
-        T *yrow = y + (oz * A1.out + oy) * A2.out;
+        T *yrow = y + oz * P.ys_[0] + oy * P.ys_[1];
 #pragma unroll
         for (int r = 0; r < RX; r++) {
             const int64_t ox = ox0 + tx + (int64_t)r * BX;
-            if (ox < A2.out) yrow[ox] = E::out(acc[r]);
+            if (ox < A2.out) yrow[ox * P.ys_[2]] = E::out(acc[r]);
         }
     }
 }
@@ -144,15 +149,17 @@ __device__ __forceinline__ void direct_sw_block(const T *__restrict__ x0, const 
 #pragma unroll
     for (int r = 0; r < RX; r++) acc[r] = E::zero();
 
-    for (int64_t kz = 0; kz < A0.K; kz++) {
+    // live taps only (taps outside [t_lo, t_lo + t_n) read padding zeros for every output)
+    const int64_t kz_end = P.t_lo[0] + P.t_n[0], ky_end = P.t_lo[1] + P.t_n[1], kx_end = P.t_lo[2] + P.t_n[2];
+    for (int64_t kz = P.t_lo[0]; kz < kz_end; kz++) {
         const int64_t mz = axis_map(A0, oz * A0.s + kz * A0.d);
         const int64_t kzs = tap_source(kz, A0.K, P.reverse);
-        for (int64_t ky0 = 0; ky0 < A1.K; ky0 += P.cky) {
-            const int cky = (int)(P.cky < A1.K - ky0 ? P.cky : A1.K - ky0);
+        for (int64_t ky0 = P.t_lo[1]; ky0 < ky_end; ky0 += P.cky) {
+            const int cky = (int)(P.cky < ky_end - ky0 ? P.cky : ky_end - ky0);
             const int64_t row0 = oy0 * s1 + ky0 * d1;
             const int nrows = (TY - 1) * s1 + (cky - 1) * d1 + 1;
-            for (int64_t kx0 = 0; kx0 < A2.K; kx0 += P.ckx) {
-                const int ckx = (int)(P.ckx < A2.K - kx0 ? P.ckx : A2.K - kx0);
+            for (int64_t kx0 = P.t_lo[2]; kx0 < kx_end; kx0 += P.ckx) {
+                const int ckx = (int)(P.ckx < kx_end - kx0 ? P.ckx : kx_end - kx0);
                 const int64_t col0 = X0 + kx0 * D;
                 const int mlen = NSEG * SEGW + ckx - 1;  // decimated elements per phase
                 const int ncols = D * mlen;
@@ -232,11 +239,11 @@ __device__ __forceinline__ void direct_sw_block(const T *__restrict__ x0, const 
     if (warp < nlines) {
         const int64_t oy = oy0 + ty;
         if (oy < A1.out) {
-            T *yrow = y + (oz * A1.out + oy) * A2.out;
+            T *yrow = y + oz * P.ys_[0] + oy * P.ys_[1];
 #pragma unroll
             for (int r = 0; r < RX; r++) {
                 const int64_t ox = X0 + phi + (int64_t)(sg * SEGW + lane * RX + r) * D;
-                if (ox < A2.out) yrow[ox] = E::out(acc[r]);
+                if (ox < A2.out) yrow[ox * P.ys_[2]] = E::out(acc[r]);
             }
         }
     }
@@ -260,13 +267,13 @@ __device__ __forceinline__ void direct_naive_one(const T *__restrict__ x, const 
     const AxisGeom &A0 = g.ax[0], &A1 = g.ax[1], &A2 = g.ax[2];
     const int64_t ox = o % A2.out, oy = (o / A2.out) % A1.out, oz = o / (A2.out * A1.out);
     Acc acc = E::zero();
-    for (int64_t kz = 0; kz < A0.K; kz++) {
+    for (int64_t kz = P.t_lo[0]; kz < P.t_lo[0] + P.t_n[0]; kz++) {
         const int64_t mz = axis_map(A0, oz * A0.s + kz * A0.d);
         const int64_t kzs = tap_source(kz, A0.K, P.reverse);
-        for (int64_t ky = 0; ky < A1.K; ky++) {
+        for (int64_t ky = P.t_lo[1]; ky < P.t_lo[1] + P.t_n[1]; ky++) {
             const int64_t my = axis_map(A1, oy * A1.s + ky * A1.d);
             const int64_t kys = tap_source(ky, A1.K, P.reverse);
-            for (int64_t kx = 0; kx < A2.K; kx++) {
+            for (int64_t kx = P.t_lo[2]; kx < P.t_lo[2] + P.t_n[2]; kx++) {
                 const T w = k[kzs * A0.ks + kys * A1.ks + tap_source(kx, A2.K, P.reverse) * A2.ks];
                 if (E::is_zero(w)) continue;
                 const int64_t mx = axis_map(A2, ox * A2.s + kx * A2.d);
@@ -274,7 +281,7 @@ __device__ __forceinline__ void direct_naive_one(const T *__restrict__ x, const 
             }
         }
     }
-    y[o] = E::out(acc);
+    y[oz * P.ys_[0] + oy * P.ys_[1] + ox * P.ys_[2]] = E::out(acc);
 }
 
 // the persistent batch kernel's naive task: output o if in range
@@ -297,6 +304,145 @@ __global__ void __launch_bounds__(256) direct_naive_kernel(const T *__restrict__
     for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < total;
          o += (int64_t)gridDim.x * blockDim.x)
         direct_naive_one<T>(x, k, y, P, o);
+}
+
+// ---- live taps -------------------------------------------------------------
+// With every border constant zero, a padded position that does not map to
+// an input sample holds zero.  A tap whose positions are such a zero for
+// every output contributes 0 * w: exactly nothing for finite w, so the
+// kernels loop over the taps [t_lo, t_lo + t_n) that can see data.  If one
+// of the skipped weights is Inf or NaN the reference's sums are NaN for
+// every output (each output has that tap on a zero); dead_tap_fixup
+// reproduces that.
+template <typename T> inline bool host_zero(const T &v) { return v == (T)0; }
+template <> inline bool host_zero<c32>(const c32 &v) { return v.re == 0.0f && v.im == 0.0f; }
+template <> inline bool host_zero<c64>(const c64 &v) { return v.re == 0.0 && v.im == 0.0; }
+
+template <typename T> void restrict_live_taps(DirectParams<T> &P) {
+    for (int a = 0; a < 3; a++) {
+        P.t_lo[a] = 0;
+        P.t_n[a] = P.g.ax[a].K;
+    }
+    for (int a = 0; a < 3; a++)
+        if (!host_zero(P.g.cf[a]) || !host_zero(P.g.cb[a])) return;
+    int64_t lo[3], n[3];
+    for (int a = 0; a < 3; a++) {
+        const AxisGeom &A = P.g.ax[a];
+        lo[a] = 0;
+        n[a] = A.K;
+        if (A.K <= 1 || A.L > (int64_t)1 << 28) continue;
+        // per residue class r mod s: prefix counts of live positions r, r+s, ...
+        const int64_t s = A.s;
+        std::vector<int64_t> pre((size_t)(A.L + s + 1), 0);
+        // pre[r + s*m] = live positions among {r, r+s, ..., r+(m-1)s}
+        for (int64_t r = 0; r < s; r++) {
+            int64_t c = 0;
+            for (int64_t p = r; p < A.L + s; p += s) {
+                pre[(size_t)p] = c;
+                if (p < A.L && axis_map(A, p) >= 0) c++;
+            }
+        }
+        int64_t first = -1, last = -1;
+        for (int64_t t = 0; t < A.K; t++) {
+            const int64_t p0 = t * A.d;
+            const int64_t p1 = p0 + (A.out - 1) * s;  // last position this tap reads
+            if (p0 >= A.L) break;
+            const int64_t r = p0 % s;
+            const int64_t cnt = pre[(size_t)(p1 + s)] - pre[(size_t)p0];
+            (void)r;
+            if (cnt > 0) {
+                if (first < 0) first = t;
+                last = t;
+            }
+        }
+        if (first < 0) return;  // no tap sees data on this axis: keep the full loops
+        lo[a] = first;
+        n[a] = last - first + 1;
+    }
+    for (int a = 0; a < 3; a++) {
+        P.t_lo[a] = lo[a];
+        P.t_n[a] = n[a];
+    }
+}
+
+// With every border constant zero the padded values do not depend on the
+// order in which axes are resolved, so the problem may be computed with its
+// axes permuted (the output written through permuted strides).  Put the
+// longest output axis last (the tiled, contiguous one) and the next longest
+// in the middle.
+template <typename T> void permute_axes_for_tiles(DirectParams<T> &P) {
+    for (int a = 0; a < 3; a++)
+        if (!host_zero(P.g.cf[a]) || !host_zero(P.g.cb[a])) return;
+    int perm[3] = {0, 1, 2};
+    // sort by output extent ascending (stable on ties keeps the original order)
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j + 1 < 3 - i; j++)
+            if (P.g.ax[perm[j]].out > P.g.ax[perm[j + 1]].out) {
+                const int t = perm[j];
+                perm[j] = perm[j + 1];
+                perm[j + 1] = t;
+            }
+    if (perm[0] == 0 && perm[1] == 1 && perm[2] == 2) return;
+    // do not move a contiguous unit-stride axis away for a longer strided one
+    // unless the gain is large (> 4x more outputs)
+    if (P.g.ax[perm[2]].out < 4 * P.g.ax[2].out) return;
+    DirectParams<T> Q = P;
+    for (int i = 0; i < 3; i++) {
+        Q.g.ax[i] = P.g.ax[perm[i]];
+        Q.g.cf[i] = P.g.cf[perm[i]];
+        Q.g.cb[i] = P.g.cb[perm[i]];
+        Q.t_lo[i] = P.t_lo[perm[i]];
+        Q.t_n[i] = P.t_n[perm[i]];
+        Q.ys_[i] = P.ys_[perm[i]];
+    }
+    P = Q;
+}
+
+template <typename T> inline bool taps_restricted(const DirectParams<T> &P) {
+    for (int a = 0; a < 3; a++)
+        if (P.t_lo[a] != 0 || P.t_n[a] != P.g.ax[a].K) return true;
+    return false;
+}
+
+template <typename T> __device__ __forceinline__ bool non_finite(T v) {
+    if constexpr (std::is_same<T, int32_t>::value) return false;  // integers are always finite
+    else if constexpr (Elem<T>::kComplex) return !isfinite(v.re) || !isfinite(v.im);
+    else return !isfinite(v);
+}
+template <typename T> __device__ __forceinline__ T nan_elem() {
+    if constexpr (Elem<T>::kComplex) return T{(decltype(T{}.re))NAN, (decltype(T{}.re))NAN};
+    else return (T)NAN;
+}
+
+// Block-level: scan this block's share of the weights outside the live box;
+// if one is not finite, every output of the instance becomes NaN.
+template <typename T>
+__device__ __forceinline__ void dead_tap_fixup_block(const T *__restrict__ k, T *__restrict__ y,
+                                                     const DirectParams<T> &P, int64_t part, int64_t nparts) {
+    __shared__ int found;
+    if (threadIdx.x == 0) found = 0;
+    __syncthreads();
+    const AxisGeom &A0 = P.g.ax[0], &A1 = P.g.ax[1], &A2 = P.g.ax[2];
+    const int64_t nk = A0.K * A1.K * A2.K;
+    const int64_t chunk = (nk + nparts - 1) / nparts;
+    const int64_t b = part * chunk, e = (b + chunk < nk) ? b + chunk : nk;
+    for (int64_t f = b + threadIdx.x; f < e; f += blockDim.x) {
+        // kernel element (ez, ey, ex) feeds tap (tz, ty, tx) (reversed when convolving)
+        const int64_t ex = f % A2.K, ey = (f / A2.K) % A1.K, ez = f / (A2.K * A1.K);
+        const int64_t tx = tap_source(ex, A2.K, P.reverse), ty = tap_source(ey, A1.K, P.reverse),
+                      tz = tap_source(ez, A0.K, P.reverse);
+        const bool live = tz >= P.t_lo[0] && tz < P.t_lo[0] + P.t_n[0] && ty >= P.t_lo[1] &&
+                          ty < P.t_lo[1] + P.t_n[1] && tx >= P.t_lo[2] && tx < P.t_lo[2] + P.t_n[2];
+        if (live) continue;
+        if (non_finite(k[ez * A0.ks + ey * A1.ks + ex * A2.ks])) found = 1;
+    }
+    __syncthreads();
+    if (!found) return;
+    const int64_t total = A0.out * A1.out * A2.out;
+    for (int64_t o = threadIdx.x; o < total; o += blockDim.x) {
+        const int64_t ox = o % A2.out, oy = (o / A2.out) % A1.out, oz = o / (A2.out * A1.out);
+        y[oz * P.ys_[0] + oy * P.ys_[1] + ox * P.ys_[2]] = nan_elem<T>();
+    }
 }
 
 namespace direct_detail {
@@ -325,13 +471,13 @@ template <typename T> bool plan_tile(DirectParams<T> &P, int RX, int &BX, int &B
         const int64_t TX = (int64_t)BX * RX;
         const int64_t base_cols = (TX - 1) * A2.s + 1;
         if (base_cols > kMaxCols) continue;
-        int64_t ckx = A2.K;
+        int64_t ckx = P.t_n[2];
         if (base_cols + (ckx - 1) * A2.d > kMaxCols) ckx = (kMaxCols - base_cols) / A2.d + 1;
         if (ckx < 1) continue;
         const int64_t W = base_cols + (ckx - 1) * A2.d;
         const int64_t base_rows = (int64_t)(BY - 1) * A1.s + 1;
         // largest cky whose window fits the budget
-        int64_t cky = A1.K;
+        int64_t cky = P.t_n[1];
         auto bytes = [&](int64_t c) {
             const int64_t rows = base_rows + (c - 1) * A1.d;
             return sizeof(T) * (rows * W + c * ckx) + 16 + sizeof(int64_t) * (rows + W);
@@ -375,10 +521,10 @@ template <typename T> bool plan_sw(DirectParams<T> &P, int RX) {
     int Q;
     int64_t rows, cols, rowe;
     // taps per staged chunk along x: all of them if a single kernel row fits
-    int64_t ckx = A2.K;
+    int64_t ckx = P.t_n[2];
     while (ckx > 1 && geom(ckx, 1, Q, rows, cols, rowe) > kSmemBudget) ckx = (ckx + 1) / 2;
     if (geom(ckx, 1, Q, rows, cols, rowe) > kSmemBudget) return false;
-    int64_t cky = A1.K;
+    int64_t cky = P.t_n[1];
     while (cky > 1 && geom(ckx, cky, Q, rows, cols, rowe) > kSmemBudget) cky = (cky + 1) / 2;
     geom(ckx, cky, Q, rows, cols, rowe);
     P.sw_ty = TY;

@@ -1306,6 +1306,14 @@ __device__ __forceinline__ int ld_acquire(const int *p) {
     return v;
 }
 
+// After the queue: instances whose skipped taps hold a non-finite weight
+// get NaN everywhere, like the reference's sums.
+__global__ void __launch_bounds__(256) batch_fixup_kernel(const DirectParams<float> *__restrict__ dargs,
+                                                          const int *__restrict__ fix) {
+    const DirectParams<float> &P = dargs[fix[blockIdx.x]];
+    dead_tap_fixup_block<float>(P.k1, P.y1, P, 0, 1);
+}
+
 __global__ void __launch_bounds__(256) persistent_kernel(const Task *__restrict__ tasks, int ntasks,
                                                          const RowArgs<float> *__restrict__ rargs,
                                                          const ColArgs<c32> *__restrict__ cargs,
@@ -1393,6 +1401,9 @@ struct ndconv_batch_plan {
     std::vector<ndconv::RowArgs<float>> rargs;
     std::vector<ndconv::ColArgs<c32>> cargs;
     std::vector<ndconv::DirectParams<float>> dargs;
+    std::vector<int> fix;  // direct instances with skipped taps (non-finite fix-up after the queue)
+    void *d_fix = nullptr;
+    int64_t graph_kernels = 0;
     int nctrs = 0;
     size_t smem = 0;
     int grid = 0;
@@ -1426,6 +1437,8 @@ size_t direct_tasks(ndconv_batch_plan *B, HostInst &h, std::vector<Task> &out) {
     D.x1 = static_cast<const float *>(h.x);
     D.k1 = static_cast<const float *>(h.k);
     D.y1 = static_cast<float *>(h.y);
+    restrict_live_taps(D);
+    permute_axes_for_tiles(D);
     const AxisGeom &A0 = D.g.ax[0], &A1 = D.g.ax[1], &A2 = D.g.ax[2];
     int kind = 0;
     int64_t gx = 0, gy = 0;
@@ -1449,6 +1462,7 @@ size_t direct_tasks(ndconv_batch_plan *B, HostInst &h, std::vector<Task> &out) {
     }
     const int arg = (int)B->dargs.size();
     B->dargs.push_back(D);
+    if (taps_restricted(D)) B->fix.push_back(arg);
     if (kind == TK_DIRECT_NAIVE) {
         const int64_t total = A0.out * A1.out * A2.out;
         for (int64_t b = 0; b * 256 < total; b++) out.push_back(Task{kind, arg, (int32_t)b, 0, 0, -1, -1, 0});
@@ -1642,7 +1656,8 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
     // ---- device copies
     int s;
     if ((s = upload(B->tasks, &B->d_tasks)) || (s = upload(B->rargs, &B->d_rargs)) ||
-        (s = upload(B->cargs, &B->d_cargs)) || (s = upload(B->dargs, &B->d_dargs)))
+        (s = upload(B->cargs, &B->d_cargs)) || (s = upload(B->dargs, &B->d_dargs)) ||
+        (s = upload(B->fix, &B->d_fix)))
         return fail(s);
     {
         cudaError_t e = cudaMalloc((void **)&B->d_ctrs, sizeof(int) * (size_t)(B->nctrs + 2));
@@ -1711,6 +1726,12 @@ int enqueue(ndconv_batch_plan *B, cudaStream_t st) {
         ndconv_count_launch();
         NDCONV_CUDA_OK(cudaGetLastError());
     }
+    if (!B->fix.empty()) {
+        batch_fixup_kernel<<<(unsigned)B->fix.size(), 256, 0, st>>>((const DirectParams<float> *)B->d_dargs,
+                                                                    (const int *)B->d_fix);
+        ndconv_count_launch();
+        NDCONV_CUDA_OK(cudaGetLastError());
+    }
     return NDCONV_OK;
 }
 
@@ -1735,7 +1756,9 @@ extern "C" int ndconv_batch_run(ndconv_batch_plan *B, int32_t use_graph, void *s
         NDCONV_CUDA_OK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
         cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
         int s = NDCONV_OK;
+        const uint64_t before = ndconv_kernel_launches();
         if (e == cudaSuccess) s = ndconv::batch::enqueue(B, cs);
+        B->graph_kernels = (int64_t)(ndconv_kernel_launches() - before);
         cudaGraph_t g = nullptr;
         cudaError_t e2 = cudaStreamEndCapture(cs, &g);
         cudaStreamDestroy(cs);
@@ -1755,6 +1778,7 @@ extern "C" int ndconv_batch_run(ndconv_batch_plan *B, int32_t use_graph, void *s
         B->graph = g;
     }
     NDCONV_CUDA_OK(cudaGraphLaunch(B->exec, st));
+    ndconv_count_launch((uint64_t)B->graph_kernels);  // the graph's kernels run again
     return NDCONV_OK;
 }
 
@@ -1820,6 +1844,7 @@ extern "C" int ndconv_batch_destroy(ndconv_batch_plan *B) {
     cudaFree(B->d_rargs);
     cudaFree(B->d_cargs);
     cudaFree(B->d_dargs);
+    cudaFree(B->d_fix);
     cudaFree(B->d_ctrs);
     cudaFree(B->ws);
     delete B;
@@ -1841,7 +1866,13 @@ extern "C" int ndconv_plan_info(const ndconv_problem *p, double out[8]) {
     const AxisGeom *A = P.ax;
     const double nout = (double)(A[0].out * A[1].out * A[2].out);
     const double nx = (double)(A[0].n * A[1].n * A[2].n);
-    const double taps = (double)(A[0].K * A[1].K * A[2].K);
+    double taps = (double)(A[0].K * A[1].K * A[2].K);
+    {
+        // the direct kernels only loop over taps that can see data
+        DirectParams<float> D = P.direct<float>();
+        restrict_live_taps(D);
+        taps = (double)(D.t_n[0] * D.t_n[1] * D.t_n[2]);
+    }
     const int es = (P.dtype == NDCONV_F64 || P.dtype == NDCONV_C32) ? 8 : (P.dtype == NDCONV_C64 ? 16 : 4);
     const double bytes = es * (nx + taps + nout);
     const double macs = nout * taps * ((P.dtype == NDCONV_C32 || P.dtype == NDCONV_C64) ? 4 : 1);

@@ -26,6 +26,13 @@ struct Plan3 {
         DirectParams<T> d{};
         d.g = geom<T>();
         d.reverse = reverse;
+        for (int a = 0; a < 3; a++) {
+            d.t_lo[a] = 0;
+            d.t_n[a] = ax[a].K;
+        }
+        d.ys_[2] = 1;
+        d.ys_[1] = ax[2].out;
+        d.ys_[0] = ax[1].out * ax[2].out;
         return d;
     }
 };

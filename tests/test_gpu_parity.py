@@ -348,3 +348,56 @@ def test_batch_i32_bitexact():
         p = problem(I32, x.cpu().numpy(), with_dilation(k.cpu().numpy(), 2), mode, pm)
         st, yo = O.conv(p, x.cpu().numpy(), k.cpu().numpy())
         assert st == 0 and np.array_equal(y.cpu().numpy(), yo)
+
+
+# ---- taps that only ever read padding zeros ----------------------------------------------------
+@pytest.mark.parametrize("shape,kshape,dil,stride,pm", [
+    ((1, 1, 300), (9, 7, 5), 1, 1, PaddingMode.Reflect),
+    ((2, 3, 257), (15, 13, 11), 2, 1, PaddingMode.Zeros),
+    ((3, 2, 100), (11, 9, 7), 1, 2, PaddingMode.Circular),
+    ((1, 500), (31, 9), 2, 2, PaddingMode.Zeros),
+    ((4, 64), (25, 3), 1, 1, PaddingMode.Replicate),
+])
+def test_dead_taps_exact(shape, kshape, dil, stride, pm):
+    rng = np.random.default_rng(sum(shape))
+    keff = [k * dil - dil + 1 for k in kshape]
+    mode = ConvMode.Explicit([[(e - 1) // 2, (e - 1) // 2] for e in keff], [stride] * len(shape))
+    xi = rng.integers(-50, 50, shape).astype(np.int32)
+    ki = rng.integers(-5, 6, kshape).astype(np.int32)
+    p = problem(I32, xi, with_dilation(ki, dil), mode, pm)
+    st, yo = O.conv(p, xi, ki)
+    assert st == 0
+    assert np.array_equal(ndconv.conv(xi, with_dilation(ki, dil), mode, pm), yo)
+    xf, kf = xi.astype(np.float32) / 7, ki.astype(np.float32) / 3
+    y64 = _oracle64(xf, with_dilation(kf, dil), mode, pm)
+    assert normwise_err(ndconv.conv(xf, with_dilation(kf, dil), mode, pm), y64) <= TOL32
+    # a non-finite weight where only padding zeros are read: NaN everywhere, like the oracle
+    for bad in (np.nan, np.inf):
+        kb = kf.copy()
+        kb.flat[0] = bad  # corner tap (reversed: pairs with the far padding)
+        st, yb = O.conv(problem(F64, xf, with_dilation(kb, dil), mode, pm), xf.astype(np.float64),
+                        kb.astype(np.float64))
+        y = ndconv.conv(xf, with_dilation(kb, dil), mode, pm)
+        assert np.array_equal(np.isnan(y), np.isnan(yb))
+        assert np.allclose(y[~np.isnan(y)], yb[~np.isnan(yb)], rtol=1e-4, atol=1e-4)
+
+
+@pytest.mark.parametrize("shape,kshape,dil,stride,pm", [
+    ((50, 1, 7), (9, 5, 11), 2, 2, PaddingMode.Replicate),
+    ((300, 7, 2), (7, 9, 5), 2, 2, PaddingMode.Replicate),
+    ((400, 3), (5, 7), 1, 2, PaddingMode.Reflect),
+    ((9, 200, 2), (3, 5, 3), 1, 1, PaddingMode.Circular),
+])
+def test_long_leading_axis(shape, kshape, dil, stride, pm):
+    # tiny contiguous output axis, long leading one (axes permuted for tiling)
+    rng = np.random.default_rng(len(shape) + shape[0])
+    keff = [k * dil - dil + 1 for k in kshape]
+    mode = ConvMode.Explicit([[(e - 1) // 2, (e - 1) // 2] for e in keff], [stride] * len(shape))
+    xi = rng.integers(-50, 50, shape).astype(np.int32)
+    ki = rng.integers(-5, 6, kshape).astype(np.int32)
+    st, yo = O.conv(problem(I32, xi, with_dilation(ki, dil), mode, pm), xi, ki)
+    assert st == 0
+    assert np.array_equal(ndconv.conv(xi, with_dilation(ki, dil), mode, pm), yo)
+    xf, kf = xi.astype(np.float32) / 7, ki.astype(np.float32) / 3
+    y64 = _oracle64(xf, with_dilation(kf, dil), mode, pm)
+    assert normwise_err(ndconv.conv(xf, with_dilation(kf, dil), mode, pm), y64) <= TOL32
