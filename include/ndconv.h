@@ -123,6 +123,26 @@ int ndconv_conv(const ndconv_problem *p, const void *data, const void *kernel, v
 int ndconv_conv_fft(const ndconv_problem *p, const void *data, const void *kernel, void *out,
                     ndconv_fft_processor *proc, void *stream);
 
+/* Algorithm variants (autotuner candidates).  Every variant computes the same
+ * convolution within the FFT path's tolerance (i32: direct only, exact).
+ * No reference counterpart: the crate has one direct and one FFT method. */
+typedef enum {
+    NDCONV_ALGO_DIRECT = 0,           /* direct, FP32 FMA (sliding-window / tiled kernels) */
+    NDCONV_ALGO_FFT = 1,              /* FFT, form and lengths picked by the cost model */
+    NDCONV_ALGO_DIRECT_BF16X3 = 2,    /* direct, 3xBF16 split products on the tensor cores */
+    NDCONV_ALGO_FFT_ND = 3,           /* FFT, full N-d transform, 7-smooth lengths */
+    NDCONV_ALGO_FFT_RS = 4,           /* FFT along the contiguous axis, leading taps in the spectral domain */
+    NDCONV_ALGO_FFT_ND_POW2 = 5,      /* as FFT_ND with power-of-two lengths */
+    NDCONV_ALGO_FFT_RS_POW2 = 6,      /* as FFT_RS with power-of-two lengths */
+    NDCONV_ALGO_COUNT = 7
+} ndconv_algo;
+
+/* One convolution by the given variant (ndconv_algo).  Direct variants
+ * follow ConvExt::conv's argument rules, FFT variants ConvFFTExt::conv_fft's.
+ * NDCONV_ERR_UNSUPPORTED when the variant does not apply (e.g. FFT of i32). */
+int ndconv_conv_algo(const ndconv_problem *p, int32_t algo, const void *data, const void *kernel, void *out,
+                     void *stream);
+
 /* Batched ConvExt::conv / ConvFFTExt::conv_fft over n instances that share
  * one problem geometry (shapes, dilation, modes); each instance has its
  * own data, kernel and output.  data / kernel / out are DEVICE arrays of n
@@ -136,8 +156,8 @@ int ndconv_conv_fft_batch(const ndconv_problem *p, int64_t n, const void *const 
                           void *stream);
 
 /* Heterogeneous batch: n independent problems (any shapes, kernels, modes,
- * element types), each run by the direct (algo[i] = 0) or FFT (1)
- * algorithm.  No counterpart in the reference (its calls are one instance
+ * element types), each run by the algorithm variant algo[i] (ndconv_algo:
+ * 0 direct, 1 FFT, 3..6 the FFT plan variants).  No counterpart in the reference (its calls are one instance
  * at a time).  data / kernel / out are HOST arrays of n device pointers,
  * bound at creation.  f32 instances become tasks of one persistent kernel
  * driven by a device-side work queue; others run as ordinary launches in
@@ -207,6 +227,26 @@ const char *ndconv_last_error(void);
 
 /* Library version string. */
 const char *ndconv_version(void);
+
+/* ---- learned dispatcher network (no counterpart in the reference) -------
+ * An MLP n_in -> n_hidden -> n_hidden -> n_out with ReLU, f32 parameters in
+ * one flat device array (W1[h][in], b1[h], W2[h][h], b2[h], W3[out][h],
+ * b3[out]).  Loss: sum over (sample, output) of mask * (y - target)^2 /
+ * (2 * sum(mask)).  x, target, mask, y, grad: device pointers, row-major
+ * [n][n_in] / [n][n_out]; loss: device pointer to one float (may be NULL). */
+typedef struct ndconv_mlp ndconv_mlp;
+int ndconv_mlp_create(int32_t n_in, int32_t n_hidden, int32_t n_out, uint64_t seed, ndconv_mlp **out);
+int ndconv_mlp_destroy(ndconv_mlp *net);
+int64_t ndconv_mlp_param_count(const ndconv_mlp *net);
+/* copy all parameters to (set = 0) or from (set = 1) a host array of n floats */
+int ndconv_mlp_params(ndconv_mlp *net, float *host, int64_t n, int32_t set);
+int ndconv_mlp_forward(ndconv_mlp *net, const float *x, int64_t n, float *y, void *stream);
+int ndconv_mlp_gradient(ndconv_mlp *net, const float *x, const float *target, const float *mask, int64_t n,
+                        float *grad, float *loss, void *stream);
+/* Adam over shuffled minibatches for `epochs` passes; final_loss (host
+ * pointer, may be NULL) receives the loss over all n samples afterwards. */
+int ndconv_mlp_train(ndconv_mlp *net, const float *x, const float *target, const float *mask, int64_t n,
+                     int32_t epochs, int32_t batch, float lr, uint64_t seed, float *final_loss, void *stream);
 
 #ifdef __cplusplus
 }

@@ -273,6 +273,40 @@ extern "C" int ndconv_conv_fft(const ndconv_problem *p, const void *data, const 
     return NDCONV_OK;
 }
 
+namespace {
+int fft_variant_of(int32_t algo) {
+    switch (algo) {
+    case NDCONV_ALGO_FFT_ND: return FFTV_ND;
+    case NDCONV_ALGO_FFT_RS: return FFTV_RS;
+    case NDCONV_ALGO_FFT_ND_POW2: return FFTV_ND_POW2;
+    case NDCONV_ALGO_FFT_RS_POW2: return FFTV_RS_POW2;
+    default: return FFTV_AUTO;
+    }
+}
+}  // namespace
+
+extern "C" int ndconv_conv_algo(const ndconv_problem *p, int32_t algo, const void *data, const void *kernel,
+                                void *out, void *stream) {
+    if (algo == NDCONV_ALGO_DIRECT) return ndconv_conv(p, data, kernel, out, stream);
+    if (algo == NDCONV_ALGO_FFT) return ndconv_conv_fft(p, data, kernel, out, nullptr, stream);
+    if (algo == NDCONV_ALGO_DIRECT_BF16X3)
+        return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "3xBF16 direct path not available in this build");
+    if (algo < 0 || algo >= NDCONV_ALGO_COUNT) return ndconv_fail(NDCONV_ERR_INVALID, "unknown algorithm variant");
+    Plan3 P;
+    int s = plan_problem(p, 1, &P);
+    if (s) return s;
+    if (!data || !kernel || !out) return ndconv_fail(NDCONV_ERR_INVALID, "null pointer");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int fv = fft_variant_of(algo);
+    switch (P.dtype) {
+    case NDCONV_F32: return conv_fft_run<float>(P.geom<float>(), P.reverse, (const float *)data, (const float *)kernel, (float *)out, nullptr, st, nullptr, 0, fv);
+    case NDCONV_F64: return conv_fft_run<double>(P.geom<double>(), P.reverse, (const double *)data, (const double *)kernel, (double *)out, nullptr, st, nullptr, 0, fv);
+    case NDCONV_C32: return conv_fft_run<c32>(P.geom<c32>(), P.reverse, (const c32 *)data, (const c32 *)kernel, (c32 *)out, nullptr, st, nullptr, 0, fv);
+    case NDCONV_C64: return conv_fft_run<c64>(P.geom<c64>(), P.reverse, (const c64 *)data, (const c64 *)kernel, (c64 *)out, nullptr, st, nullptr, 0, fv);
+    default: return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "integer FFT convolution is not supported (documented broken upstream)");
+    }
+}
+
 extern "C" int ndconv_conv_batch(const ndconv_problem *p, int64_t n, const void *const *data,
                                  const void *const *kernel, void *const *out, void *stream) {
     Plan3 P;

@@ -102,15 +102,19 @@ __global__ void __launch_bounds__(256) direct_tile_kernel(const T *__restrict__ 
     direct_tile_block<T, RX>(x0, k0, y0, P, blockIdx.x, blockIdx.y, blockIdx.z, smem_raw);
 }
 
-// Sliding-window variant for unit stride along the contiguous axis
-// (s_x == 1, any dilation d_x <= 8).  Output ox = X0 + phi + j d_x reads
-// input X0 + phi + (j + t) d_x for tap t, so each phase phi of the row is an
-// undilated 1-D correlation over the decimated sequence D_phi[m] =
-// row[phi + m d_x].  A warp owns one (output row, phase, segment) line of
-// 32 * RX outputs; lane l owns RX consecutive phase outputs j = l*RX + r and
-// slides a register window over D_phi, so each shared-memory load feeds up
-// to CKX FMAs.  D_phi is stored swizzled (element m at (m % RX) * Q + m / RX)
-// so the lanes' window loads hit consecutive banks.
+// Sliding-window variant along the contiguous axis, any stride s and
+// dilation d (g = gcd(s, d), D = d / g phases, S = s / g tap residues).
+// Output ox = X0 + phi + D j, tap u = rho + S t of a chunk starting at kx0
+// reads padded column X0 s + kx0 d + rho d + s (phi + D (j + t)), so for
+// every (residue rho, phase phi) the outputs are an undilated unit-stride
+// 1-D correlation over the decimated sequence
+//   G[rho][phi][m] = row[X0 s + kx0 d + rho d + s (phi + D m)]
+// with the taps rho, rho + S, ...  (s = 1: one residue, D = d phases).  A
+// warp owns one (output row, phase, segment) line of 32 * RX outputs; lane
+// l owns RX consecutive phase outputs j = l*RX + r and slides a register
+// window over G, so each shared-memory load feeds up to CKX FMAs.  G is
+// stored swizzled (element m at (m % RX) * Q + m / RX) so the lanes' window
+// loads hit consecutive banks.
 template <typename T, int RX, int CKX>
 __device__ __forceinline__ void direct_sw_block(const T *__restrict__ x0, const T *__restrict__ k0,
                                                 T *__restrict__ y0, const DirectParams<T> &P, unsigned bx,
@@ -122,12 +126,15 @@ __device__ __forceinline__ void direct_sw_block(const T *__restrict__ x0, const 
     const T *__restrict__ x = P.xs ? P.xs[P.inst_base + inst] : (P.x1 ? P.x1 : x0);
     const T *__restrict__ k = P.ks ? P.ks[P.inst_base + inst] : (P.k1 ? P.k1 : k0);
     T *__restrict__ y = P.ys ? P.ys[P.inst_base + inst] : (P.y1 ? P.y1 : y0);
-    const int D = (int)A2.d;            // phases
+    const int D = P.sw_ph;              // phases
+    const int S = P.sw_res;             // tap residues
+    const int TR = P.sw_tr;             // weight slots per residue
+    const int SD = S * D;
     const int TY = P.sw_ty, NSEG = P.sw_nseg;
     const int SEGW = 32 * RX;           // phase outputs per line
     const int Q = P.sw_q;               // swizzle pitch
-    const int PH = RX * Q;              // smem elements per phase of one row
-    const int ROWE = D * PH;            // smem elements per staged row
+    const int PH = RX * Q;              // smem elements per (residue, phase) of one row
+    const int ROWE = SD * PH;           // smem elements per staged row
     T *tile = reinterpret_cast<T *>(smem_raw);
     T *wsm = tile + P.tile_elems;
     int64_t *mrow = reinterpret_cast<int64_t *>(smem_raw + P.maps_off);
@@ -144,6 +151,7 @@ __device__ __forceinline__ void direct_sw_block(const T *__restrict__ x0, const 
     const int64_t TXo = (int64_t)NSEG * D * SEGW;
     const int64_t X0 = (int64_t)bx * TXo;
     const int s1 = (int)A1.s, d1 = (int)A1.d;
+    const int64_t s2 = A2.s, d2 = A2.d;
 
     Acc acc[RX];
 #pragma unroll
@@ -160,9 +168,10 @@ __device__ __forceinline__ void direct_sw_block(const T *__restrict__ x0, const 
             const int nrows = (TY - 1) * s1 + (cky - 1) * d1 + 1;
             for (int64_t kx0 = P.t_lo[2]; kx0 < kx_end; kx0 += P.ckx) {
                 const int ckx = (int)(P.ckx < kx_end - kx0 ? P.ckx : kx_end - kx0);
-                const int64_t col0 = X0 + kx0 * D;
-                const int mlen = NSEG * SEGW + ckx - 1;  // decimated elements per phase
-                const int ncols = D * mlen;
+                const int tr0 = (ckx + S - 1) / S;          // taps of residue 0 (the most)
+                const int64_t col0 = X0 * s2 + kx0 * d2;
+                const int mlen = NSEG * SEGW + tr0 - 1;     // decimated elements per (residue, phase)
+                const int ncols = SD * mlen;
                 __syncthreads();
                 // per staged row: data offset of an interior row, or -1 (then the
                 // general border resolution is used); per column: mapped index
@@ -171,15 +180,27 @@ __device__ __forceinline__ void direct_sw_block(const T *__restrict__ x0, const 
                     mrow[i] = my;
                     rowoff[i] = (mz >= 0 && my >= 0) ? mz * A0.xs + my * A1.xs : -1;
                 }
-                for (int i = tid; i < ncols; i += blockDim.x) mcol[i] = axis_map(A2, col0 + i);
+                // column cc = (m, rho, phi) with (rho, phi) fastest: neighbouring
+                // threads read neighbouring columns
+                for (int i = tid; i < ncols; i += blockDim.x) {
+                    const int m = (SD == 1) ? i : i / SD;
+                    const int rem = i - m * SD;
+                    const int rho = rem / D, ph = rem - rho * D;
+                    mcol[i] = axis_map(A2, col0 + rho * d2 + s2 * (ph + (int64_t)D * m));
+                }
                 for (int i = tid; i < cky; i += blockDim.x) zrow[i] = 0;
                 __syncthreads();
-                for (int i = tid; i < cky * ckx; i += blockDim.x) {
-                    const int a = i / ckx, b = i - a * ckx;
-                    const T w = k[kzs * A0.ks + tap_source(ky0 + a, A1.K, P.reverse) * A1.ks +
-                                  tap_source(kx0 + b, A2.K, P.reverse) * A2.ks];
+                for (int i = tid; i < cky * S * TR; i += blockDim.x) {
+                    const int a = i / (S * TR), rem = i - a * (S * TR);
+                    const int rho = rem / TR, t = rem - rho * TR;
+                    const int u = rho + S * t;
+                    T w = E::zero();
+                    if (u < ckx) {
+                        w = k[kzs * A0.ks + tap_source(ky0 + a, A1.K, P.reverse) * A1.ks +
+                              tap_source(kx0 + u, A2.K, P.reverse) * A2.ks];
+                        if (E::is_zero(w)) zrow[a] = 1;  // this kernel row has taps to skip
+                    }
                     wsm[i] = w;
-                    if (E::is_zero(w)) zrow[a] = 1;  // this kernel row has taps to skip
                 }
                 __syncthreads();
                 const int64_t xs2 = A2.xs;
@@ -190,9 +211,9 @@ __device__ __forceinline__ void direct_sw_block(const T *__restrict__ x0, const 
                         const int64_t mc = mcol[cc];
                         const T v = (ro >= 0 && mc >= 0) ? x[ro + mc * xs2]
                                                          : resolve_padded<T>(x, P.g, mz, mrow[rr], mc);
-                        const int ph = (D == 1) ? 0 : cc % D;
-                        const int m = (D == 1) ? cc : cc / D;
-                        trow[ph * PH + (m & (RX - 1)) * Q + m / RX] = v;
+                        const int m = (SD == 1) ? cc : cc / SD;
+                        const int rp = cc - m * SD;  // rho * D + phi
+                        trow[rp * PH + (m & (RX - 1)) * Q + m / RX] = v;
                     }
                 }
                 __syncthreads();
@@ -202,30 +223,34 @@ __device__ __forceinline__ void direct_sw_block(const T *__restrict__ x0, const 
                     // (q % RX) * Q + (jbase + t0) / RX + q / RX
                     const int lbase = sg * (SEGW / RX) + lane;
                     for (int a = 0; a < cky; a++) {
-                        const T *prow = tile + (ty * s1 + a * d1) * ROWE + phi * PH + lbase;
-                        const T *wrow = wsm + a * ckx;
-                        for (int t0 = 0; t0 < ckx; t0 += CKX) {
-                            T win[RX + CKX - 1];
-                            const T *pw = prow + t0 / RX;
+                        const T *prow_a = tile + (ty * s1 + a * d1) * ROWE + phi * PH + lbase;
+                        for (int rho = 0; rho < S; rho++) {
+                            const T *prow = prow_a + rho * D * PH;
+                            const T *wrow = wsm + (a * S + rho) * TR;
+                            const int ckr = (ckx - rho + S - 1) / S;  // taps of this residue
+                            for (int t0 = 0; t0 < ckr; t0 += CKX) {
+                                T win[RX + CKX - 1];
+                                const T *pw = prow + t0 / RX;
 #pragma unroll
-                            for (int q = 0; q < RX + CKX - 1; q++)
-                                win[q] = (t0 + q < ckx + RX - 1) ? pw[(q % RX) * Q + q / RX] : E::zero();
-                            if (t0 + CKX <= ckx && !zrow[a]) {
-                                // full chunk without zero taps: no per-tap branches
+                                for (int q = 0; q < RX + CKX - 1; q++)
+                                    win[q] = (t0 + q < ckr + RX - 1) ? pw[(q % RX) * Q + q / RX] : E::zero();
+                                if (t0 + CKX <= ckr && !zrow[a]) {
+                                    // full chunk without zero taps: no per-tap branches
 #pragma unroll
-                                for (int t = 0; t < CKX; t++) {
-                                    const T w = wrow[t0 + t];
-#pragma unroll
-                                    for (int r = 0; r < RX; r++) E::mac(acc[r], win[r + t], w);
-                                }
-                            } else {
-#pragma unroll
-                                for (int t = 0; t < CKX; t++) {
-                                    if (t0 + t < ckx) {
+                                    for (int t = 0; t < CKX; t++) {
                                         const T w = wrow[t0 + t];
-                                        if (!E::is_zero(w)) {
 #pragma unroll
-                                            for (int r = 0; r < RX; r++) E::mac(acc[r], win[r + t], w);
+                                        for (int r = 0; r < RX; r++) E::mac(acc[r], win[r + t], w);
+                                    }
+                                } else {
+#pragma unroll
+                                    for (int t = 0; t < CKX; t++) {
+                                        if (t0 + t < ckr) {
+                                            const T w = wrow[t0 + t];
+                                            if (!E::is_zero(w)) {
+#pragma unroll
+                                                for (int r = 0; r < RX; r++) E::mac(acc[r], win[r + t], w);
+                                            }
                                         }
                                     }
                                 }
@@ -365,39 +390,6 @@ template <typename T> void restrict_live_taps(DirectParams<T> &P) {
     }
 }
 
-// With every border constant zero the padded values do not depend on the
-// order in which axes are resolved, so the problem may be computed with its
-// axes permuted (the output written through permuted strides).  Put the
-// longest output axis last (the tiled, contiguous one) and the next longest
-// in the middle.
-template <typename T> void permute_axes_for_tiles(DirectParams<T> &P) {
-    for (int a = 0; a < 3; a++)
-        if (!host_zero(P.g.cf[a]) || !host_zero(P.g.cb[a])) return;
-    int perm[3] = {0, 1, 2};
-    // sort by output extent ascending (stable on ties keeps the original order)
-    for (int i = 0; i < 3; i++)
-        for (int j = 0; j + 1 < 3 - i; j++)
-            if (P.g.ax[perm[j]].out > P.g.ax[perm[j + 1]].out) {
-                const int t = perm[j];
-                perm[j] = perm[j + 1];
-                perm[j + 1] = t;
-            }
-    if (perm[0] == 0 && perm[1] == 1 && perm[2] == 2) return;
-    // do not move a contiguous unit-stride axis away for a longer strided one
-    // unless the gain is large (> 4x more outputs)
-    if (P.g.ax[perm[2]].out < 4 * P.g.ax[2].out) return;
-    DirectParams<T> Q = P;
-    for (int i = 0; i < 3; i++) {
-        Q.g.ax[i] = P.g.ax[perm[i]];
-        Q.g.cf[i] = P.g.cf[perm[i]];
-        Q.g.cb[i] = P.g.cb[perm[i]];
-        Q.t_lo[i] = P.t_lo[perm[i]];
-        Q.t_n[i] = P.t_n[perm[i]];
-        Q.ys_[i] = P.ys_[perm[i]];
-    }
-    P = Q;
-}
-
 template <typename T> inline bool taps_restricted(const DirectParams<T> &P) {
     for (int a = 0; a < 3; a++)
         if (P.t_lo[a] != 0 || P.t_n[a] != P.g.ax[a].K) return true;
@@ -498,11 +490,31 @@ template <typename T> bool plan_tile(DirectParams<T> &P, int RX, int &BX, int &B
     return false;
 }
 
+inline int64_t gcd64(int64_t a, int64_t b) {
+    while (b) {
+        const int64_t t = a % b;
+        a = b;
+        b = t;
+    }
+    return a;
+}
+
+// Phases D = d / gcd(s, d) and tap residues S = s / gcd(s, d) of the
+// contiguous axis; the sliding-window kernel takes D <= 8 and S * D <= 8.
+inline bool sw_axis_ok(const AxisGeom &A2, int &D, int &S) {
+    const int64_t g = gcd64(A2.s, A2.d);
+    const int64_t d = A2.d / g, s = A2.s / g;
+    if (d > 8 || s * d > 8) return false;
+    D = (int)d;
+    S = (int)s;
+    return true;
+}
+
 // Sliding-window tiling: warps = TY rows x NSEG segments x D phases (<= 8).
 template <typename T> bool plan_sw(DirectParams<T> &P, int RX) {
     const AxisGeom &A1 = P.g.ax[1], &A2 = P.g.ax[2];
-    if (A2.s != 1 || A2.d > 8) return false;
-    const int D = (int)A2.d;
+    int D, S;
+    if (!sw_axis_ok(A2, D, S)) return false;
     const int lines = 8 / D;
     int TY = 1;
     while (TY * 2 <= lines && TY * 2 <= A1.out) TY *= 2;
@@ -511,11 +523,12 @@ template <typename T> bool plan_sw(DirectParams<T> &P, int RX) {
     const int64_t segs_needed = (A2.out + (int64_t)D * SEGW - 1) / ((int64_t)D * SEGW);
     if (NSEG > segs_needed) NSEG = (int)(segs_needed < 1 ? 1 : segs_needed);
     auto geom = [&](int64_t ckx, int64_t cky, int &Q, int64_t &rows, int64_t &cols, int64_t &rowe) {
-        Q = (int)((NSEG * SEGW + ckx - 1 + RX - 1) / RX);
-        rowe = (int64_t)D * RX * Q;
+        const int64_t tr = (ckx + S - 1) / S;
+        Q = (int)((NSEG * SEGW + tr - 1 + RX - 1) / RX);
+        rowe = (int64_t)S * D * RX * Q;
         rows = (TY - 1) * A1.s + (cky - 1) * A1.d + 1;
-        cols = (int64_t)D * (NSEG * SEGW + ckx - 1);
-        return sizeof(T) * (rows * rowe + cky * ckx) + 16 + sizeof(int64_t) * (2 * rows + cols) +
+        cols = (int64_t)S * D * (NSEG * SEGW + tr - 1);
+        return sizeof(T) * (rows * rowe + cky * S * tr) + 16 + sizeof(int64_t) * (2 * rows + cols) +
                sizeof(int) * cky;
     };
     int Q;
@@ -530,14 +543,22 @@ template <typename T> bool plan_sw(DirectParams<T> &P, int RX) {
     P.sw_ty = TY;
     P.sw_nseg = NSEG;
     P.sw_q = Q;
+    P.sw_ph = D;
+    P.sw_res = S;
+    P.sw_tr = (int)((ckx + S - 1) / S);
     P.cky = cky;
     P.ckx = ckx;
     P.max_rows = rows;
     P.max_cols = cols;
     P.tile_elems = rows * rowe;
-    P.w_elems = cky * ckx;
+    P.w_elems = cky * S * P.sw_tr;
     P.maps_off = ((int64_t)sizeof(T) * (P.tile_elems + P.w_elems) + 15) / 16 * 16;
     return true;
+}
+
+// Output columns one sliding-window CTA covers.
+template <typename T> inline int64_t sw_cols_per_cta(const DirectParams<T> &P, int RX) {
+    return (int64_t)P.sw_nseg * P.sw_ph * 32 * RX;
 }
 
 template <typename T, int RX, int CKX>
@@ -548,7 +569,7 @@ cudaError_t launch_sw(const T *x, const T *k, T *y, const DirectParams<T> &P, cu
     cudaError_t e = ndconv_allow_smem((const void *)fn, (int)kSmemBudget + 4096);
     if (e != cudaSuccess) return e;
     const AxisGeom &A0 = P.g.ax[0], &A1 = P.g.ax[1], &A2 = P.g.ax[2];
-    const int64_t TXo = (int64_t)P.sw_nseg * A2.d * 32 * RX;
+    const int64_t TXo = sw_cols_per_cta(P, RX);
     dim3 grid((unsigned)((A2.out + TXo - 1) / TXo), (unsigned)((A1.out + P.sw_ty - 1) / P.sw_ty),
               (unsigned)(A0.out * n_inst));
     fn<<<grid, 256, sm, st>>>(x, k, y, P);
@@ -572,6 +593,95 @@ template <typename T, int RX> cudaError_t launch_tile(const T *x, const T *k, T 
 }
 }  // namespace direct_detail
 using namespace direct_detail;
+
+// Estimated issue slots (warp instructions) of a sliding-window launch of
+// RX outputs per lane and CKX-tap windows, after plan_sw: staging of the
+// padded window (a global load, border map and swizzled store per element;
+// a strided x axis costs whole sectors), and the window loads + FMAs.
+template <typename T> double sw_cost(const DirectParams<T> &P, int RX, int CKX) {
+    const AxisGeom &A0 = P.g.ax[0], &A1 = P.g.ax[1], &A2 = P.g.ax[2];
+    const int64_t TXo = sw_cols_per_cta(P, RX);
+    const double ctas = (double)((A2.out + TXo - 1) / TXo) * (double)((A1.out + P.sw_ty - 1) / P.sw_ty) *
+                        (double)A0.out;
+    const int S = P.sw_res, D = P.sw_ph, TY = P.sw_ty;
+    const double nlines = (double)TY * P.sw_nseg * D;
+    double per_cta = 0;
+    const int64_t ny = (P.t_n[1] + P.cky - 1) / P.cky, nx = (P.t_n[2] + P.ckx - 1) / P.ckx;
+    for (int64_t iy = 0; iy < ny; iy++) {
+        const int64_t cky = iy + 1 < ny ? P.cky : P.t_n[1] - iy * P.cky;
+        const int64_t rows = (TY - 1) * A1.s + (cky - 1) * A1.d + 1;
+        for (int64_t ix = 0; ix < nx; ix++) {
+            const int64_t ckx = ix + 1 < nx ? P.ckx : P.t_n[2] - ix * P.ckx;
+            const int64_t tr0 = (ckx + S - 1) / S;
+            const double cols = (double)S * D * (P.sw_nseg * 32.0 * RX + tr0 - 1);
+            const double stage = rows * cols / 32.0 * ((A2.xs == 1 || A2.xs == -1) ? 10.0 : 24.0) +
+                                 (rows + cols) / 32.0 * 30.0 + 200.0;
+            double comp = 0;
+            for (int r = 0; r < S; r++) {
+                const int64_t ckr = (ckx - r + S - 1) / S;
+                comp += (double)((ckr + CKX - 1) / CKX) * (2.0 * (RX + CKX - 1) + (double)CKX * RX);
+            }
+            per_cta += stage + nlines * cky * comp;
+        }
+    }
+    return ctas * per_cta * (double)P.t_n[0];
+}
+
+// With every border constant zero the padded values do not depend on the
+// order in which axes are resolved, so the problem may be computed with its
+// axes permuted (the output written through permuted strides).  Of the six
+// orders, take the one whose sliding-window launch has the lowest estimated
+// cost; when no order fits that kernel, put the longest output axis last
+// (the tiled one) and the next longest in the middle.
+template <typename T> void permute_axes_for_tiles(DirectParams<T> &P) {
+    for (int a = 0; a < 3; a++)
+        if (!host_zero(P.g.cf[a]) || !host_zero(P.g.cb[a])) return;
+    auto permuted = [&](const int *perm) {
+        DirectParams<T> Q = P;
+        for (int i = 0; i < 3; i++) {
+            Q.g.ax[i] = P.g.ax[perm[i]];
+            Q.g.cf[i] = P.g.cf[perm[i]];
+            Q.g.cb[i] = P.g.cb[perm[i]];
+            Q.t_lo[i] = P.t_lo[perm[i]];
+            Q.t_n[i] = P.t_n[perm[i]];
+            Q.ys_[i] = P.ys_[perm[i]];
+        }
+        return Q;
+    };
+    constexpr int RX = (sizeof(T) <= 4) ? 8 : 4;
+    static const int perms[6][3] = {{0, 1, 2}, {1, 0, 2}, {0, 2, 1}, {2, 0, 1}, {1, 2, 0}, {2, 1, 0}};
+    double best = 0;
+    int pick = -1;
+    for (int i = 0; i < 6; i++) {
+        DirectParams<T> Q = permuted(perms[i]);
+        // the grid's y and z extents are limited to 65535
+        if (Q.g.ax[0].out >= 65536 || Q.g.ax[1].out >= 65536) continue;
+        if (!plan_sw(Q, RX)) continue;
+        const double c = sw_cost(Q, RX, 2 * RX);
+        if (pick < 0 || c < best * 0.9) {
+            best = c;
+            pick = i;
+        }
+    }
+    if (pick >= 0) {
+        if (pick > 0) P = permuted(perms[pick]);
+        return;
+    }
+    int perm[3] = {0, 1, 2};
+    // sort by output extent ascending (stable on ties keeps the original order)
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j + 1 < 3 - i; j++)
+            if (P.g.ax[perm[j]].out > P.g.ax[perm[j + 1]].out) {
+                const int t = perm[j];
+                perm[j] = perm[j + 1];
+                perm[j + 1] = t;
+            }
+    if (perm[0] == 0 && perm[1] == 1 && perm[2] == 2) return;
+    // do not move a contiguous unit-stride axis away for a longer strided one
+    // unless the gain is large (> 4x more outputs)
+    if (P.g.ax[perm[2]].out < 4 * P.g.ax[2].out) return;
+    P = permuted(perm);
+}
 
 
 }  // namespace ndconv

@@ -17,6 +17,7 @@
 // length >= pds gives the same cropped result as the reference's good_size
 // (the circular wrap only touches indices < k_eff - 1).
 #include <algorithm>
+#include <cmath>
 #include <map>
 #include <string>
 #include <mutex>
@@ -182,6 +183,12 @@ int64_t smooth_size(int64_t n, bool even) {
     return best;
 }
 
+int64_t pow2_size(int64_t n, bool even) {
+    int64_t v = even ? 2 : 1;
+    while (v < n) v *= 2;
+    return v;
+}
+
 // ------------------------------------------------------------- row pass --
 enum RowMode : int {
     ROW_FWD_DATA = 0,    // padded data row -> spectrum row
@@ -190,6 +197,7 @@ enum RowMode : int {
     ROW_FUSED = 3,       // rank 1: data row -> fwd -> * Kh -> inv -> cropped output
     ROW_FWD_PLAIN = 4,   // contiguous input row -> spectrum row (processor API)
     ROW_INV_PLAIN = 5,   // spectrum row -> scaled contiguous output row (processor API)
+    ROW_INV_MAC = 6,     // sum over leading-axis taps of kernel row x data row spectra -> output row
 };
 enum RowKind : int { RK_COMPLEX = 0, RK_REAL_EVEN = 1, RK_REAL_ODD = 2 };
 
@@ -225,6 +233,13 @@ template <typename T> struct RowArgs {
     const C *twF;    // table for F (real even)
     R scale;
     int nb, lognb;
+    // row-spectral form (FFT along the contiguous axis only, taps of the
+    // leading axes summed in the spectral domain):
+    int kcompact;            // FWD_KERNEL: rows are the K0 x K1 kernel rows in tap order
+    int l2only;              // INV_MAC: read spectra through L2 only (same-launch producers)
+    int mk0, mk1;            // INV_MAC: leading-axis taps
+    int64_t mbase0, mbase1;  // INV_MAC: spectrum offset per output index (stride x row pitch)
+    int64_t mstep0, mstep1;  // INV_MAC: spectrum offset per tap (dilation x row pitch)
 };
 
 // kernel-buffer value at padded position j of one axis: tap index or -1
@@ -355,8 +370,15 @@ __device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsi
             ri.interior = ri.m0 >= 0 && ri.m1 >= 0;
             ri.xoff = ri.interior ? ri.m0 * A.g.ax[0].xs + ri.m1 * A.g.ax[1].xs : 0;
         } else if constexpr (MODE == ROW_FWD_KERNEL) {
-            ri.t0 = kbuf_tap(A.g.ax[0], i0, A.reverse);
-            ri.t1 = kbuf_tap(A.g.ax[1], i1, A.reverse);
+            if (A.kcompact) {
+                ri.t0 = tap_source(i0, A.g.ax[0].K, A.reverse);
+                ri.t1 = tap_source(i1, A.g.ax[1].K, A.reverse);
+            } else {
+                ri.t0 = kbuf_tap(A.g.ax[0], i0, A.reverse);
+                ri.t1 = kbuf_tap(A.g.ax[1], i1, A.reverse);
+            }
+        } else if constexpr (MODE == ROW_INV_MAC) {
+            ri.soff = i0 * A.mbase0 + i1 * A.mbase1;
         }
         rinfo[b] = ri;
     }
@@ -435,10 +457,46 @@ __device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsi
         const int H = (int)A.H;
         const int tot = H << lognb;
         C *dst = (A.kind == RK_REAL_EVEN) ? buf1 : buf0;
-        for (int u = threadIdx.x; u < tot; u += blockDim.x) {
-            const int b = u & (nb - 1), k = u >> lognb;
-            const RowInfo &ri = rinfo[b];
-            dst[sx<C>(u)] = ri.valid ? ldcg_c(spec + ri.soff + k) : C{0, 0};
+        if constexpr (MODE == ROW_INV_MAC) {
+            // output row spectrum = sum over leading taps (tz, ty) of kernel row
+            // (tz, ty) times data row (o0 s0 + tz d0, o1 s1 + ty d1)
+            const int mk0 = A.mk0, mk1 = A.mk1;
+            const int64_t st0 = A.mstep0, st1 = A.mstep1, Hh = A.H;
+            for (int u = threadIdx.x; u < tot; u += blockDim.x) {
+                const int b = u & (nb - 1), k = u >> lognb;
+                const RowInfo &ri = rinfo[b];
+                C acc{0, 0};
+                if (ri.valid) {
+                    const C *kq = kspec + k;
+                    const C *sp0 = spec + ri.soff + k;
+                    if (A.l2only) {
+                        for (int tz = 0; tz < mk0; tz++, sp0 += st0) {
+                            const C *sp = sp0;
+                            for (int ty = 0; ty < mk1; ty++, sp += st1, kq += Hh) {
+                                const C kv = ldcg_c(kq), dv = ldcg_c(sp);
+                                acc.re = fmaf_t(kv.re, dv.re, fmaf_t(-kv.im, dv.im, acc.re));
+                                acc.im = fmaf_t(kv.re, dv.im, fmaf_t(kv.im, dv.re, acc.im));
+                            }
+                        }
+                    } else {
+                        for (int tz = 0; tz < mk0; tz++, sp0 += st0) {
+                            const C *sp = sp0;
+                            for (int ty = 0; ty < mk1; ty++, sp += st1, kq += Hh) {
+                                const C kv = ldg_c(kq), dv = ldg_c(sp);
+                                acc.re = fmaf_t(kv.re, dv.re, fmaf_t(-kv.im, dv.im, acc.re));
+                                acc.im = fmaf_t(kv.re, dv.im, fmaf_t(kv.im, dv.re, acc.im));
+                            }
+                        }
+                    }
+                }
+                dst[sx<C>(u)] = acc;
+            }
+        } else {
+            for (int u = threadIdx.x; u < tot; u += blockDim.x) {
+                const int b = u & (nb - 1), k = u >> lognb;
+                const RowInfo &ri = rinfo[b];
+                dst[sx<C>(u)] = ri.valid ? ldcg_c(spec + ri.soff + k) : C{0, 0};
+            }
         }
         __syncthreads();
         if (A.kind == RK_REAL_ODD) {
@@ -667,8 +725,37 @@ template <typename T> int launch_row(RowArgs<T> A, cudaStream_t st, int n_inst =
     case ROW_INV_OUT: return launch_row_mode<T, ROW_INV_OUT>(A, sm, (unsigned)grid, n_inst, st);
     case ROW_FUSED: return launch_row_mode<T, ROW_FUSED>(A, sm, (unsigned)grid, n_inst, st);
     case ROW_FWD_PLAIN: return launch_row_mode<T, ROW_FWD_PLAIN>(A, sm, (unsigned)grid, n_inst, st);
+    case ROW_INV_MAC: return launch_row_mode<T, ROW_INV_MAC>(A, sm, (unsigned)grid, n_inst, st);
     default: return launch_row_mode<T, ROW_INV_PLAIN>(A, sm, (unsigned)grid, n_inst, st);
     }
+}
+
+// Two independent forward row passes in one launch (the kernel rows and the
+// data rows of the row-spectral form): CTAs [0, ga) take pass A, the rest B.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) row_pair_kernel(const __grid_constant__ RowArgs<T> A,
+                                                            const __grid_constant__ RowArgs<T> B, unsigned ga) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    if (blockIdx.x < ga) row_block<T, ROW_FWD_KERNEL>(A, blockIdx.x, blockIdx.y, smem_raw);
+    else row_block<T, ROW_FWD_DATA>(B, blockIdx.x - ga, blockIdx.y, smem_raw);
+}
+
+template <typename T> int launch_row_pair(RowArgs<T> A, RowArgs<T> B, cudaStream_t st, int n_inst) {
+    if (n_inst <= 0) return NDCONV_OK;
+    if (A.n_rows <= 0) return launch_row<T>(B, st, n_inst);
+    if (B.n_rows <= 0) return launch_row<T>(A, st, n_inst);
+    int64_t ga, gb;
+    size_t sa, sb;
+    int s = prep_row(A, n_inst, ga, sa);
+    if (s) return s;
+    if ((s = prep_row(B, n_inst, gb, sb))) return s;
+    if (ga + gb > 0x7fffffff) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "too many FFT rows");
+    if ((s = ensure_smem(row_pair_kernel<T>))) return s;
+    row_pair_kernel<T><<<dim3((unsigned)(ga + gb), (unsigned)n_inst), kThreads, std::max(sa, sb), st>>>(
+        A, B, (unsigned)ga);
+    ndconv_count_launch();
+    NDCONV_CUDA_OK(cudaGetLastError());
+    return NDCONV_OK;
 }
 
 // Fill nb / lognb and the launch shape of a column pass.
@@ -786,18 +873,44 @@ template <typename T> struct FftConvPlan {
     using C = typename CplxT<R>::type;
     int64_t P[3], F[3], H;
     int astar;
+    int rs;  // row-spectral form: FFT along the contiguous axis only
     RowArgs<T> rk;  // row plan (kind, pl, tw, twF, F, H)
     FftPlanDev pl0, pl1;
     const C *tw0, *tw1;
     size_t nK, nS;  // complex elements of Kh and S per instance
 };
 
-template <typename T> int make_conv_plan(const Geom3<T> &g, FftConvPlan<T> &cp) {
+// Row-spectral form vs full N-d FFT, by a flop model (an FFT of length n
+// ~ 5 n log2 n flops, half for a real row; a spectral tap ~ 16 flop-equivalents
+// with its two loads; a spectrum byte through HBM ~ 4.4 flop-equivalents).
+// The row-spectral form skips the column transforms and their spectrum
+// round trips at the price of |K0 x K1| complex MACs per output bin.
+template <typename T> bool rs_preferred(const Geom3<T> &g, const FftConvPlan<T> &cp) {
+    const AxisGeom &A0 = g.ax[0], &A1 = g.ax[1];
+    auto lg = [](double n) { return n > 1 ? std::log2(n) : 0.0; };
+    const bool real = !Elem<T>::kComplex;
+    const double F0 = (double)cp.F[0], F1 = (double)cp.F[1], F2 = (double)cp.F[2], H = (double)cp.H;
+    const double rowc = (real ? 2.5 : 5.0) * F2 * lg(F2);
+    const double common = rowc * ((double)cp.P[0] * cp.P[1] + (double)A0.out * A1.out);
+    const double taps = (double)A0.K * A1.K;
+    const double rs = common + rowc * taps + 16.0 * (double)A0.out * A1.out * H * taps;
+    double col = common + rowc * (double)A0.keff * A1.keff;
+    const double vol = F0 * F1 * H;
+    if (cp.F[1] > 1) col += 5.0 * F1 * lg(F1) * H * ((double)A0.keff + cp.P[0] + 2.0 * A0.out);
+    if (cp.F[0] > 1) col += 5.0 * F0 * lg(F0) * F1 * H * 3.0;
+    const double csz = (double)sizeof(typename FftConvPlan<T>::C);
+    const int passes = (cp.F[0] > 1 ? 2 : 0) + (cp.F[1] > 1 ? 2 : 0);
+    col += 4.4 * csz * vol * (2.0 * passes + 2.0);
+    return rs < col;
+}
+
+template <typename T> int make_conv_plan(const Geom3<T> &g, FftConvPlan<T> &cp, int variant = FFTV_AUTO) {
     using C = typename FftConvPlan<T>::C;
     const bool real = !Elem<T>::kComplex;
+    const bool pow2 = (variant == FFTV_ND_POW2 || variant == FFTV_RS_POW2);
     for (int a = 0; a < 3; a++) {
         cp.P[a] = g.ax[a].L;
-        cp.F[a] = (cp.P[a] == 1) ? 1 : smooth_size(cp.P[a], real && a == 2);
+        cp.F[a] = (cp.P[a] == 1) ? 1 : (pow2 ? pow2_size(cp.P[a], real && a == 2) : smooth_size(cp.P[a], real && a == 2));
     }
     cp.astar = cp.F[0] > 1 ? 0 : (cp.F[1] > 1 ? 1 : 2);
     cp.rk = RowArgs<T>{};
@@ -811,6 +924,14 @@ template <typename T> int make_conv_plan(const Geom3<T> &g, FftConvPlan<T> &cp) 
     if (cp.F[1] > 1 && (s = plan_with_tw<C>(cp.F[1], cp.pl1, &cp.tw1))) return s;
     cp.nK = (size_t)cp.F[0] * cp.F[1] * cp.H;
     cp.nS = (cp.astar == 2) ? 0 : (size_t)cp.P[0] * cp.F[1] * cp.H;
+    cp.rs = 0;
+    const bool want_rs = (variant == FFTV_RS || variant == FFTV_RS_POW2) ||
+                         (variant == FFTV_AUTO && rs_preferred(g, cp));
+    if (cp.astar < 2 && want_rs) {
+        cp.rs = 1;
+        cp.nK = (size_t)g.ax[0].K * g.ax[1].K * cp.H;
+        cp.nS = (size_t)cp.P[0] * cp.P[1] * cp.H;
+    }
     return NDCONV_OK;
 }
 
@@ -818,17 +939,77 @@ template <typename T> int make_conv_plan(const Geom3<T> &g, FftConvPlan<T> &cp) 
 // emit_col (launch them, or record them as tasks).  Kh / S hold cnt
 // instances' spectra back to back.  Pointers come from the device arrays
 // xs / ks / ys when given, else x / k / y (cnt == 1).
-template <typename T, typename EmitRow, typename EmitCol>
+template <typename T, typename EmitRow, typename EmitCol, typename EmitPair>
 int conv_fft_passes(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, const T *x, const T *k, T *y,
                     const T *const *xs, const T *const *ks, T *const *ys, int64_t base, int cnt,
                     typename FftConvPlan<T>::C *Kh, typename FftConvPlan<T>::C *S, EmitRow &&emit_row,
-                    EmitCol &&emit_col) {
+                    EmitCol &&emit_col, EmitPair &&emit_pair) {
     using R = typename Elem<T>::Real;
     using C = typename FftConvPlan<T>::C;
     const AxisGeom &A0 = g.ax[0], &A1 = g.ax[1], &A2 = g.ax[2];
     const int64_t *P = cp.P, *F = cp.F, H = cp.H;
     const int64_t K_is = (int64_t)cp.nK, S_is = (int64_t)cp.nS;
     int s;
+
+    if (cp.rs) {
+        // ---- row-spectral form: kernel rows Kh[K0][K1][H] (tap order) and
+        // padded data rows S[P0][P1][H] in one pass, then per output row the
+        // sum over leading taps, inverse, crop
+        RowArgs<T> kr = cp.rk;
+        kr.mode = ROW_FWD_KERNEL;
+        kr.kcompact = 1;
+        kr.g = g;
+        kr.k = k;
+        kr.ks = ks;
+        kr.inst_base = base;
+        kr.reverse = reverse;
+        kr.n1 = A1.K;
+        kr.n_rows = A0.K * A1.K;
+        kr.spec = Kh;
+        kr.spec_s0 = A1.K * H;
+        kr.spec_s1 = H;
+        kr.spec_is = K_is;
+        kr.scale = 1;
+        RowArgs<T> dr = cp.rk;
+        dr.mode = ROW_FWD_DATA;
+        dr.g = g;
+        dr.x = x;
+        dr.xs = xs;
+        dr.inst_base = base;
+        dr.n1 = P[1];
+        dr.n_rows = P[0] * P[1];
+        dr.spec = S;
+        dr.spec_s0 = P[1] * H;
+        dr.spec_s1 = H;
+        dr.spec_is = S_is;
+        dr.scale = 1;
+        if ((s = emit_pair(kr, dr, cnt))) return s;
+        RowArgs<T> ir = cp.rk;
+        ir.mode = ROW_INV_MAC;
+        ir.g = g;
+        ir.n1 = A1.out;
+        ir.n_rows = A0.out * A1.out;
+        ir.spec = S;
+        ir.spec_is = S_is;
+        ir.kspec = Kh;
+        ir.kspec_is = K_is;
+        ir.mk0 = (int)A0.K;
+        ir.mk1 = (int)A1.K;
+        ir.mbase0 = A0.s * P[1] * H;
+        ir.mbase1 = A1.s * H;
+        ir.mstep0 = A0.d * P[1] * H;
+        ir.mstep1 = A1.d * H;
+        ir.y = y;
+        ir.ys = ys;
+        ir.inst_base = base;
+        ir.y_s0 = A1.out * A2.out;
+        ir.y_s1 = A2.out;
+        ir.out_n = A2.out;
+        ir.crop_off = A2.keff - 1;
+        ir.crop_step = A2.s;
+        ir.scale = (R)(1.0 / (double)F[2]);
+        return emit_row(ir, cnt);
+    }
 
     // ---- kernel spectrum
     RowArgs<T> kr = cp.rk;
@@ -1002,7 +1183,8 @@ int conv_fft_wave(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, cons
     return conv_fft_passes<T>(
         g, reverse, cp, x, k, y, xs, ks, ys, base, cnt, Kh, S,
         [&](RowArgs<T> &A, int n) { return launch_row<T>(A, st, n); },
-        [&](ColArgs<C> &A, int n) { return launch_col<C>(A, st, n); });
+        [&](ColArgs<C> &A, int n) { return launch_col<C>(A, st, n); },
+        [&](RowArgs<T> &A, RowArgs<T> &B, int n) { return launch_row_pair<T>(A, B, st, n); });
 }
 
 // bytes of spectra a wave may keep so that they stay in L2 between passes
@@ -1018,10 +1200,10 @@ size_t wave_budget_bytes() {
 
 template <typename T>
 int conv_fft_run(const Geom3<T> &g, int reverse, const T *x, const T *k, T *y,
-                 ndconv_fft_processor *proc, cudaStream_t st, void *scratch, size_t scratch_bytes) {
+                 ndconv_fft_processor *proc, cudaStream_t st, void *scratch, size_t scratch_bytes, int variant) {
     using C = typename FftConvPlan<T>::C;
     FftConvPlan<T> cp;
-    int s = make_conv_plan(g, cp);
+    int s = make_conv_plan(g, cp, variant);
     if (s) return s;
     const size_t bytes = sizeof(C) * (cp.nK + cp.nS) + 256;
     Workspace ws{proc, st};
@@ -1038,11 +1220,11 @@ int conv_fft_run(const Geom3<T> &g, int reverse, const T *x, const T *k, T *y,
 
 template <typename T>
 int conv_fft_batch_run(const Geom3<T> &g, int reverse, int64_t n, const T *const *xs, const T *const *ks,
-                       T *const *ys, ndconv_fft_processor *proc, cudaStream_t st) {
+                       T *const *ys, ndconv_fft_processor *proc, cudaStream_t st, int variant) {
     using C = typename FftConvPlan<T>::C;
     if (n <= 0) return NDCONV_OK;
     FftConvPlan<T> cp;
-    int s = make_conv_plan(g, cp);
+    int s = make_conv_plan(g, cp, variant);
     if (s) return s;
     const size_t per = sizeof(C) * (cp.nK + cp.nS);
     int64_t W = (int64_t)(wave_budget_bytes() / (per ? per : 1));
@@ -1062,12 +1244,16 @@ int conv_fft_batch_run(const Geom3<T> &g, int reverse, int64_t n, const T *const
     return NDCONV_OK;
 }
 
-template <typename T> size_t conv_fft_scratch_bytes(const Geom3<T> &g) {
+// Spectra bytes of the full N-d form; the row-spectral form needs no more
+// (K0 K1 <= F0 F1 kernel rows, P0 P1 <= P0 F1 data rows).
+template <typename T> size_t conv_fft_scratch_bytes(const Geom3<T> &g, int variant) {
     using R = typename Elem<T>::Real;
     using C = typename CplxT<R>::type;
     const bool real = !Elem<T>::kComplex;
+    const bool pow2 = (variant == FFTV_ND_POW2 || variant == FFTV_RS_POW2);
     int64_t P[3] = {g.ax[0].L, g.ax[1].L, g.ax[2].L}, F[3];
-    for (int a = 0; a < 3; a++) F[a] = (P[a] == 1) ? 1 : smooth_size(P[a], real && a == 2);
+    for (int a = 0; a < 3; a++)
+        F[a] = (P[a] == 1) ? 1 : (pow2 ? pow2_size(P[a], real && a == 2) : smooth_size(P[a], real && a == 2));
     const int64_t H = real ? F[2] / 2 + 1 : F[2];
     const int astar = F[0] > 1 ? 0 : (F[1] > 1 ? 1 : 2);
     const size_t nK = (size_t)F[0] * F[1] * H;
@@ -1077,11 +1263,11 @@ template <typename T> size_t conv_fft_scratch_bytes(const Geom3<T> &g) {
 
 #define NDCONV_INST_FFT(T)                                                                          \
     template int conv_fft_run<T>(const Geom3<T> &, int, const T *, const T *, T *,                \
-                                 ndconv_fft_processor *, cudaStream_t, void *, size_t);          \
+                                 ndconv_fft_processor *, cudaStream_t, void *, size_t, int);     \
     template int conv_fft_batch_run<T>(const Geom3<T> &, int, int64_t, const T *const *,          \
                                        const T *const *, T *const *, ndconv_fft_processor *,      \
-                                       cudaStream_t);                                              \
-    template size_t conv_fft_scratch_bytes<T>(const Geom3<T> &);
+                                       cudaStream_t, int);                                         \
+    template size_t conv_fft_scratch_bytes<T>(const Geom3<T> &, int);
 NDCONV_INST_FFT(float)
 NDCONV_INST_FFT(double)
 NDCONV_INST_FFT(c32)
@@ -1287,6 +1473,7 @@ enum TaskKind : int32_t {
     TK_ROW_FWD_KERNEL = 11,
     TK_ROW_INV_OUT = 12,
     TK_ROW_FUSED = 13,
+    TK_ROW_INV_MAC = 14,
     TK_COL = 20,
 };
 
@@ -1366,6 +1553,7 @@ __global__ void __launch_bounds__(256) persistent_kernel(const Task *__restrict_
         case TK_ROW_FWD_KERNEL: row_block<float, ROW_FWD_KERNEL>(rargs[tk.arg], tk.bx, 0, smem_raw); break;
         case TK_ROW_INV_OUT: row_block<float, ROW_INV_OUT>(rargs[tk.arg], tk.bx, 0, smem_raw); break;
         case TK_ROW_FUSED: row_block<float, ROW_FUSED>(rargs[tk.arg], tk.bx, 0, smem_raw); break;
+        case TK_ROW_INV_MAC: row_block<float, ROW_INV_MAC>(rargs[tk.arg], tk.bx, 0, smem_raw); break;
         case TK_COL: {
             const ColArgs<c32> &A = cargs[tk.arg];
             col_block<c32>(A, tk.bx, tk.by, A.n_outer, 0, smem_raw);
@@ -1382,6 +1570,7 @@ __global__ void __launch_bounds__(256) persistent_kernel(const Task *__restrict_
 // work estimate of one instance (for ordering direct tiles, longest first)
 struct HostInst {
     int algo;        // 0 direct, 1 FFT
+    int fv;          // FFT plan variant (FftVariant)
     int standalone;  // runs as ordinary launches before the persistent kernel
     Plan3 P;
     const void *x, *k;
@@ -1442,9 +1631,9 @@ size_t direct_tasks(ndconv_batch_plan *B, HostInst &h, std::vector<Task> &out) {
     const AxisGeom &A0 = D.g.ax[0], &A1 = D.g.ax[1], &A2 = D.g.ax[2];
     int kind = 0;
     int64_t gx = 0, gy = 0;
-    if (A2.s == 1 && A2.d <= 8 && plan_sw(D, 8) && smem_bytes(D) <= kBatchSmem) {
+    if (plan_sw(D, 8) && smem_bytes(D) <= kBatchSmem) {
         kind = TK_DIRECT_SW;
-        const int64_t TXo = (int64_t)D.sw_nseg * A2.d * 32 * 8;
+        const int64_t TXo = sw_cols_per_cta(D, 8);
         gx = (A2.out + TXo - 1) / TXo;
         gy = (A1.out + D.sw_ty - 1) / D.sw_ty;
     } else {
@@ -1496,8 +1685,12 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
     size_t ws = 0;
     for (int64_t i = 0; i < n; i++) {
         HostInst &h = B->inst[(size_t)i];
-        h.algo = algo ? algo[i] : 1;
-        if (h.algo != 0 && h.algo != 1) return fail(ndconv_fail(NDCONV_ERR_INVALID, "algo must be 0 (direct) or 1 (FFT)"));
+        const int32_t a = algo ? algo[i] : NDCONV_ALGO_FFT;
+        if (a < 0 || a >= NDCONV_ALGO_COUNT || a == NDCONV_ALGO_DIRECT_BF16X3)
+            return fail(ndconv_fail(NDCONV_ERR_INVALID, "algo must be 0 (direct), 1 (FFT) or 3..6 (FFT variants)"));
+        h.algo = (a == NDCONV_ALGO_DIRECT) ? 0 : 1;
+        h.fv = (a == NDCONV_ALGO_FFT_ND) ? FFTV_ND : (a == NDCONV_ALGO_FFT_RS) ? FFTV_RS
+             : (a == NDCONV_ALGO_FFT_ND_POW2) ? FFTV_ND_POW2 : (a == NDCONV_ALGO_FFT_RS_POW2) ? FFTV_RS_POW2 : FFTV_AUTO;
         int s = plan_problem(&probs[i], h.algo, &h.P);
         if (s) {
             std::string m = "instance " + std::to_string(i) + ": " + ndconv_last_error();
@@ -1511,7 +1704,7 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
         h.standalone = (h.P.dtype != NDCONV_F32);
         h.ws_off = 0;
         if (h.algo == 1 && !h.standalone) {
-            if ((s = make_conv_plan<float>(h.P.geom<float>(), h.cp))) return fail(s);
+            if ((s = make_conv_plan<float>(h.P.geom<float>(), h.cp, h.fv))) return fail(s);
             h.ws_off = ws;
             ws += (sizeof(c32) * (h.cp.nK + h.cp.nS) + 255) / 256 * 256;
         }
@@ -1527,20 +1720,20 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
             switch (h.P.dtype) {
             case NDCONV_F64: {
                 FftConvPlan<double> cp;
-                s = make_conv_plan<double>(h.P.geom<double>(), cp);
-                b = conv_fft_scratch_bytes<double>(h.P.geom<double>());
+                s = make_conv_plan<double>(h.P.geom<double>(), cp, h.fv);
+                b = conv_fft_scratch_bytes<double>(h.P.geom<double>(), h.fv);
                 break;
             }
             case NDCONV_C32: {
                 FftConvPlan<c32> cp;
-                s = make_conv_plan<c32>(h.P.geom<c32>(), cp);
-                b = conv_fft_scratch_bytes<c32>(h.P.geom<c32>());
+                s = make_conv_plan<c32>(h.P.geom<c32>(), cp, h.fv);
+                b = conv_fft_scratch_bytes<c32>(h.P.geom<c32>(), h.fv);
                 break;
             }
             default: {
                 FftConvPlan<c64> cp;
-                s = make_conv_plan<c64>(h.P.geom<c64>(), cp);
-                b = conv_fft_scratch_bytes<c64>(h.P.geom<c64>());
+                s = make_conv_plan<c64>(h.P.geom<c64>(), cp, h.fv);
+                b = conv_fft_scratch_bytes<c64>(h.P.geom<c64>(), h.fv);
                 break;
             }
             }
@@ -1567,7 +1760,7 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
         c32 *Kh = reinterpret_cast<c32 *>(static_cast<unsigned char *>(B->ws) + h.ws_off);
         c32 *S = Kh + h.cp.nK;
         std::vector<Level> &lv = per_inst[(size_t)i];
-        bool too_big = false;
+        bool too_big = false, same_level = false;
         size_t inst_smem = 0;
         auto new_level = [&]() -> Level & {
             lv.push_back(Level{i, B->nctrs++, {}});
@@ -1583,17 +1776,28 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
             if (sm > kBatchSmem) too_big = true;
             inst_smem = std::max(inst_smem, sm);
             const int arg = (int)B->rargs.size();
+            A.l2only = 1;  // producers run in the same launch: no L1-cached reads
             B->rargs.push_back(A);
             int kind = TK_ROW_FWD_DATA;
             switch (A.mode) {
             case ROW_FWD_DATA: kind = TK_ROW_FWD_DATA; break;
             case ROW_FWD_KERNEL: kind = TK_ROW_FWD_KERNEL; break;
             case ROW_INV_OUT: kind = TK_ROW_INV_OUT; break;
+            case ROW_INV_MAC: kind = TK_ROW_INV_MAC; break;
             default: kind = TK_ROW_FUSED; break;
             }
-            Level &L = new_level();
+            Level &L = same_level ? lv.back() : new_level();
             for (int64_t b = 0; b < grid; b++) L.tasks.push_back(Task{kind, arg, (int32_t)b, 0, 0, L.ctr, -1, 0});
             return NDCONV_OK;
+        };
+        // independent passes share one level (one counter)
+        auto emit_pair = [&](RowArgs<float> &A, RowArgs<float> &B2, int cnt) -> int {
+            int s2 = emit_row(A, cnt);
+            if (s2) return s2;
+            same_level = !lv.empty();
+            s2 = emit_row(B2, cnt);
+            same_level = false;
+            return s2;
         };
         auto emit_col = [&](ColArgs<c32> &A, int cnt) -> int {
             (void)cnt;
@@ -1615,7 +1819,7 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
         const Geom3<float> g = h.P.geom<float>();
         int s = conv_fft_passes<float>(g, h.P.reverse, h.cp, static_cast<const float *>(h.x),
                                        static_cast<const float *>(h.k), static_cast<float *>(h.y), nullptr,
-                                       nullptr, nullptr, 0, 1, Kh, S, emit_row, emit_col);
+                                       nullptr, nullptr, 0, 1, Kh, S, emit_row, emit_col, emit_pair);
         if (s) return fail(s);
         if (too_big) {
             // does not fit the persistent kernel's shared memory: ordinary launches
@@ -1701,12 +1905,12 @@ int run_standalone(ndconv_batch_plan *B, cudaStream_t st) {
         switch (h.P.dtype) {
         case NDCONV_F32: {
             const size_t b = sizeof(c32) * (h.cp.nK + h.cp.nS) + 256;
-            s = conv_fft_run<float>(h.P.geom<float>(), h.P.reverse, (const float *)h.x, (const float *)h.k, (float *)h.y, nullptr, st, scr, b);
+            s = conv_fft_run<float>(h.P.geom<float>(), h.P.reverse, (const float *)h.x, (const float *)h.k, (float *)h.y, nullptr, st, scr, b, h.fv);
             break;
         }
-        case NDCONV_F64: s = conv_fft_run<double>(h.P.geom<double>(), h.P.reverse, (const double *)h.x, (const double *)h.k, (double *)h.y, nullptr, st, scr, conv_fft_scratch_bytes<double>(h.P.geom<double>())); break;
-        case NDCONV_C32: s = conv_fft_run<c32>(h.P.geom<c32>(), h.P.reverse, (const c32 *)h.x, (const c32 *)h.k, (c32 *)h.y, nullptr, st, scr, conv_fft_scratch_bytes<c32>(h.P.geom<c32>())); break;
-        default: s = conv_fft_run<c64>(h.P.geom<c64>(), h.P.reverse, (const c64 *)h.x, (const c64 *)h.k, (c64 *)h.y, nullptr, st, scr, conv_fft_scratch_bytes<c64>(h.P.geom<c64>())); break;
+        case NDCONV_F64: s = conv_fft_run<double>(h.P.geom<double>(), h.P.reverse, (const double *)h.x, (const double *)h.k, (double *)h.y, nullptr, st, scr, conv_fft_scratch_bytes<double>(h.P.geom<double>(), h.fv), h.fv); break;
+        case NDCONV_C32: s = conv_fft_run<c32>(h.P.geom<c32>(), h.P.reverse, (const c32 *)h.x, (const c32 *)h.k, (c32 *)h.y, nullptr, st, scr, conv_fft_scratch_bytes<c32>(h.P.geom<c32>(), h.fv), h.fv); break;
+        default: s = conv_fft_run<c64>(h.P.geom<c64>(), h.P.reverse, (const c64 *)h.x, (const c64 *)h.k, (c64 *)h.y, nullptr, st, scr, conv_fft_scratch_bytes<c64>(h.P.geom<c64>(), h.fv), h.fv); break;
         }
         if (s) return s;
     }
@@ -1802,10 +2006,10 @@ extern "C" int ndconv_batch_run_plain(ndconv_batch_plan *B, void *stream) {
         }
         int s;
         switch (h.P.dtype) {
-        case NDCONV_F32: s = ndconv::conv_fft_run<float>(h.P.geom<float>(), h.P.reverse, (const float *)h.x, (const float *)h.k, (float *)h.y, nullptr, st, scr, ndconv::conv_fft_scratch_bytes<float>(h.P.geom<float>())); break;
-        case NDCONV_F64: s = ndconv::conv_fft_run<double>(h.P.geom<double>(), h.P.reverse, (const double *)h.x, (const double *)h.k, (double *)h.y, nullptr, st, scr, ndconv::conv_fft_scratch_bytes<double>(h.P.geom<double>())); break;
-        case NDCONV_C32: s = ndconv::conv_fft_run<c32>(h.P.geom<c32>(), h.P.reverse, (const c32 *)h.x, (const c32 *)h.k, (c32 *)h.y, nullptr, st, scr, ndconv::conv_fft_scratch_bytes<c32>(h.P.geom<c32>())); break;
-        default: s = ndconv::conv_fft_run<c64>(h.P.geom<c64>(), h.P.reverse, (const c64 *)h.x, (const c64 *)h.k, (c64 *)h.y, nullptr, st, scr, ndconv::conv_fft_scratch_bytes<c64>(h.P.geom<c64>())); break;
+        case NDCONV_F32: s = ndconv::conv_fft_run<float>(h.P.geom<float>(), h.P.reverse, (const float *)h.x, (const float *)h.k, (float *)h.y, nullptr, st, scr, sizeof(c32) * (h.cp.nK + h.cp.nS) + 256, h.fv); break;
+        case NDCONV_F64: s = ndconv::conv_fft_run<double>(h.P.geom<double>(), h.P.reverse, (const double *)h.x, (const double *)h.k, (double *)h.y, nullptr, st, scr, ndconv::conv_fft_scratch_bytes<double>(h.P.geom<double>(), h.fv), h.fv); break;
+        case NDCONV_C32: s = ndconv::conv_fft_run<c32>(h.P.geom<c32>(), h.P.reverse, (const c32 *)h.x, (const c32 *)h.k, (c32 *)h.y, nullptr, st, scr, ndconv::conv_fft_scratch_bytes<c32>(h.P.geom<c32>(), h.fv), h.fv); break;
+        default: s = ndconv::conv_fft_run<c64>(h.P.geom<c64>(), h.P.reverse, (const c64 *)h.x, (const c64 *)h.k, (c64 *)h.y, nullptr, st, scr, ndconv::conv_fft_scratch_bytes<c64>(h.P.geom<c64>(), h.fv), h.fv); break;
         }
         if (s) return s;
     }
@@ -1867,16 +2071,25 @@ extern "C" int ndconv_plan_info(const ndconv_problem *p, double out[8]) {
     const double nout = (double)(A[0].out * A[1].out * A[2].out);
     const double nx = (double)(A[0].n * A[1].n * A[2].n);
     double taps = (double)(A[0].K * A[1].K * A[2].K);
+    double sw_slots = -1;  // issue slots of the sliding-window kernel, if it applies
     {
         // the direct kernels only loop over taps that can see data
         DirectParams<float> D = P.direct<float>();
         restrict_live_taps(D);
         taps = (double)(D.t_n[0] * D.t_n[1] * D.t_n[2]);
+        permute_axes_for_tiles(D);
+        if (plan_sw(D, 8)) sw_slots = sw_cost(D, 8, 16);
     }
     const int es = (P.dtype == NDCONV_F64 || P.dtype == NDCONV_C32) ? 8 : (P.dtype == NDCONV_C64 ? 16 : 4);
     const double bytes = es * (nx + taps + nout);
     const double macs = nout * taps * ((P.dtype == NDCONV_C32 || P.dtype == NDCONV_C64) ? 4 : 1);
-    out[0] = macs / 40e12 + bytes / 6.8e12 + 4e-6;  // direct, seconds
+    // direct, seconds: FMA rate, or the sliding-window issue model (152 SMs x
+    // 4 schedulers x ~1.9 GHz) when that kernel applies; other tilings run
+    // at about a third of the FMA rate
+    const double issue = 152.0 * 4 * 1.9e9;
+    const double t_fma = (sw_slots >= 0) ? (sw_slots / issue > macs / 40e12 ? sw_slots / issue : macs / 40e12)
+                                         : 3.0 * macs / 40e12;
+    out[0] = t_fma + bytes / 6.8e12 + 4e-6;
     out[2] = macs;
     out[3] = bytes;
     // FFT: sizes, shared-memory fit, smem-traffic model

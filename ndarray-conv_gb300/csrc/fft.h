@@ -5,18 +5,25 @@
 
 namespace ndconv {
 
+// FFT plan variants (autotuner candidates): the form (full N-d transform,
+// or row-spectral: FFT along the contiguous axis with the leading-axis taps
+// summed in the spectral domain) and the transform lengths (7-smooth, or
+// powers of two: radix-8/4/2 stages only).
+enum FftVariant : int { FFTV_AUTO = 0, FFTV_ND = 1, FFTV_RS = 2, FFTV_ND_POW2 = 3, FFTV_RS_POW2 = 4 };
+
 // conv_fft on the canonical geometry.  scratch (optional) must hold
 // conv_fft_scratch_bytes(g) bytes; otherwise the processor's workspace or
 // a stream-ordered allocation is used.
 template <typename T>
 int conv_fft_run(const Geom3<T> &g, int reverse, const T *x, const T *k, T *y,
-                 ndconv_fft_processor *proc, cudaStream_t st, void *scratch, size_t scratch_bytes);
-template <typename T> size_t conv_fft_scratch_bytes(const Geom3<T> &g);
+                 ndconv_fft_processor *proc, cudaStream_t st, void *scratch, size_t scratch_bytes,
+                 int variant = FFTV_AUTO);
+template <typename T> size_t conv_fft_scratch_bytes(const Geom3<T> &g, int variant = FFTV_AUTO);
 // n instances sharing the geometry; xs / ks / ys are device arrays of n
 // device pointers.  Runs in waves whose spectra fit a share of L2.
 template <typename T>
 int conv_fft_batch_run(const Geom3<T> &g, int reverse, int64_t n, const T *const *xs, const T *const *ks,
-                       T *const *ys, ndconv_fft_processor *proc, cudaStream_t st);
+                       T *const *ys, ndconv_fft_processor *proc, cudaStream_t st, int variant = FFTV_AUTO);
 
 template <typename T>
 int proc_forward(ndconv_fft_processor *proc, int rank, const int64_t *shape, const T *in,
@@ -46,6 +53,7 @@ struct TwArenaScope {
     TwArena *prev;
 };
 int64_t smooth_size(int64_t n, bool even);
+int64_t pow2_size(int64_t n, bool even);
 
 }  // namespace ndconv
 

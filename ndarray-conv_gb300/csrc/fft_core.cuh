@@ -59,6 +59,19 @@ template <typename C> __host__ __device__ __forceinline__ int64_t padded_slots(i
 
 // Load a complex value past L1 (other CTAs of the same launch may have
 // written it).
+__device__ __forceinline__ float fmaf_t(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fmaf_t(double a, double b, double c) { return fma(a, b, c); }
+
+// read-only (L1-cached) load of data written by an earlier launch
+template <typename C> __device__ __forceinline__ C ldg_c(const C *p) {
+    if constexpr (sizeof(C) == 8) {
+        const float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+        return C{v.x, v.y};
+    } else {
+        const double2 v = __ldg(reinterpret_cast<const double2 *>(p));
+        return C{v.x, v.y};
+    }
+}
 template <typename C> __device__ __forceinline__ C ldcg_c(const C *p) {
     if constexpr (sizeof(C) == 8) {
         const float2 v = __ldcg(reinterpret_cast<const float2 *>(p));

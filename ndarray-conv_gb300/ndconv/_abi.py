@@ -12,6 +12,12 @@ LIB_PATH = os.path.join(os.path.dirname(_HERE), "_build", "libndconv.so")
 # ndconv_dtype
 F32, F64, I32, C32, C64 = 0, 1, 2, 3, 4
 # ndconv_status
+# ndconv_algo: algorithm variants (autotuner candidates)
+ALGO_DIRECT, ALGO_FFT, ALGO_DIRECT_BF16X3 = 0, 1, 2
+ALGO_FFT_ND, ALGO_FFT_RS, ALGO_FFT_ND_POW2, ALGO_FFT_RS_POW2 = 3, 4, 5, 6
+ALGO_NAMES = {0: "direct", 1: "fft", 2: "direct_bf16x3", 3: "fft_nd", 4: "fft_rs", 5: "fft_nd_pow2",
+              6: "fft_rs_pow2"}
+
 OK = 0
 ERR_DATA_SHAPE = 1
 ERR_KERNEL_SHAPE = 2
@@ -79,6 +85,7 @@ def lib():
         "ndconv_conv": (ctypes.c_int, [pp, vp, vp, vp, vp]),
         "ndconv_conv_fft": (ctypes.c_int, [pp, vp, vp, vp, vp, vp]),
         "ndconv_conv_fft_noalloc": (ctypes.c_int, [pp, vp, vp, vp, vp]),
+        "ndconv_conv_algo": (ctypes.c_int, [pp, i32, vp, vp, vp, vp]),
         "ndconv_conv_batch": (ctypes.c_int, [pp, ctypes.c_int64, vp, vp, vp, vp]),
         "ndconv_conv_fft_batch": (ctypes.c_int, [pp, ctypes.c_int64, vp, vp, vp, vp, vp]),
         "ndconv_fft_processor_create": (ctypes.c_int, [i32, ctypes.POINTER(vp)]),

@@ -2,7 +2,8 @@
 
 BatchPlan binds n problems (any shapes, kernels, modes; f32 ones run inside
 one persistent kernel with a device work queue, replayed as a CUDA graph)
-to their device buffers.  `algos[i]` picks direct (0) or FFT (1) per
+to their device buffers.  `algos[i]` picks the variant (ndconv_algo: direct 0,
+FFT 1, FFT plan variants 3..6) per
 instance; `ndconv.dispatch` chooses them by cost model, timing DB or MLP.
 """
 import ctypes
@@ -36,7 +37,8 @@ class BatchPlan:
             p = build_problem(dtype_code(self.datas[i].dtype), tuple(self.datas[i].shape), kw, cm, pm)
             probs[i] = p
             algo = 1 if algos is None else int(algos[i])
-            st = L.ndconv_output_shape(ctypes.byref(p), algo, shape)
+            # output_shape knows the two argument-check orders: direct (0) and FFT (1)
+            st = L.ndconv_output_shape(ctypes.byref(p), 0 if algo in (0, 2) else 1, shape)
             if st:
                 raise RuntimeError(f"instance {i}: {_abi.last_error()}")
             if outs is None:

@@ -46,14 +46,17 @@ def _prepare(data, kernel, conv_mode, padding_mode):
     return p, x, k, x_host
 
 
-def _run(algo, data, kernel, conv_mode, padding_mode, processor=None, stream=None):
+def _run(algo, data, kernel, conv_mode, padding_mode, processor=None, stream=None, variant=None):
     L = _abi.lib()
     p, x, k, x_host = _prepare(data, kernel, conv_mode, padding_mode)
     shape = (ctypes.c_int64 * 3)()
     raise_for_status(L.ndconv_output_shape(ctypes.byref(p), algo, shape), p, algo)
     y = torch.empty([shape[i] for i in range(p.rank)], dtype=x.dtype, device=x.device)
     sp = _stream_ptr(stream)
-    if algo == 0:
+    if variant is not None:
+        st = L.ndconv_conv_algo(ctypes.byref(p), variant, ctypes.c_void_p(x.data_ptr()),
+                                ctypes.c_void_p(k.data_ptr()), ctypes.c_void_p(y.data_ptr()), sp)
+    elif algo == 0:
         st = L.ndconv_conv(ctypes.byref(p), ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(k.data_ptr()),
                            ctypes.c_void_p(y.data_ptr()), sp)
     else:
@@ -84,6 +87,13 @@ def conv_fft_with_processor(data, kernel, conv_mode, padding_mode, processor, st
 def conv_fft_par(data, kernel, conv_mode, padding_mode, stream=None):
     """ConvFFTExt::conv_fft_par: on the GPU the same kernels as conv_fft."""
     return _run(1, data, kernel, conv_mode, padding_mode, stream=stream)
+
+
+def conv_algo(data, kernel, conv_mode, padding_mode, algo, stream=None):
+    """One convolution by an explicit algorithm variant (ndconv_algo code,
+    e.g. _abi.ALGO_FFT_RS); the autotuner times these."""
+    base = 0 if algo in (_abi.ALGO_DIRECT, _abi.ALGO_DIRECT_BF16X3) else 1
+    return _run(base, data, kernel, conv_mode, padding_mode, stream=stream, variant=int(algo))
 
 
 class FftProcessor:
