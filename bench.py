@@ -1,6 +1,6 @@
 """Benchmark: convolution GB/s and % of HBM roofline on one GB300.
 
-Workload (config 2 of the reference's benchmark set, batched): B
+Workload (the reference's 2-D benchmark case, batched): B
 independent instances of a 2-D f32 convolution x[200, 5000] with a kernel
 [11, 31] dilated by 2, ConvMode::Same, PaddingMode::Custom([Reflect,
 Circular]); every instance has its own seeded Uniform[0,1) data and kernel.
@@ -29,6 +29,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path[:0] = [ROOT, os.path.join(ROOT, "ndarray-conv_gb300")]
 
 import numpy as np  # noqa: E402
+
+# DRAM bytes per instance of the batched FFT path from one ncu capture (waves
+# of 10 instances, caches flushed between the two launches): an upper bound
+PROFILED_TRAFFIC = {"fft": 9.43e6}
 
 SHAPE_X = (200, 5000)
 SHAPE_K = (11, 31)
@@ -161,7 +165,7 @@ def run_reference(args, rank, world):
             "ms_per_step": el / steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Uniform[0,1))",
             "impl": "reference",
-            "config": {"workload": "config2: 2-D f32 x[200,5000] * k[11,31] dilation 2, Same, "
+            "config": {"workload": "2-D f32 x[200,5000] * k[11,31] dilation 2, Same, "
                                    "Custom([Reflect, Circular]); conv_fft"},
             "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": nth, "kind": "port", "sample": sample},
             "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -182,7 +186,7 @@ def flat_views(shapes, dtype, device):
 
 
 def bench_uneven(args, world, rank, local_rank):
-    """Config 4: an uneven batch of independent instances in one persistent
+    """The uneven batch: independent instances in one persistent
     launch (device work queue, CUDA graph), against the same instances
     through the per-instance entry points (the plain drop-in)."""
     import torch
@@ -195,17 +199,27 @@ def bench_uneven(args, world, rank, local_rank):
         dist.init_process_group("nccl")
     from ndconv import _abi, with_dilation
     from ndconv import workloads as W
+    from ndconv import shard
     from ndconv.batch import BatchPlan
     from ndconv.dispatch import ModelDispatcher
     L = _abi.lib()
-    specs = W.uneven_batch(args.n_instances, seed=4000 + rank)
+    # one batch of n instances per rank, split across ranks by estimated cost
+    # (no data exchange between ranks)
+    specs_all = W.uneven_batch(args.n_instances * world, seed=4000)
+    specs = [specs_all[i] for i in shard.local_share(specs_all, rank, world)]
     gen = torch.Generator(device="cuda").manual_seed(4000 + rank)
     xbuf, xs = flat_views([s.shape for s in specs], torch.float32, "cuda")
     kbuf, ks = flat_views([s.kshape for s in specs], torch.float32, "cuda")
     ybuf, ys = flat_views([tuple(s.out_shape()) for s in specs], torch.float32, "cuda")
     xbuf.uniform_(-1, 1, generator=gen)
     kbuf.uniform_(-1, 1, generator=gen)
-    algos = ModelDispatcher().choose(specs)
+    if args.dispatch == "mlp":
+        from ndconv.mlp import MLPDispatcher, default_available
+        avail = default_available()
+        avail[1] = 0.0  # the tensor-core variant is not a persistent-queue task
+        algos = MLPDispatcher(available=avail).choose(specs)
+    else:
+        algos = ModelDispatcher().choose(specs)
     plan = BatchPlan([(s.conv_mode(), s.padding_mode()) for s in specs], xs,
                      [with_dilation(k, s.dilation) for k, s in zip(ks, specs)], outs=ys, algos=algos)
     info = plan.info()
@@ -272,7 +286,7 @@ def bench_uneven(args, world, rank, local_rank):
     from ndconv import build_problem
     errs = []
     for want in (0, 1):
-        cand = [i for i, s in enumerate(specs) if algos[i] == want]
+        cand = [i for i, s in enumerate(specs) if (algos[i] != 0) == bool(want)]
         cand.sort(key=lambda i: specs[i].out_shape()[0] * 0 + int(np.prod(specs[i].out_shape())) *
                   int(np.prod(specs[i].kshape)))
         for i in cand[len(cand) // 2: len(cand) // 2 + 2]:
@@ -291,13 +305,14 @@ def bench_uneven(args, world, rank, local_rank):
             "metric": "conv GB/s (algorithmic bytes 4*(|x|+|k|+|y|)), uneven batch",
             "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic (seeded; config-4 distribution)",
-            "config": {"workload": f"config4: {len(specs)} uneven instances (rank 1/2/3 = 60/35/5%, "
+            "dtype": "f32", "data": "synthetic (seeded; uneven-batch distribution)",
+            "config": {"workload": f"uneven batch: {len(specs)} instances (rank 1/2/3 = 60/35/5%, "
                                    "2^8..2^20 elements, odd kernels 3..127, dilation/stride 1|2, "
                                    "Zeros/Reflect/Replicate/Circular), one persistent launch + CUDA graph",
                        "instances_per_gpu": len(specs), "algos": {"direct": int(sum(a == 0 for a in algos)),
-                                                                  "fft": int(sum(a == 1 for a in algos))},
-                       "dispatcher": "cost model", "plan": info,
+                                                                  "fft": int(sum(a != 0 for a in algos))},
+                       "dispatcher": {"mlp": "trained network (ndconv/data/dispatcher_mlp.json)",
+                                      "model": "cost model"}[args.dispatch], "plan": info,
                        "plain_per_instance_gbs": bytes_step * world / (plain_ms * 1e-3) / 1e9,
                        "batched_over_plain": plain_ms / ms,
                        "l2": f"inputs {xbuf.numel() * 4 / 1e9:.2f} GB per GPU, larger than L2, no flush"},
@@ -361,6 +376,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--config", default="c2", choices=["c2", "c4"])
     ap.add_argument("--n-instances", type=int, default=4096)
+    ap.add_argument("--dispatch", default="mlp", choices=["mlp", "model"])
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -531,14 +547,18 @@ def main():
             "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded Uniform[0,1), distinct data and kernel per instance)",
-            "config": {"workload": f"config2 x{B}: 2-D f32 x[200,5000] * k[11,31] dilation 2, Same, "
+            "config": {"workload": f"{B} x 2-D f32 x[200,5000] * k[11,31] dilation 2, Same, "
                                    f"Custom([Reflect, Circular]); {'conv_fft' if algo else 'conv'}, "
                                    f"{args.form} submission",
                        "batch_per_gpu": B, "algo": args.algo, "form": args.form,
                        "plain_per_instance_gbs": (bytes_step * world / (plain_ms * 1e-3) / 1e9) if plain_ms else None,
                        "l2": "inputs (256 MB per GPU) larger than L2, no flush"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak,
+                         "traffic": PROFILED_TRAFFIC.get(args.algo) if args.form == "batched" else None,
+                         "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per instance, "
+                                            "profiles/conv_fft_rowspectral_kernels_full.md")
+                         if args.algo == "fft" and args.form == "batched" else None,
                          "kernel": "one instance's convolution (all its launches)",
                          "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"},
             "cpu_baseline": cpu,

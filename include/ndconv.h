@@ -143,6 +143,14 @@ typedef enum {
 int ndconv_conv_algo(const ndconv_problem *p, int32_t algo, const void *data, const void *kernel, void *out,
                      void *stream);
 
+/* ConvExt::conv for f32 on the tensor cores: 3xBF16 split products
+ * (x k ~ xh kh + xh kl + xl kh) accumulated in f32, normwise error ~1e-6 vs
+ * f64.  Unit stride along the middle canonical axis only (else
+ * NDCONV_ERR_UNSUPPORTED); non-finite inputs fall back to the FP32 loop so
+ * NaN / Inf propagate as in the reference.  Same as
+ * ndconv_conv_algo(p, NDCONV_ALGO_DIRECT_BF16X3, ...); synchronises stream. */
+int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, const void *kernel, void *out, void *stream);
+
 /* Batched ConvExt::conv / ConvFFTExt::conv_fft over n instances that share
  * one problem geometry (shapes, dilation, modes); each instance has its
  * own data, kernel and output.  data / kernel / out are DEVICE arrays of n

@@ -289,8 +289,7 @@ extern "C" int ndconv_conv_algo(const ndconv_problem *p, int32_t algo, const voi
                                 void *out, void *stream) {
     if (algo == NDCONV_ALGO_DIRECT) return ndconv_conv(p, data, kernel, out, stream);
     if (algo == NDCONV_ALGO_FFT) return ndconv_conv_fft(p, data, kernel, out, nullptr, stream);
-    if (algo == NDCONV_ALGO_DIRECT_BF16X3)
-        return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "3xBF16 direct path not available in this build");
+    if (algo == NDCONV_ALGO_DIRECT_BF16X3) return ndconv_conv_bf16x3(p, data, kernel, out, stream);
     if (algo < 0 || algo >= NDCONV_ALGO_COUNT) return ndconv_fail(NDCONV_ERR_INVALID, "unknown algorithm variant");
     Plan3 P;
     int s = plan_problem(p, 1, &P);

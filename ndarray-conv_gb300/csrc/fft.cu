@@ -459,37 +459,57 @@ __device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsi
         C *dst = (A.kind == RK_REAL_EVEN) ? buf1 : buf0;
         if constexpr (MODE == ROW_INV_MAC) {
             // output row spectrum = sum over leading taps (tz, ty) of kernel row
-            // (tz, ty) times data row (o0 s0 + tz d0, o1 s1 + ty d1)
+            // (tz, ty) times data row (o0 s0 + tz d0, o1 s1 + ty d1); four bins
+            // per thread at a time so that eight loads are in flight per tap
             const int mk0 = A.mk0, mk1 = A.mk1;
             const int64_t st0 = A.mstep0, st1 = A.mstep1, Hh = A.H;
-            for (int u = threadIdx.x; u < tot; u += blockDim.x) {
-                const int b = u & (nb - 1), k = u >> lognb;
-                const RowInfo &ri = rinfo[b];
-                C acc{0, 0};
-                if (ri.valid) {
-                    const C *kq = kspec + k;
-                    const C *sp0 = spec + ri.soff + k;
-                    if (A.l2only) {
-                        for (int tz = 0; tz < mk0; tz++, sp0 += st0) {
-                            const C *sp = sp0;
-                            for (int ty = 0; ty < mk1; ty++, sp += st1, kq += Hh) {
-                                const C kv = ldcg_c(kq), dv = ldcg_c(sp);
-                                acc.re = fmaf_t(kv.re, dv.re, fmaf_t(-kv.im, dv.im, acc.re));
-                                acc.im = fmaf_t(kv.re, dv.im, fmaf_t(kv.im, dv.re, acc.im));
+            const bool l2 = A.l2only;
+            const int T_ = blockDim.x;
+            for (int u0 = threadIdx.x; u0 < tot; u0 += 4 * T_) {
+                C acc[4];
+                int64_t soff[4], koff[4];
+                bool ok[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int u = u0 + q * T_;
+                    const int b = u & (nb - 1), k = u >> lognb;
+                    ok[q] = u < tot && rinfo[b].valid;
+                    soff[q] = ok[q] ? rinfo[b].soff + k : 0;
+                    koff[q] = ok[q] ? k : 0;
+                    acc[q] = C{0, 0};
+                }
+                const C *kq[4], *sq[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    kq[q] = kspec + koff[q];
+                    sq[q] = spec + soff[q];
+                }
+                auto taps = [&](auto load) {
+                    for (int tz = 0; tz < mk0; tz++) {
+                        for (int ty = 0; ty < mk1; ty++) {
+                            const int64_t so = tz * st0 + ty * st1, ko = (int64_t)(tz * mk1 + ty) * Hh;
+                            C kv[4], dv[4];
+#pragma unroll
+                            for (int q = 0; q < 4; q++) {
+                                kv[q] = load(kq[q] + ko);
+                                dv[q] = load(sq[q] + so);
                             }
-                        }
-                    } else {
-                        for (int tz = 0; tz < mk0; tz++, sp0 += st0) {
-                            const C *sp = sp0;
-                            for (int ty = 0; ty < mk1; ty++, sp += st1, kq += Hh) {
-                                const C kv = ldg_c(kq), dv = ldg_c(sp);
-                                acc.re = fmaf_t(kv.re, dv.re, fmaf_t(-kv.im, dv.im, acc.re));
-                                acc.im = fmaf_t(kv.re, dv.im, fmaf_t(kv.im, dv.re, acc.im));
+#pragma unroll
+                            for (int q = 0; q < 4; q++) {
+                                acc[q].re = fmaf_t(kv[q].re, dv[q].re, fmaf_t(-kv[q].im, dv[q].im, acc[q].re));
+                                acc[q].im = fmaf_t(kv[q].re, dv[q].im, fmaf_t(kv[q].im, dv[q].re, acc[q].im));
                             }
                         }
                     }
+                };
+                // the load kind is uniform: one loop nest per kind, no per-load select
+                if (l2) taps([](const C *p) { return ldcg_c(p); });
+                else taps([](const C *p) { return ldg_c(p); });
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int u = u0 + q * T_;
+                    if (u < tot) dst[sx<C>(u)] = ok[q] ? acc[q] : C{0, 0};
                 }
-                dst[sx<C>(u)] = acc;
             }
         } else {
             for (int u = threadIdx.x; u < tot; u += blockDim.x) {

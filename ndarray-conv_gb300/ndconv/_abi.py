@@ -79,6 +79,7 @@ def lib():
             "`python -c 'import __graft_entry__ as g; g.build()'`")
     L = ctypes.CDLL(LIB_PATH)
     vp, i32, i64p = ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)
+    fp = ctypes.POINTER(ctypes.c_float)
     pp = ctypes.POINTER(Problem)
     sig = {
         "ndconv_output_shape": (ctypes.c_int, [pp, i32, i64p]),
@@ -102,6 +103,14 @@ def lib():
         "ndconv_batch_info": (ctypes.c_int, [vp, i64p]),
         "ndconv_batch_destroy": (ctypes.c_int, [vp]),
         "ndconv_plan_info": (ctypes.c_int, [pp, ctypes.POINTER(ctypes.c_double)]),
+        "ndconv_mlp_create": (ctypes.c_int, [i32, i32, i32, ctypes.c_uint64, ctypes.POINTER(vp)]),
+        "ndconv_mlp_destroy": (ctypes.c_int, [vp]),
+        "ndconv_mlp_param_count": (ctypes.c_int64, [vp]),
+        "ndconv_mlp_params": (ctypes.c_int, [vp, fp, ctypes.c_int64, i32]),
+        "ndconv_mlp_forward": (ctypes.c_int, [vp, fp, ctypes.c_int64, fp, vp]),
+        "ndconv_mlp_gradient": (ctypes.c_int, [vp, fp, fp, fp, ctypes.c_int64, fp, fp, vp]),
+        "ndconv_mlp_train": (ctypes.c_int, [vp, fp, fp, fp, ctypes.c_int64, i32, i32, ctypes.c_float,
+                                            ctypes.c_uint64, fp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -1,0 +1,229 @@
+"""Autotuner: times every algorithm variant of an instance on the GPU (CUDA
+events, warm-up first, best of `reps`), keeps the timings in a database,
+and trains / judges the learned dispatcher against them.
+
+The exhaustive autotuner is the ground truth: the dispatcher's regret on a
+held-out set is t(pick) / t(best) - 1 per instance, and the total-time ratio
+sum t(pick) / sum t(best) over the set.
+
+    python -m ndconv.autotune --train 20000 --holdout 2000 --out DIR
+
+times the configurations (dispatcher distribution: the uneven-batch
+distribution, with its 2-D instances extended up to 4096 x 4096 and
+kernels up to 63 x 63), trains the network with the library's CUDA
+kernels, and writes DIR/timings.npz, DIR/dispatcher_mlp.json and
+DIR/dispatcher_report.json.
+"""
+import argparse
+import ctypes
+import json
+import math
+import os
+import time
+
+import numpy as np
+
+from . import _abi
+from .api import build_problem, with_dilation
+from .workloads import PAD_MODES, Spec
+
+# the candidates (network outputs) and the cost model's FFT choice
+MEASURED = [_abi.ALGO_DIRECT, _abi.ALGO_DIRECT_BF16X3, _abi.ALGO_FFT_ND, _abi.ALGO_FFT_RS,
+            _abi.ALGO_FFT_ND_POW2, _abi.ALGO_FFT_RS_POW2, _abi.ALGO_FFT]
+
+
+def dispatcher_configs(n, seed=0):
+    """Seeded configurations: rank {1: 60%, 2: 35%, 3: 5%}; ranks 1 and 3 as
+    the uneven batch (2^8..2^20 elements, odd kernels 3..127); rank 2 with
+    2^8..2^24 elements, each axis <= 4096, odd kernels 3..63 per axis;
+    dilation {1, 2}, stride {1, 2}, padding uniform over the four modes."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        rank = int(rng.choice([1, 2, 3], p=(0.6, 0.35, 0.05)))
+        hi, kmax = (24, 63) if rank == 2 else (20, 127)
+        total = math.exp(rng.uniform(8 * math.log(2), hi * math.log(2)))
+        props = rng.dirichlet(np.ones(rank))
+        shape = [max(1, int(round(total ** p))) for p in props]
+        if rank == 2:
+            shape = [min(s, 4096) for s in shape]
+        kshape = [int(rng.choice(np.arange(3, kmax + 1, 2))) for _ in range(rank)]
+        out.append(Spec(shape, kshape, int(rng.choice([1, 2])), int(rng.choice([1, 2])),
+                        PAD_MODES[int(rng.integers(0, 4))]))
+    return out
+
+
+def spec_key(s):
+    return (tuple(s.shape), tuple(s.kshape), s.dilation, s.stride, s.pad)
+
+
+class TimingDB:
+    """spec -> ms per MEASURED variant (inf: variant unavailable / failed)."""
+
+    def __init__(self):
+        self.specs, self.times = [], []
+        self._index = {}
+
+    def add(self, spec, times):
+        self._index[spec_key(spec)] = len(self.specs)
+        self.specs.append(spec)
+        self.times.append(list(times))
+
+    def lookup(self, spec):
+        i = self._index.get(spec_key(spec))
+        return None if i is None else self.times[i]
+
+    def save(self, path):
+        S = self.specs
+        r = np.array([s.rank for s in S], np.int8)
+        sh = np.array([list(s.shape) + [1] * (3 - s.rank) for s in S], np.int32)
+        ks = np.array([list(s.kshape) + [1] * (3 - s.rank) for s in S], np.int16)
+        misc = np.array([[s.dilation, s.stride, PAD_MODES.index(s.pad)] for s in S], np.int8)
+        np.savez_compressed(path, rank=r, shape=sh, kshape=ks, misc=misc,
+                            times=np.array(self.times, np.float32), measured=np.array(MEASURED, np.int8))
+
+    @classmethod
+    def load(cls, path):
+        z = np.load(path)
+        db = cls()
+        for r, sh, ks, mi, t in zip(z["rank"], z["shape"], z["kshape"], z["misc"], z["times"]):
+            r = int(r)
+            db.add(Spec([int(v) for v in sh[:r]], [int(v) for v in ks[:r]], int(mi[0]), int(mi[1]),
+                        PAD_MODES[int(mi[2])]),
+                   [float(v) for v in t])
+        return db
+
+
+class Autotuner:
+    """Times the variants of one instance with seeded Uniform[-1, 1) data."""
+
+    def __init__(self, reps=2, seed=0):
+        import torch
+        self.torch = torch
+        self.reps = reps
+        self.gen = torch.Generator(device="cuda").manual_seed(seed)
+        self.L = _abi.lib()
+
+    def time_spec(self, spec, variants=MEASURED):
+        torch = self.torch
+        x = torch.rand(spec.shape, generator=self.gen, device="cuda") * 2 - 1
+        k = torch.rand(spec.kshape, generator=self.gen, device="cuda") * 2 - 1
+        p = build_problem(_abi.F32, spec.shape, with_dilation(k, spec.dilation), spec.conv_mode(),
+                          spec.padding_mode())
+        y = torch.empty(spec.out_shape(), device="cuda")
+        st = torch.cuda.current_stream()
+        sp = ctypes.c_void_p(st.cuda_stream)
+        args = (ctypes.byref(p), None, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(k.data_ptr()),
+                ctypes.c_void_p(y.data_ptr()), sp)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        out = []
+        for v in variants:
+            call = (args[0], v) + args[2:]
+            if self.L.ndconv_conv_algo(*call) != 0:  # unavailable for this instance / build
+                out.append(math.inf)
+                continue
+            best = math.inf
+            for _ in range(self.reps):
+                e0.record(st)
+                self.L.ndconv_conv_algo(*call)
+                e1.record(st)
+                e1.synchronize()
+                best = min(best, e0.elapsed_time(e1))
+            out.append(best)
+        torch.cuda.synchronize()
+        return out
+
+    def tune(self, specs, db=None, log_every=0):
+        db = db or TimingDB()
+        t0 = time.time()
+        for i, s in enumerate(specs):
+            db.add(s, self.time_spec(s))
+            if log_every and (i + 1) % log_every == 0:
+                print(f"timed {i + 1}/{len(specs)} in {time.time() - t0:.0f} s", flush=True)
+        return db
+
+
+def candidate_arrays(db):
+    """(times [n, 6] of the network's candidates, mask, the cost model's pick times)."""
+    T = np.array(db.times, np.float64)
+    cand = T[:, :6]
+    mask = np.isfinite(cand).astype(np.float64)
+    return cand, mask
+
+
+def model_pick_times(db):
+    """time of the cost model's choice (direct, or the FFT form it picks) per instance"""
+    from .dispatch import ModelDispatcher
+    T = np.array(db.times, np.float64)
+    picks = ModelDispatcher().choose(db.specs)
+    return np.array([T[i, 0] if a == 0 else T[i, 6] for i, a in enumerate(picks)])
+
+
+def regret(times_pick, times_best):
+    tp, tb = np.asarray(times_pick), np.asarray(times_best)
+    per = tp / tb - 1.0
+    return {"mean": float(per.mean()), "median": float(np.median(per)), "p90": float(np.quantile(per, 0.9)),
+            "total_ratio": float(tp.sum() / tb.sum()), "exact_picks": float((per <= 1e-9).mean())}
+
+
+def evaluate(net, db):
+    """Regret of the network's picks and of the cost model's picks vs the
+    exhaustive autotuner on db."""
+    from .dispatch import features
+    cand, mask = candidate_arrays(db)
+    best = np.where(mask > 0, cand, np.inf).min(1)
+    F = np.array([features(s) for s in db.specs])
+    from .mlp import CANDIDATES
+    picks = net.pick(F, mask)
+    t_mlp = np.array([cand[i, CANDIDATES.index(a)] for i, a in enumerate(picks)])
+    t_model = model_pick_times(db)
+    return {"n": len(db.specs), "mlp": regret(t_mlp, best), "cost_model": regret(t_model, best),
+            "sum_ms": {"best": float(best.sum()), "mlp": float(t_mlp.sum()), "cost_model": float(t_model.sum())}}
+
+
+def train_network(db, epochs=300, batch=256, lr=2e-3, seed=0):
+    from .dispatch import features
+    from .mlp import MLP
+    cand, mask = candidate_arrays(db)
+    F = np.array([features(s) for s in db.specs])
+    logt = np.log(np.where(mask > 0, cand, 1.0))
+    net = MLP(seed=seed)
+    loss = net.fit(F, logt, mask, epochs=epochs, batch=batch, lr=lr, seed=seed)
+    return net, loss
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--train", type=int, default=20000)
+    ap.add_argument("--holdout", type=int, default=2000)
+    ap.add_argument("--epochs", type=int, default=300)
+    ap.add_argument("--out", required=True)
+    ap.add_argument("--seed", type=int, default=5000)
+    ap.add_argument("--timings", default=None, help="reuse a saved timings.npz (train + holdout)")
+    args = ap.parse_args()
+    os.makedirs(args.out, exist_ok=True)
+    n = args.train + args.holdout
+    t0 = time.time()
+    if args.timings:
+        db = TimingDB.load(args.timings)
+    else:
+        db = Autotuner().tune(dispatcher_configs(n, seed=args.seed), log_every=1000)
+        db.save(os.path.join(args.out, "timings.npz"))
+    t_tune = time.time() - t0
+    train, hold = TimingDB(), TimingDB()
+    for i, (s, t) in enumerate(zip(db.specs, db.times)):
+        (train if i < args.train else hold).add(s, t)
+    t1 = time.time()
+    net, loss = train_network(train, epochs=args.epochs)
+    t_train = time.time() - t1
+    rep = {"train": len(train.specs), "holdout": len(hold.specs), "final_train_loss": loss,
+           "tune_s": t_tune, "train_s": t_train, "holdout_eval": evaluate(net, hold),
+           "train_eval": evaluate(net, train)}
+    net.save(os.path.join(args.out, "dispatcher_mlp.json"), extra={"report": rep["holdout_eval"]})
+    with open(os.path.join(args.out, "dispatcher_report.json"), "w") as f:
+        json.dump(rep, f, indent=1)
+    print(json.dumps(rep["holdout_eval"]), flush=True)
+
+
+if __name__ == "__main__":
+    main()

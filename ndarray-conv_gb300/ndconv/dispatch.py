@@ -1,10 +1,10 @@
 """Per-instance algorithm choice for batches.
 
-Three dispatchers share one interface (`choose(problems) -> [0|1]`):
-  * ModelDispatcher: the library's cost model (ndconv_plan_info);
+Three dispatchers share one interface (`choose(specs) -> [ndconv_algo]`):
+  * ModelDispatcher: the library's cost model (ndconv_plan_info): direct (0)
+    or FFT (1, form picked inside the library);
   * TunedDispatcher: the autotuner's timing database (measured, exhaustive);
-  * the learned MLP (ndconv.mlp) trained on the autotuner's timings.
-"""
+  * MLPDispatcher (ndconv.mlp): the network trained on those timings."""
 import ctypes
 import math
 
@@ -61,12 +61,14 @@ class ModelDispatcher:
 
 
 class TunedDispatcher:
-    """argmin of measured times from the autotuner's database."""
+    """argmin of measured times from the autotuner's database (the cost
+    model for instances it has not timed)."""
 
     def __init__(self, db):
         self.db = db
 
     def choose(self, specs):
+        from .autotune import MEASURED
         out = []
         for s in specs:
             t = self.db.lookup(s)
@@ -74,5 +76,5 @@ class TunedDispatcher:
                 info = plan_info(spec_problem(s))
                 out.append(1 if info[7] and info[1] < info[0] else 0)
             else:
-                out.append(int(np.argmin(t)))
+                out.append(int(MEASURED[int(np.argmin(t[:6]))]))
         return out

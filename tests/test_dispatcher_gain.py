@@ -1,0 +1,73 @@
+"""What the trained dispatcher network gains over the cost model, judged by
+the exhaustive autotuner's timings of 2,000 held-out configurations
+(committed with the network in ndconv/data).
+
+The host test evaluates the committed parameters with the f64 oracle of the
+network; the GPU test repeats the picks with the library's CUDA forward
+kernel and checks that both agree."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import mlp_ref
+
+DATA = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "ndarray-conv_gb300", "ndconv",
+                    "data")
+
+
+def _load():
+    from ndconv.autotune import TimingDB, candidate_arrays
+    from ndconv.dispatch import features
+    with open(os.path.join(DATA, "dispatcher_mlp.json")) as f:
+        net = json.load(f)
+    db = TimingDB.load(os.path.join(DATA, "dispatcher_timings.npz"))
+    n_train = 20000
+    hold = TimingDB()
+    for s, t in zip(db.specs[n_train:], db.times[n_train:]):
+        hold.add(s, t)
+    F = np.array([features(s) for s in hold.specs])
+    cand, mask = candidate_arrays(hold)
+    return net, hold, F, cand, mask
+
+
+def _oracle_picks(net, F, mask):
+    x = (F - np.array(net["mu"])) / np.array(net["sd"])
+    y, _ = mlp_ref.forward(np.array(net["params"], np.float64), x, *net["dims"])
+    return np.argmin(np.where(mask > 0, y, np.inf), axis=1)
+
+
+def test_trained_network_beats_cost_model_on_held_out_timings():
+    from ndconv.autotune import model_pick_times
+    net, hold, F, cand, mask = _load()
+    assert len(hold.specs) == 2000
+    best = np.where(mask > 0, cand, np.inf).min(1)
+    idx = _oracle_picks(net, F, mask)
+    t_net = cand[np.arange(len(idx)), idx]
+    t_model = model_pick_times(hold)
+    r_net, r_model = t_net.sum() / best.sum(), t_model.sum() / best.sum()
+    # the network's picks cost at most 5 % over the exhaustive autotuner's,
+    # and clearly less than the cost model's
+    assert r_net <= 1.05, r_net
+    assert r_net < r_model - 0.1, (r_net, r_model)
+    assert (t_net / best - 1).mean() < 0.05
+
+
+@pytest.mark.gpu
+def test_cuda_forward_picks_match_oracle():
+    import __graft_entry__ as g
+    g.build()
+    from ndconv.mlp import MLP
+    net_json, hold, F, cand, mask = _load()
+    net = MLP.load(os.path.join(DATA, "dispatcher_mlp.json"))
+    pred = net.predict(F)
+    x = (F - np.array(net_json["mu"])) / np.array(net_json["sd"])
+    y64, _ = mlp_ref.forward(np.array(net_json["params"], np.float64), x, *net_json["dims"])
+    assert np.abs(pred - y64).max() < 1e-3
+    a = np.argmin(np.where(mask > 0, pred, np.inf), axis=1)
+    b = _oracle_picks(net_json, F, mask)
+    # ties within float rounding may flip; the time of the picks must agree
+    ta, tb = cand[np.arange(len(a)), a], cand[np.arange(len(b)), b]
+    assert abs(ta.sum() - tb.sum()) <= 0.01 * tb.sum()
+    net.close()

@@ -1,0 +1,73 @@
+"""The 3xBF16 split tensor-core direct path (tcgen05 + TMA) against the f64
+oracle: normwise error <= 1e-5 on f32 problems, the reference's NaN
+pattern when an input is not finite, and UNSUPPORTED where it does not
+apply."""
+import numpy as np
+import pytest
+
+import ndconv
+from ndconv import _abi
+from helpers import F64, BorderType, ConvMode, PaddingMode, normwise_err, problem, with_dilation
+from oracle import oracle as O
+from test_gpu_parity import _c3, _oracle64
+
+pytestmark = pytest.mark.gpu
+TOL32 = 1e-5
+BF = _abi.ALGO_DIRECT_BF16X3
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    import __graft_entry__ as g
+    g.build()
+
+
+@pytest.mark.parametrize("shape,kshape,dil,mode,pm", [
+    ((40, 150), (3, 5), 1, ConvMode.Same, PaddingMode.Zeros),
+    ((70, 300), (7, 15), 2, ConvMode.Same, PaddingMode.Custom([BorderType.Reflect, BorderType.Circular])),
+    ((3, 70, 150), (2, 3, 5), [1, 2, 3], ConvMode.Custom([1, 2, 3], [2, 1, 2]), PaddingMode.Replicate),
+    ((5, 9, 140), (2, 3, 4), 1, ConvMode.Explicit([[1, 0], [2, 1], [0, 3]], [2, 1, 3]), PaddingMode.Const(0.5)),
+    ((1000,), (31,), 1, ConvMode.Full, PaddingMode.Zeros),
+    ((130, 257), (17, 17), 1, ConvMode.Valid, PaddingMode.Zeros),
+    ((64, 640), (15, 63), 1, ConvMode.Same, PaddingMode.Circular),
+])
+def test_bf16x3_vs_oracle(shape, kshape, dil, mode, pm):
+    rng = np.random.default_rng(sum(shape) + sum(kshape))
+    x = rng.random(shape).astype(np.float32)
+    k = rng.random(kshape).astype(np.float32)
+    y64 = _oracle64(x, with_dilation(k, dil), mode, pm)
+    y = ndconv.conv_algo(x, with_dilation(k, dil), mode, pm, BF)
+    assert y.shape == y64.shape
+    assert normwise_err(y, y64) <= TOL32, normwise_err(y, y64)
+    # signed data (cancellation) too
+    xs, ks = (x - 0.5).astype(np.float32), (k - 0.5).astype(np.float32)
+    y64 = _oracle64(xs, with_dilation(ks, dil), mode, pm)
+    assert normwise_err(ndconv.conv_algo(xs, with_dilation(ks, dil), mode, pm, BF), y64) <= TOL32
+
+
+@pytest.mark.parametrize("cplx", [False])
+def test_bf16x3_config3(cplx):
+    x, kw, mode, pm = _c3(cplx)
+    y64 = _oracle64(x, kw, mode, pm)
+    assert normwise_err(ndconv.conv_algo(x, kw, mode, pm, BF), y64) <= TOL32
+
+
+def test_bf16x3_nonfinite_follows_reference():
+    rng = np.random.default_rng(3)
+    x = rng.random((20, 200)).astype(np.float32)
+    k = rng.random((5, 9)).astype(np.float32)
+    x[7, 33] = np.inf
+    mode, pm = ConvMode.Same, PaddingMode.Zeros
+    st, y64 = O.conv(problem(F64, x, k, mode, pm), x.astype(np.float64), k.astype(np.float64))
+    y = ndconv.conv_algo(x, k, mode, pm, BF)
+    assert np.array_equal(np.isnan(y), np.isnan(y64)) and np.array_equal(np.isinf(y), np.isinf(y64))
+    fin = np.isfinite(y64)
+    assert np.allclose(y[fin], y64[fin], rtol=1e-5, atol=1e-5)
+
+
+def test_bf16x3_unsupported():
+    x = np.ones((30, 40), np.float32)
+    with pytest.raises(ndconv.ConvError):
+        ndconv.conv_algo(x, np.ones((3, 3), np.float32), ConvMode.Custom([1, 1], [2, 1]), PaddingMode.Zeros, BF)
+    with pytest.raises(ndconv.ConvError):
+        ndconv.conv_algo(x.astype(np.int32), np.ones((3, 3), np.int32), ConvMode.Same, PaddingMode.Zeros, BF)
