@@ -343,6 +343,29 @@ template <typename T> inline bool host_zero(const T &v) { return v == (T)0; }
 template <> inline bool host_zero<c32>(const c32 &v) { return v.re == 0.0f && v.im == 0.0f; }
 template <> inline bool host_zero<c64>(const c64 &v) { return v.re == 0.0 && v.im == 0.0; }
 
+// Does tap t of an axis (positions t d + o s, o < out) read data (an input
+// sample, directly or through the border map) for at least one output?
+// The data region [p0, p0 + n) is answered arithmetically; only positions
+// in the pads (O(k_eff) of them) consult the border map.
+inline bool tap_reads_data(const AxisGeom &A, int64_t t, const std::vector<char> &front,
+                           const std::vector<char> &back) {
+    const int64_t s = A.s, f = t * A.d, last = f + (A.out - 1) * s;
+    const int64_t lo = f > A.p0 ? f : A.p0, hi = last < A.p0 + A.n - 1 ? last : A.p0 + A.n - 1;
+    if (lo <= hi) {
+        const int64_t p = f + (lo - f + s - 1) / s * s;  // first position >= lo
+        if (p <= hi) return true;
+    }
+    for (int64_t p = f; p <= last && p < A.p0; p += s)
+        if (front[(size_t)p]) return true;
+    const int64_t b0 = A.p0 + A.n;
+    if (last >= b0) {
+        int64_t p = f >= b0 ? f : f + (b0 - f + s - 1) / s * s;
+        for (; p <= last && p < A.L; p += s)
+            if (back[(size_t)(p - b0)]) return true;
+    }
+    return false;
+}
+
 template <typename T> void restrict_live_taps(DirectParams<T> &P) {
     for (int a = 0; a < 3; a++) {
         P.t_lo[a] = 0;
@@ -355,27 +378,15 @@ template <typename T> void restrict_live_taps(DirectParams<T> &P) {
         const AxisGeom &A = P.g.ax[a];
         lo[a] = 0;
         n[a] = A.K;
-        if (A.K <= 1 || A.L > (int64_t)1 << 28) continue;
-        // per residue class r mod s: prefix counts of live positions r, r+s, ...
-        const int64_t s = A.s;
-        std::vector<int64_t> pre((size_t)(A.L + s + 1), 0);
-        // pre[r + s*m] = live positions among {r, r+s, ..., r+(m-1)s}
-        for (int64_t r = 0; r < s; r++) {
-            int64_t c = 0;
-            for (int64_t p = r; p < A.L + s; p += s) {
-                pre[(size_t)p] = c;
-                if (p < A.L && axis_map(A, p) >= 0) c++;
-            }
-        }
+        if (A.K <= 1) continue;
+        // pad cells that hold data after the border map
+        std::vector<char> front((size_t)(A.p0 > 0 ? A.p0 : 0)), back((size_t)(A.p1 > 0 ? A.p1 : 0));
+        for (int64_t j = 0; j < A.p0; j++) front[(size_t)j] = axis_map(A, j) >= 0;
+        for (int64_t j = 0; j < A.p1; j++) back[(size_t)j] = axis_map(A, A.p0 + A.n + j) >= 0;
         int64_t first = -1, last = -1;
         for (int64_t t = 0; t < A.K; t++) {
-            const int64_t p0 = t * A.d;
-            const int64_t p1 = p0 + (A.out - 1) * s;  // last position this tap reads
-            if (p0 >= A.L) break;
-            const int64_t r = p0 % s;
-            const int64_t cnt = pre[(size_t)(p1 + s)] - pre[(size_t)p0];
-            (void)r;
-            if (cnt > 0) {
+            if (t * A.d >= A.L) break;
+            if (tap_reads_data(A, t, front, back)) {
                 if (first < 0) first = t;
                 last = t;
             }

@@ -562,7 +562,7 @@ __device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsi
 }
 
 template <typename T, int MODE>
-__global__ void __launch_bounds__(256) row_kernel(const __grid_constant__ RowArgs<T> A) {
+__global__ void __launch_bounds__(512) row_kernel(const __grid_constant__ RowArgs<T> A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     row_block<T, MODE>(A, blockIdx.x, blockIdx.y, smem_raw);
 }
@@ -706,12 +706,22 @@ int pick_nb(int64_t len, int64_t rows, size_t per_row_bytes) {
     return nb;
 }
 
+// Threads per row-pass CTA: one radix-8 (or the widest) butterfly per thread
+// in a single round where that fits 128..512 threads (e.g. 320 for a
+// 2560-point transform), else 256.
+template <typename T> int row_threads(const RowArgs<T> &A) {
+    int maxw = 0;
+    for (int i = 0; i < A.pl.nst; i++) maxw = std::max(maxw, (A.pl.L / A.pl.rad[i]) << A.lognb);
+    if (maxw < 128 || maxw > 512) return kThreads;
+    return (maxw + 31) / 32 * 32;
+}
+
 // n_inst instances (grid.y); A.spec_is etc. describe their spacing
 template <typename T, int MODE> int launch_row_mode(const RowArgs<T> &A, size_t sm, unsigned grid, int n_inst,
                                                     cudaStream_t st) {
     int st_ = ensure_smem(row_kernel<T, MODE>);
     if (st_) return st_;
-    row_kernel<T, MODE><<<dim3(grid, (unsigned)n_inst), kThreads, sm, st>>>(A);
+    row_kernel<T, MODE><<<dim3(grid, (unsigned)n_inst), row_threads(A), sm, st>>>(A);
     ndconv_count_launch();
     NDCONV_CUDA_OK(cudaGetLastError());
     return NDCONV_OK;
@@ -753,7 +763,7 @@ template <typename T> int launch_row(RowArgs<T> A, cudaStream_t st, int n_inst =
 // Two independent forward row passes in one launch (the kernel rows and the
 // data rows of the row-spectral form): CTAs [0, ga) take pass A, the rest B.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) row_pair_kernel(const __grid_constant__ RowArgs<T> A,
+__global__ void __launch_bounds__(512) row_pair_kernel(const __grid_constant__ RowArgs<T> A,
                                                             const __grid_constant__ RowArgs<T> B, unsigned ga) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     if (blockIdx.x < ga) row_block<T, ROW_FWD_KERNEL>(A, blockIdx.x, blockIdx.y, smem_raw);
@@ -771,7 +781,8 @@ template <typename T> int launch_row_pair(RowArgs<T> A, RowArgs<T> B, cudaStream
     if ((s = prep_row(B, n_inst, gb, sb))) return s;
     if (ga + gb > 0x7fffffff) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "too many FFT rows");
     if ((s = ensure_smem(row_pair_kernel<T>))) return s;
-    row_pair_kernel<T><<<dim3((unsigned)(ga + gb), (unsigned)n_inst), kThreads, std::max(sa, sb), st>>>(
+    row_pair_kernel<T><<<dim3((unsigned)(ga + gb), (unsigned)n_inst), std::max(row_threads(A), row_threads(B)),
+                         std::max(sa, sb), st>>>(
         A, B, (unsigned)ga);
     ndconv_count_launch();
     NDCONV_CUDA_OK(cudaGetLastError());
@@ -1856,12 +1867,7 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
         max_levels = std::max(max_levels, (int)lv.size());
         B->n_fft++;
     }
-    for (int l = 0; l < max_levels; l++)
-        for (int64_t i = 0; i < n; i++) {
-            std::vector<Level> &lv = per_inst[(size_t)i];
-            if ((int)lv.size() > l) B->tasks.insert(B->tasks.end(), lv[l].tasks.begin(), lv[l].tasks.end());
-        }
-    // ---- direct tiles, largest instances first
+    // ---- direct tiles, largest instances first, with a work estimate per task
     std::vector<std::pair<double, int64_t>> order;
     for (int64_t i = 0; i < n; i++) {
         HostInst &h = B->inst[(size_t)i];
@@ -1871,10 +1877,41 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
         order.push_back({-work, i});
     }
     std::sort(order.begin(), order.end());
+    std::vector<Task> dtasks;
+    std::vector<double> dwork;
     for (auto &o : order) {
         HostInst &h = B->inst[(size_t)o.second];
-        B->smem = std::max(B->smem, direct_tasks(B, h, B->tasks));
+        const size_t before = dtasks.size();
+        B->smem = std::max(B->smem, direct_tasks(B, h, dtasks));
+        const size_t cnt = dtasks.size() - before;
+        for (size_t t = 0; t < cnt; t++) dwork.push_back(-o.first / (double)(cnt ? cnt : 1));
         B->n_direct++;
+    }
+    // ---- queue order.  A task of FFT level l > 0 spins until level l - 1 of
+    // its instance is done, so levels are separated by slices of direct work
+    // (which never waits): the costliest direct tiles first (they set the
+    // critical path), then level 0, a slice of direct tiles, level 1, ...
+    {
+        double total = 0;
+        for (double w : dwork) total += w;
+        size_t d = 0;
+        double done = 0;
+        auto take = [&](double upto) {
+            while (d < dtasks.size() && done < upto) {
+                B->tasks.push_back(dtasks[d]);
+                done += dwork[d];
+                d++;
+            }
+        };
+        take(max_levels > 0 ? 0.25 * total : total);
+        for (int l = 0; l < max_levels; l++) {
+            for (int64_t i = 0; i < n; i++) {
+                std::vector<Level> &lv = per_inst[(size_t)i];
+                if ((int)lv.size() > l) B->tasks.insert(B->tasks.end(), lv[l].tasks.begin(), lv[l].tasks.end());
+            }
+            take(0.25 * total + 0.75 * total * (double)(l + 1) / (double)max_levels);
+        }
+        take(total * 2 + 1);
     }
     for (auto &h : B->inst) B->n_standalone += h.standalone;
     // ---- device copies

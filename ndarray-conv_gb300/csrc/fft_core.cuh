@@ -199,8 +199,14 @@ __device__ __forceinline__ void stockham_stage(const C *src, C *dst, int L, int 
 #pragma unroll
         for (int r = 0; r < RAD; r++) v[r] = src[sx<C>(((j + r * nr) << lognb) + b)];
         if (t) {
+            // one table load per butterfly; the other powers by products in
+            // a log-depth tree (w^k from at most three rounded products)
+            C w[RAD];
+            w[1] = twiddle<INV>(tw, t * twstep);
 #pragma unroll
-            for (int r = 1; r < RAD; r++) v[r] = cmul(v[r], twiddle<INV>(tw, t * r * twstep));
+            for (int r = 2; r < RAD; r++) w[r] = (r & 1) ? cmul(w[r - 1], w[1]) : cmul(w[r / 2], w[r / 2]);
+#pragma unroll
+            for (int r = 1; r < RAD; r++) v[r] = cmul(v[r], w[r]);
         }
         if constexpr (RAD == 2) dft2<INV>(v);
         else if constexpr (RAD == 3) dft3<INV>(v);
