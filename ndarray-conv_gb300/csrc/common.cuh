@@ -26,6 +26,7 @@ template <> struct Elem<float> {
     __host__ __device__ static float from(double re, double) { return (float)re; }
     __device__ static bool is_zero(float v) { return v == 0.0f; }
     __device__ static void mac(float &a, float x, float w) { a = fmaf(x, w, a); }
+    __device__ static void add(float &a, float x) { a += x; }
     __device__ static float out(float a) { return a; }
 };
 template <> struct Elem<double> {
@@ -36,6 +37,7 @@ template <> struct Elem<double> {
     __host__ __device__ static double from(double re, double) { return re; }
     __device__ static bool is_zero(double v) { return v == 0.0; }
     __device__ static void mac(double &a, double x, double w) { a = fma(x, w, a); }
+    __device__ static void add(double &a, double x) { a += x; }
     __device__ static double out(double a) { return a; }
 };
 // i32: wrapping two's-complement arithmetic, as the reference's release build
@@ -47,6 +49,7 @@ template <> struct Elem<int32_t> {
     __host__ __device__ static int32_t from(double re, double) { return (int32_t)re; }
     __device__ static bool is_zero(int32_t v) { return v == 0; }
     __device__ static void mac(uint32_t &a, int32_t x, int32_t w) { a += (uint32_t)x * (uint32_t)w; }
+    __device__ static void add(uint32_t &a, int32_t x) { a += (uint32_t)x; }
     __device__ static int32_t out(uint32_t a) { return (int32_t)a; }
 };
 template <> struct Elem<c32> {
@@ -62,6 +65,10 @@ template <> struct Elem<c32> {
         a.im = fmaf(x.re, w.im, a.im);
         a.im = fmaf(x.im, w.re, a.im);
     }
+    __device__ static void add(c32 &a, c32 x) {
+        a.re += x.re;
+        a.im += x.im;
+    }
     __device__ static c32 out(c32 a) { return a; }
 };
 template <> struct Elem<c64> {
@@ -76,6 +83,10 @@ template <> struct Elem<c64> {
         a.re = fma(-x.im, w.im, a.re);
         a.im = fma(x.re, w.im, a.im);
         a.im = fma(x.im, w.re, a.im);
+    }
+    __device__ static void add(c64 &a, c64 x) {
+        a.re += x.re;
+        a.im += x.im;
     }
     __device__ static c64 out(c64 a) { return a; }
 };

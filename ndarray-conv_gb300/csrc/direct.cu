@@ -12,6 +12,7 @@
 #include "common.cuh"
 #include "direct.h"
 #include "direct_blocks.cuh"
+#include "fold.h"
 
 #include <type_traits>
 
@@ -63,11 +64,15 @@ cudaError_t launch_main(const T *x, const T *k, T *y, DirectParams<T> &P, cudaSt
 
 template <typename T>
 cudaError_t launch_any(const T *x, const T *k, T *y, DirectParams<T> P, cudaStream_t st, int force_naive,
-                       int64_t n_inst) {
+                       int64_t n_inst, void *scratch = nullptr, size_t scratch_bytes = 0) {
     const AxisGeom &A0 = P.g.ax[0], &A1 = P.g.ax[1], &A2 = P.g.ax[2];
     if (A0.out <= 0 || A1.out <= 0 || A2.out <= 0 || n_inst <= 0) return cudaSuccess;
     if (!force_naive) {
+        const DirectParams<T> full = P;
         restrict_live_taps(P);
+        FoldParams F;
+        if (n_inst == 1 && !P.xs && plan_fold(P, F))
+            return fold_launch<T>(x, k, y, F, full, st, scratch, scratch_bytes);
         permute_axes_for_tiles(P);
     }
     cudaError_t e = launch_main<T>(x, k, y, P, st, force_naive, n_inst);
@@ -84,12 +89,18 @@ cudaError_t launch_any(const T *x, const T *k, T *y, DirectParams<T> P, cudaStre
 
 template <typename T>
 cudaError_t direct_conv_launch(const T *x, const T *k, T *y, DirectParams<T> P, cudaStream_t st,
-                               int force_naive) {
+                               int force_naive, void *scratch, size_t scratch_bytes) {
     P.xs = nullptr;
     P.ks = nullptr;
     P.ys = nullptr;
     P.inst_base = 0;
-    return launch_any<T>(x, k, y, P, st, force_naive, 1);
+    return launch_any<T>(x, k, y, P, st, force_naive, 1, scratch, scratch_bytes);
+}
+
+template <typename T> size_t direct_scratch_bytes(DirectParams<T> P) {
+    restrict_live_taps(P);
+    FoldParams F;
+    return plan_fold(P, F) ? fold_scratch_bytes<T>(F) : 0;
 }
 
 template <typename T>
@@ -118,15 +129,14 @@ NDCONV_INST_DIRECT_BATCH(double)
 NDCONV_INST_DIRECT_BATCH(int32_t)
 NDCONV_INST_DIRECT_BATCH(c32)
 NDCONV_INST_DIRECT_BATCH(c64)
-template cudaError_t direct_conv_launch<float>(const float *, const float *, float *, DirectParams<float>,
-                                               cudaStream_t, int);
-template cudaError_t direct_conv_launch<double>(const double *, const double *, double *,
-                                                DirectParams<double>, cudaStream_t, int);
-template cudaError_t direct_conv_launch<int32_t>(const int32_t *, const int32_t *, int32_t *,
-                                                 DirectParams<int32_t>, cudaStream_t, int);
-template cudaError_t direct_conv_launch<c32>(const c32 *, const c32 *, c32 *, DirectParams<c32>,
-                                             cudaStream_t, int);
-template cudaError_t direct_conv_launch<c64>(const c64 *, const c64 *, c64 *, DirectParams<c64>,
-                                             cudaStream_t, int);
+#define NDCONV_INST_DIRECT(T)                                                                             \
+    template cudaError_t direct_conv_launch<T>(const T *, const T *, T *, DirectParams<T>, cudaStream_t, int, \
+                                               void *, size_t);                                            \
+    template size_t direct_scratch_bytes<T>(DirectParams<T>);
+NDCONV_INST_DIRECT(float)
+NDCONV_INST_DIRECT(double)
+NDCONV_INST_DIRECT(int32_t)
+NDCONV_INST_DIRECT(c32)
+NDCONV_INST_DIRECT(c64)
 
 }  // namespace ndconv

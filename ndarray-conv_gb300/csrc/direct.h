@@ -33,9 +33,13 @@ template <typename T> struct DirectParams {
 
 // x, k: device pointers (strided per g.ax[i].xs / ks); y: contiguous output.
 // force_naive selects the unstaged kernel (tests use it as a second path).
+// scratch (optional, direct_scratch_bytes(P) bytes) serves the axis-folding
+// form; without it that form allocates stream-ordered.
 template <typename T>
 cudaError_t direct_conv_launch(const T *x, const T *k, T *y, DirectParams<T> P, cudaStream_t st,
-                               int force_naive);
+                               int force_naive, void *scratch = nullptr, size_t scratch_bytes = 0);
+// device scratch the launch would use (0 when no folding applies)
+template <typename T> size_t direct_scratch_bytes(DirectParams<T> P);
 
 // n instances sharing the geometry; xs / ks / ys: device arrays of n device pointers.
 template <typename T>

@@ -706,10 +706,12 @@ int pick_nb(int64_t len, int64_t rows, size_t per_row_bytes) {
     return nb;
 }
 
-// Threads per row-pass CTA: one radix-8 (or the widest) butterfly per thread
-// in a single round where that fits 128..512 threads (e.g. 320 for a
-// 2560-point transform), else 256.
-template <typename T> int row_threads(const RowArgs<T> &A) {
+// Threads per row-pass CTA.  A launch of few CTAs is latency-bound: one
+// radix-8 (or the widest) butterfly per thread in a single round where that
+// fits 128..512 threads (e.g. 320 for a 2560-point transform).  A launch of
+// many CTAs is throughput-bound: 256, which keeps more CTAs resident.
+template <typename T> int row_threads(const RowArgs<T> &A, int64_t ctas) {
+    if (ctas > 4 * 152) return kThreads;
     int maxw = 0;
     for (int i = 0; i < A.pl.nst; i++) maxw = std::max(maxw, (A.pl.L / A.pl.rad[i]) << A.lognb);
     if (maxw < 128 || maxw > 512) return kThreads;
@@ -721,7 +723,7 @@ template <typename T, int MODE> int launch_row_mode(const RowArgs<T> &A, size_t 
                                                     cudaStream_t st) {
     int st_ = ensure_smem(row_kernel<T, MODE>);
     if (st_) return st_;
-    row_kernel<T, MODE><<<dim3(grid, (unsigned)n_inst), row_threads(A), sm, st>>>(A);
+    row_kernel<T, MODE><<<dim3(grid, (unsigned)n_inst), row_threads(A, (int64_t)grid * n_inst), sm, st>>>(A);
     ndconv_count_launch();
     NDCONV_CUDA_OK(cudaGetLastError());
     return NDCONV_OK;
@@ -781,8 +783,9 @@ template <typename T> int launch_row_pair(RowArgs<T> A, RowArgs<T> B, cudaStream
     if ((s = prep_row(B, n_inst, gb, sb))) return s;
     if (ga + gb > 0x7fffffff) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "too many FFT rows");
     if ((s = ensure_smem(row_pair_kernel<T>))) return s;
-    row_pair_kernel<T><<<dim3((unsigned)(ga + gb), (unsigned)n_inst), std::max(row_threads(A), row_threads(B)),
-                         std::max(sa, sb), st>>>(
+    const int64_t ctas = (ga + gb) * n_inst;
+    row_pair_kernel<T><<<dim3((unsigned)(ga + gb), (unsigned)n_inst),
+                         std::max(row_threads(A, ctas), row_threads(B, ctas)), std::max(sa, sb), st>>>(
         A, B, (unsigned)ga);
     ndconv_count_launch();
     NDCONV_CUDA_OK(cudaGetLastError());
@@ -1606,7 +1609,8 @@ struct HostInst {
     Plan3 P;
     const void *x, *k;
     void *y;
-    size_t ws_off;   // spectra offset (FFT)
+    size_t ws_off;   // workspace offset: spectra (FFT) or folded weights (direct)
+    size_t ws_bytes; // direct: folded-form scratch (0: none)
     FftConvPlan<float> cp;
 };
 
@@ -1734,6 +1738,23 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
         h.y = out[i];
         h.standalone = (h.P.dtype != NDCONV_F32);
         h.ws_off = 0;
+        h.ws_bytes = 0;
+        if (h.algo == 0) {
+            // direct instances taken by the axis-folding form run as ordinary
+            // launches with their scratch in the plan's workspace
+            switch (h.P.dtype) {
+            case NDCONV_F32: h.ws_bytes = direct_scratch_bytes<float>(h.P.direct<float>()); break;
+            case NDCONV_F64: h.ws_bytes = direct_scratch_bytes<double>(h.P.direct<double>()); break;
+            case NDCONV_I32: h.ws_bytes = direct_scratch_bytes<int32_t>(h.P.direct<int32_t>()); break;
+            case NDCONV_C32: h.ws_bytes = direct_scratch_bytes<c32>(h.P.direct<c32>()); break;
+            default: h.ws_bytes = direct_scratch_bytes<c64>(h.P.direct<c64>()); break;
+            }
+            if (h.ws_bytes) {
+                h.standalone = 1;
+                h.ws_off = ws;
+                ws += (h.ws_bytes + 255) / 256 * 256;
+            }
+        }
         if (h.algo == 1 && !h.standalone) {
             if ((s = make_conv_plan<float>(h.P.geom<float>(), h.cp, h.fv))) return fail(s);
             h.ws_off = ws;
@@ -1949,12 +1970,14 @@ int run_standalone(ndconv_batch_plan *B, cudaStream_t st) {
         int s = NDCONV_OK;
         if (h.algo == 0) {
             cudaError_t e = cudaSuccess;
+            void *ds = h.ws_bytes ? scr : nullptr;
+            const size_t db = h.ws_bytes;
             switch (h.P.dtype) {
-            case NDCONV_F32: e = direct_conv_launch<float>((const float *)h.x, (const float *)h.k, (float *)h.y, h.P.direct<float>(), st, 0); break;
-            case NDCONV_F64: e = direct_conv_launch<double>((const double *)h.x, (const double *)h.k, (double *)h.y, h.P.direct<double>(), st, 0); break;
-            case NDCONV_I32: e = direct_conv_launch<int32_t>((const int32_t *)h.x, (const int32_t *)h.k, (int32_t *)h.y, h.P.direct<int32_t>(), st, 0); break;
-            case NDCONV_C32: e = direct_conv_launch<c32>((const c32 *)h.x, (const c32 *)h.k, (c32 *)h.y, h.P.direct<c32>(), st, 0); break;
-            default: e = direct_conv_launch<c64>((const c64 *)h.x, (const c64 *)h.k, (c64 *)h.y, h.P.direct<c64>(), st, 0); break;
+            case NDCONV_F32: e = direct_conv_launch<float>((const float *)h.x, (const float *)h.k, (float *)h.y, h.P.direct<float>(), st, 0, ds, db); break;
+            case NDCONV_F64: e = direct_conv_launch<double>((const double *)h.x, (const double *)h.k, (double *)h.y, h.P.direct<double>(), st, 0, ds, db); break;
+            case NDCONV_I32: e = direct_conv_launch<int32_t>((const int32_t *)h.x, (const int32_t *)h.k, (int32_t *)h.y, h.P.direct<int32_t>(), st, 0, ds, db); break;
+            case NDCONV_C32: e = direct_conv_launch<c32>((const c32 *)h.x, (const c32 *)h.k, (c32 *)h.y, h.P.direct<c32>(), st, 0, ds, db); break;
+            default: e = direct_conv_launch<c64>((const c64 *)h.x, (const c64 *)h.k, (c64 *)h.y, h.P.direct<c64>(), st, 0, ds, db); break;
             }
             if (e != cudaSuccess) return ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e));
             continue;
