@@ -256,6 +256,24 @@ def bench_uneven(args, world, rank, local_rank):
     e1.record(stream)
     barrier()
     plain_ms = e0.elapsed_time(e1) / nplain
+    # the plain drop-in: the same instances as per-instance library calls with
+    # the library's default choice (cost model), no batching, no tuning
+    dropin_ms = plain_ms
+    if args.dispatch != "model":
+        dplan = BatchPlan([(s.conv_mode(), s.padding_mode()) for s in specs], xs,
+                          [with_dilation(k, s.dilation) for k, s in zip(ks, specs)], outs=ys,
+                          algos=ModelDispatcher().choose(specs))
+        dplan.run_plain()
+        barrier()
+        e0.record(stream)
+        for _ in range(nplain):
+            dplan.run_plain()
+        e1.record(stream)
+        barrier()
+        dropin_ms = e0.elapsed_time(e1) / nplain
+        dplan.close()
+        plan.run(graph=True)  # outputs of the measured plan again (spot checks below)
+        barrier()
     # end to end: inputs from pinned host memory, outputs back to it
     hx, hk = xbuf.cpu().pin_memory(), kbuf.cpu().pin_memory()
     hy = torch.empty_like(ybuf, device="cpu").pin_memory()
@@ -275,9 +293,9 @@ def bench_uneven(args, world, rank, local_rank):
     barrier()
     e2e_ms = e0.elapsed_time(e1) / args.steps
     if dist:
-        t = torch.tensor([ms, plain_ms, e2e_ms], device="cuda")
+        t = torch.tensor([ms, plain_ms, e2e_ms, dropin_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms, plain_ms, e2e_ms = [float(v) for v in t.tolist()]
+        ms, plain_ms, e2e_ms, dropin_ms = [float(v) for v in t.tolist()]
     bytes_step = sum(s.bytes() for s in specs)
     peak, peak_kind = peaks()
     value = bytes_step * world / (ms * 1e-3) / 1e9
@@ -315,6 +333,10 @@ def bench_uneven(args, world, rank, local_rank):
                                       "model": "cost model"}[args.dispatch], "plan": info,
                        "plain_per_instance_gbs": bytes_step * world / (plain_ms * 1e-3) / 1e9,
                        "batched_over_plain": plain_ms / ms,
+                       "plain_dropin_gbs": bytes_step * world / (dropin_ms * 1e-3) / 1e9,
+                       "batched_tuned_over_plain_dropin": dropin_ms / ms,
+                       "plain_note": "plain = per-instance calls with the same picks; plain drop-in = "
+                                     "per-instance calls with the library's default (cost model) picks",
                        "l2": f"inputs {xbuf.numel() * 4 / 1e9:.2f} GB per GPU, larger than L2, no flush"},
             "roofline": {"bound": "hbm", "achieved": bytes_step / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": bytes_step / (ms * 1e-3) / 1e9 / peak, "traffic": None,
@@ -501,15 +523,21 @@ def main():
     dk = [torch.empty_like(k) for k in ks]
 
     PD_X, PD_K = ptrs(dx), ptrs(dk)
+    arr = ctypes.c_void_p * B
+    HX, HK, HY = arr(*[t.data_ptr() for t in hx]), arr(*[t.data_ptr() for t in hk]), arr(*[t.data_ptr() for t in hy])
 
     def e2e_step():
+        if args.form == "batched":
+            # the library's host-memory batch: copies of one chunk overlap the
+            # convolution of the previous one
+            s = L.ndconv_conv_batch_host(pp, algo, B, HX, HK, HY, proc._handle if algo == 1 else None, sp)
+            if s:
+                raise RuntimeError(_abi.last_error())
+            return
         for i in range(B):
             dx[i].copy_(hx[i], non_blocking=True)
             dk[i].copy_(hk[i], non_blocking=True)
-        if args.form == "plain":
-            plain_step(dx, dk, ys)
-        else:
-            batched_step_ptrs(PD_X, PD_K, P_Y)
+        plain_step(dx, dk, ys)
         for i in range(B):
             hy[i].copy_(ys[i], non_blocking=True)
 

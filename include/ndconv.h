@@ -143,6 +143,18 @@ typedef enum {
 int ndconv_conv_algo(const ndconv_problem *p, int32_t algo, const void *data, const void *kernel, void *out,
                      void *stream);
 
+/* conv (algo 0) or conv_fft (algo 1) over n same-geometry instances whose
+ * data, kernels and outputs are HOST arrays (contiguous; pinned memory for
+ * full speed): chunks of instances are staged through library-owned device
+ * buffers so that host->device copies, the convolution and device->host
+ * copies of successive chunks overlap.  Asynchronous on `stream`: the host
+ * arrays must stay valid, and the outputs are complete, when `stream` has
+ * synchronised.  No reference counterpart (the crate converts one host
+ * array per call). */
+int ndconv_conv_batch_host(const ndconv_problem *p, int32_t algo, int64_t n, const void *const *data,
+                           const void *const *kernel, void *const *out, ndconv_fft_processor *proc,
+                           void *stream);
+
 /* ConvExt::conv for f32 on the tensor cores: 3xBF16 split products
  * (x k ~ xh kh + xh kl + xl kh) accumulated in f32, normwise error ~1e-6 vs
  * f64.  Unit stride along the middle canonical axis only (else

@@ -1278,8 +1278,7 @@ int conv_fft_batch_run(const Geom3<T> &g, int reverse, int64_t n, const T *const
     return NDCONV_OK;
 }
 
-// Spectra bytes of the full N-d form; the row-spectral form needs no more
-// (K0 K1 <= F0 F1 kernel rows, P0 P1 <= P0 F1 data rows).
+// Spectra bytes of whichever FFT form needs more.
 template <typename T> size_t conv_fft_scratch_bytes(const Geom3<T> &g, int variant) {
     using R = typename Elem<T>::Real;
     using C = typename CplxT<R>::type;
@@ -1292,7 +1291,9 @@ template <typename T> size_t conv_fft_scratch_bytes(const Geom3<T> &g, int varia
     const int astar = F[0] > 1 ? 0 : (F[1] > 1 ? 1 : 2);
     const size_t nK = (size_t)F[0] * F[1] * H;
     const size_t nS = (astar == 2) ? 0 : (size_t)P[0] * F[1] * H;
-    return sizeof(C) * (nK + nS) + 256;
+    // the row-spectral form: kernel rows and padded data rows
+    const size_t rs = (astar == 2) ? 0 : (size_t)(g.ax[0].K * g.ax[1].K + P[0] * P[1]) * H;
+    return sizeof(C) * std::max(nK + nS, rs) + 256;
 }
 
 #define NDCONV_INST_FFT(T)                                                                          \
@@ -1705,6 +1706,33 @@ size_t direct_tasks(ndconv_batch_plan *B, HostInst &h, std::vector<Task> &out) {
 namespace ndconv {
 namespace batch {
 
+// NDCONV_OK when every pass of the FFT form fits the kernels' limits
+// (shared memory, grid), NDCONV_ERR_UNSUPPORTED otherwise.  Host only.
+template <typename T> int fft_fits(const Geom3<T> &g, int fv) {
+    using C = typename FftConvPlan<T>::C;
+    FftConvPlan<T> cp;
+    int s = make_conv_plan<T>(g, cp, fv);
+    if (s) return s;
+    return conv_fft_passes<T>(
+        g, 0, cp, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0, 1, nullptr, nullptr,
+        [&](RowArgs<T> &A, int) {
+            int64_t grid;
+            size_t sm;
+            return A.n_rows > 0 ? prep_row(A, 1, grid, sm) : NDCONV_OK;
+        },
+        [&](ColArgs<C> &A, int) {
+            int64_t gx, gy;
+            size_t sm;
+            return (A.n_outer > 0 && A.n_inner > 0) ? prep_col(A, gx, gy, sm) : NDCONV_OK;
+        },
+        [&](RowArgs<T> &A, RowArgs<T> &B, int) {
+            int64_t grid;
+            size_t sm;
+            int r = A.n_rows > 0 ? prep_row(A, 1, grid, sm) : NDCONV_OK;
+            return r ? r : (B.n_rows > 0 ? prep_row(B, 1, grid, sm) : NDCONV_OK);
+        });
+}
+
 // Build the plan: per-instance tasks, spectra, device copies of everything.
 int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const void *const *data,
            const void *const *kernel, void *const *out, ndconv_batch_plan **outp) {
@@ -1739,6 +1767,19 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
         h.standalone = (h.P.dtype != NDCONV_F32);
         h.ws_off = 0;
         h.ws_bytes = 0;
+        if (h.algo == 1) {
+            // transforms that do not fit one CTA's shared memory: the same
+            // convolution by the direct kernels (as ndconv_conv_fft does)
+            int fs = NDCONV_OK;
+            switch (h.P.dtype) {
+            case NDCONV_F32: fs = fft_fits<float>(h.P.geom<float>(), h.fv); break;
+            case NDCONV_F64: fs = fft_fits<double>(h.P.geom<double>(), h.fv); break;
+            case NDCONV_C32: fs = fft_fits<c32>(h.P.geom<c32>(), h.fv); break;
+            default: fs = fft_fits<c64>(h.P.geom<c64>(), h.fv); break;
+            }
+            if (fs == NDCONV_ERR_UNSUPPORTED) h.algo = 0;
+            else if (fs) return fail(fs);
+        }
         if (h.algo == 0) {
             // direct instances taken by the axis-folding form run as ordinary
             // launches with their scratch in the plan's workspace

@@ -210,3 +210,29 @@ def conv_batch(datas, kernels, conv_mode, padding_mode, stream=None):
 def conv_fft_batch(datas, kernels, conv_mode, padding_mode, processor=None, stream=None):
     """conv_fft over many instances with one geometry, L2-sized waves."""
     return _run_batch(1, datas, kernels, conv_mode, padding_mode, processor=processor, stream=stream)
+
+
+def conv_batch_host(xs, ks, ys, conv_mode, padding_mode, algo=1, processor=None, stream=None, sync=True):
+    """conv (algo 0) / conv_fft (algo 1) over same-geometry instances held in
+    HOST memory: xs, ks inputs and ys preallocated outputs, each a list of
+    contiguous CPU torch tensors (pinned for full speed).  The library pipelines
+    the copies with the convolution; `sync` waits for the stream."""
+    L = _abi.lib()
+    if not (len(xs) == len(ks) == len(ys)) or not xs:
+        raise ValueError("need equally many data, kernel and output arrays (at least one)")
+    kwd0 = into_kernel_with_dilation(ks[0])
+    kt = [into_kernel_with_dilation(k).kernel for k in ks]
+    from .api import KernelWithDilation
+    p = build_problem(dtype_code(xs[0].dtype), tuple(xs[0].shape),
+                      KernelWithDilation(kt[0], kwd0.dilation, kwd0.reverse_flag), conv_mode, padding_mode)
+    n = len(xs)
+    arr = ctypes.c_void_p * n
+    px = arr(*[x.data_ptr() for x in xs])
+    pk = arr(*[k.data_ptr() for k in kt])
+    py = arr(*[y.data_ptr() for y in ys])
+    h = processor._handle if processor is not None else None
+    st = L.ndconv_conv_batch_host(ctypes.byref(p), algo, n, px, pk, py, h, _stream_ptr(stream))
+    raise_for_status(st, p, algo)
+    if sync:
+        (stream or torch.cuda.current_stream()).synchronize()
+    return ys

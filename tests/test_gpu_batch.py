@@ -84,3 +84,27 @@ def test_batch_mixed_types_standalone():
         f = ndconv.conv if algos[i] == 0 else ndconv.conv_fft
         assert torch.equal(plan.outs[i], f(xs[i], ks[i], *modes[i]))
     plan.close()
+
+
+@pytest.mark.parametrize("algo", [0, 1])
+@pytest.mark.parametrize("dt", ["float32", "int32"])
+def test_host_batch_equals_device_calls(algo, dt):
+    import torch
+    from helpers import BorderType, ConvMode, PaddingMode
+    if algo == 1 and dt == "int32":
+        pytest.skip("no integer FFT")
+    g = torch.Generator().manual_seed(7)
+    n, xs_, ks_ = 37, (64, 900), (5, 9)
+    if dt == "int32":
+        xs = [torch.randint(-100, 100, xs_, generator=g, dtype=torch.int32).pin_memory() for _ in range(n)]
+        ks = [torch.randint(-9, 9, ks_, generator=g, dtype=torch.int32).pin_memory() for _ in range(n)]
+    else:
+        xs = [torch.rand(xs_, generator=g).pin_memory() for _ in range(n)]
+        ks = [torch.rand(ks_, generator=g).pin_memory() for _ in range(n)]
+    mode, pm = ConvMode.Same, PaddingMode.Custom([BorderType.Reflect, BorderType.Circular])
+    ys = [torch.empty(xs_, dtype=xs[0].dtype).pin_memory() for _ in range(n)]
+    ndconv.conv_batch_host(xs, [with_dilation(k, 2) for k in ks], ys, mode, pm, algo=algo)
+    f = ndconv.conv if algo == 0 else ndconv.conv_fft
+    for i in range(n):
+        ref = f(xs[i].cuda(), with_dilation(ks[i].cuda(), 2), mode, pm).cpu()
+        assert torch.equal(ys[i], ref), i
