@@ -218,6 +218,16 @@ int ndconv_conv_fft_noalloc(const ndconv_problem *p, const void *data, const voi
 int ndconv_fft_processor_create(int32_t dtype, ndconv_fft_processor **out);
 int ndconv_fft_processor_destroy(ndconv_fft_processor *proc);
 
+/* Kernel-spectrum reuse (the crate sketches a "baked" processor in
+ * commented-out code, src/conv_fft/mod.rs:22-42,306-392): transform `kernel`
+ * (device pointer) for problem p once and keep its spectrum in proc; later
+ * ndconv_conv_fft(p2, x, kernel, y, proc, s) calls whose geometry equals p's
+ * (shapes, dilation, modes, padding; data strides may differ) and whose
+ * kernel pointer equals `kernel` skip the kernel transform.  Bake again after
+ * changing the kernel's contents. */
+int ndconv_fft_processor_bake(ndconv_fft_processor *proc, const ndconv_problem *p, const void *kernel,
+                              void *stream);
+
 /* Processor::forward (src/conv_fft/processor/mod.rs:79-100; real.rs:24-155,
  * complex.rs:119-128).  Output layout is the reference's: axes rotated right
  * after each pass; out_shape receives it (query with out == NULL). */

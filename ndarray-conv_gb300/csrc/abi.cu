@@ -306,6 +306,23 @@ extern "C" int ndconv_conv_algo(const ndconv_problem *p, int32_t algo, const voi
     }
 }
 
+extern "C" int ndconv_fft_processor_bake(ndconv_fft_processor *proc, const ndconv_problem *p, const void *kernel,
+                                         void *stream) {
+    if (!proc || !kernel) return ndconv_fail(NDCONV_ERR_INVALID, "null argument");
+    Plan3 P;
+    int s = plan_problem(p, 1, &P);
+    if (s) return s;
+    if (P.dtype != ndconv_proc_dtype(proc)) return ndconv_fail(NDCONV_ERR_INVALID, "processor element type differs");
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (P.dtype) {
+    case NDCONV_F32: return conv_fft_bake<float>(P.geom<float>(), P.reverse, (const float *)kernel, proc, st);
+    case NDCONV_F64: return conv_fft_bake<double>(P.geom<double>(), P.reverse, (const double *)kernel, proc, st);
+    case NDCONV_C32: return conv_fft_bake<c32>(P.geom<c32>(), P.reverse, (const c32 *)kernel, proc, st);
+    case NDCONV_C64: return conv_fft_bake<c64>(P.geom<c64>(), P.reverse, (const c64 *)kernel, proc, st);
+    default: return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "integer FFT convolution is not supported");
+    }
+}
+
 extern "C" int ndconv_conv_batch(const ndconv_problem *p, int64_t n, const void *const *data,
                                  const void *const *kernel, void *const *out, void *stream) {
     Plan3 P;

@@ -78,8 +78,8 @@ cudaError_t launch_any(const T *x, const T *k, T *y, DirectParams<T> P, cudaStre
     cudaError_t e = launch_main<T>(x, k, y, P, st, force_naive, n_inst);
     if (e != cudaSuccess || !taps_restricted(P) || std::is_same<T, int32_t>::value) return e;
     // skipped taps with a non-finite weight: every output is NaN, as in the reference
-    const int64_t nk = A0.K * A1.K * A2.K;
-    int64_t parts = (nk + 4095) / 4096;
+    const int64_t nk = A0.K * A1.K;  // kernel rows
+    int64_t parts = (nk + 255) / 256;
     if (parts > 64) parts = 64;
     dead_tap_fixup_kernel<T><<<dim3((unsigned)parts, (unsigned)n_inst), 256, 0, st>>>(k, y, P);
     ndconv_count_launch();

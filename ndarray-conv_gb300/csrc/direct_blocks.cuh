@@ -426,19 +426,28 @@ __device__ __forceinline__ void dead_tap_fixup_block(const T *__restrict__ k, T 
     if (threadIdx.x == 0) found = 0;
     __syncthreads();
     const AxisGeom &A0 = P.g.ax[0], &A1 = P.g.ax[1], &A2 = P.g.ax[2];
-    const int64_t nk = A0.K * A1.K * A2.K;
-    const int64_t chunk = (nk + nparts - 1) / nparts;
-    const int64_t b = part * chunk, e = (b + chunk < nk) ? b + chunk : nk;
-    for (int64_t f = b + threadIdx.x; f < e; f += blockDim.x) {
-        // kernel element (ez, ey, ex) feeds tap (tz, ty, tx) (reversed when convolving)
-        const int64_t ex = f % A2.K, ey = (f / A2.K) % A1.K, ez = f / (A2.K * A1.K);
-        const int64_t tx = tap_source(ex, A2.K, P.reverse), ty = tap_source(ey, A1.K, P.reverse),
-                      tz = tap_source(ez, A0.K, P.reverse);
-        const bool live = tz >= P.t_lo[0] && tz < P.t_lo[0] + P.t_n[0] && ty >= P.t_lo[1] &&
-                          ty < P.t_lo[1] + P.t_n[1] && tx >= P.t_lo[2] && tx < P.t_lo[2] + P.t_n[2];
-        if (live) continue;
-        if (non_finite(k[ez * A0.ks + ey * A1.ks + ex * A2.ks])) found = 1;
+    // kernel rows (ez, ey) split over the parts; within a row whose z and y
+    // taps are live only the x taps outside the live range are read
+    const int64_t nrows = A0.K * A1.K;
+    const int64_t chunk = (nrows + nparts - 1) / nparts;
+    const int64_t b = part * chunk, e = (b + chunk < nrows) ? b + chunk : nrows;
+    const int64_t lo2 = P.t_lo[2], hi2 = P.t_lo[2] + P.t_n[2];
+    bool bad = false;
+    for (int64_t r = b + threadIdx.x; r < e; r += blockDim.x) {
+        const int64_t ey = r % A1.K, ez = r / A1.K;
+        const int64_t ty = tap_source(ey, A1.K, P.reverse), tz = tap_source(ez, A0.K, P.reverse);
+        const bool zy_live = tz >= P.t_lo[0] && tz < P.t_lo[0] + P.t_n[0] && ty >= P.t_lo[1] &&
+                             ty < P.t_lo[1] + P.t_n[1];
+        const T *kr = k + ez * A0.ks + ey * A1.ks;
+        if (zy_live) {
+            // tap tx is fed by element tap_source(tx) (an involution)
+            for (int64_t tx = 0; tx < lo2; tx++) bad |= non_finite(kr[tap_source(tx, A2.K, P.reverse) * A2.ks]);
+            for (int64_t tx = hi2; tx < A2.K; tx++) bad |= non_finite(kr[tap_source(tx, A2.K, P.reverse) * A2.ks]);
+        } else {
+            for (int64_t ex = 0; ex < A2.K; ex++) bad |= non_finite(kr[ex * A2.ks]);
+        }
     }
+    if (bad) found = 1;
     __syncthreads();
     if (!found) return;
     const int64_t total = A0.out * A1.out * A2.out;

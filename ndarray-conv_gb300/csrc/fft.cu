@@ -18,6 +18,7 @@
 // (the circular wrap only touches indices < k_eff - 1).
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <map>
 #include <string>
 #include <mutex>
@@ -872,6 +873,12 @@ struct ndconv_fft_processor {
     void *ws;
     size_t ws_bytes;
     int device;
+    // baked kernel spectrum (ndconv_fft_processor_bake): valid for calls
+    // whose geometry key and kernel pointer match
+    void *kbuf = nullptr;
+    size_t kbuf_bytes = 0;
+    const void *kptr = nullptr;
+    std::vector<unsigned char> kkey;
 };
 
 namespace ndconv {
@@ -969,6 +976,10 @@ template <typename T> int make_conv_plan(const Geom3<T> &g, FftConvPlan<T> &cp, 
     return NDCONV_OK;
 }
 
+// Which passes conv_fft_passes emits: all, only the kernel spectrum, or
+// only the data passes (kernel spectrum already in Kh).
+enum : int { PASSES_ALL = 0, PASSES_KERNEL = 1, PASSES_DATA = 2 };
+
 // The passes of instances [base, base + cnt), in order, handed to emit_row /
 // emit_col (launch them, or record them as tasks).  Kh / S hold cnt
 // instances' spectra back to back.  Pointers come from the device arrays
@@ -977,7 +988,7 @@ template <typename T, typename EmitRow, typename EmitCol, typename EmitPair>
 int conv_fft_passes(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, const T *x, const T *k, T *y,
                     const T *const *xs, const T *const *ks, T *const *ys, int64_t base, int cnt,
                     typename FftConvPlan<T>::C *Kh, typename FftConvPlan<T>::C *S, EmitRow &&emit_row,
-                    EmitCol &&emit_col, EmitPair &&emit_pair) {
+                    EmitCol &&emit_col, EmitPair &&emit_pair, int which = PASSES_ALL) {
     using R = typename Elem<T>::Real;
     using C = typename FftConvPlan<T>::C;
     const AxisGeom &A0 = g.ax[0], &A1 = g.ax[1], &A2 = g.ax[2];
@@ -1017,7 +1028,8 @@ int conv_fft_passes(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, co
         dr.spec_s1 = H;
         dr.spec_is = S_is;
         dr.scale = 1;
-        if ((s = emit_pair(kr, dr, cnt))) return s;
+        if (which == PASSES_KERNEL) return emit_row(kr, cnt);
+        if ((s = (which == PASSES_DATA) ? emit_row(dr, cnt) : emit_pair(kr, dr, cnt))) return s;
         RowArgs<T> ir = cp.rk;
         ir.mode = ROW_INV_MAC;
         ir.g = g;
@@ -1060,8 +1072,8 @@ int conv_fft_passes(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, co
     kr.spec_s1 = H;
     kr.spec_is = K_is;
     kr.scale = 1;
-    if ((s = emit_row(kr, cnt))) return s;
-    if (F[1] > 1) {
+    if (which != PASSES_DATA && (s = emit_row(kr, cnt))) return s;
+    if (F[1] > 1 && which != PASSES_DATA) {
         ColArgs<C> c{};
         c.mode = COL_FWD;
         c.src = c.dst = Kh;
@@ -1075,7 +1087,7 @@ int conv_fft_passes(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, co
         c.tw = cp.tw1;
         if ((s = emit_col(c, cnt))) return s;
     }
-    if (F[0] > 1) {
+    if (F[0] > 1 && which != PASSES_DATA) {
         ColArgs<C> c{};
         c.mode = COL_FWD;
         c.src = c.dst = Kh;
@@ -1089,6 +1101,7 @@ int conv_fft_passes(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, co
         if ((s = emit_col(c, cnt))) return s;
     }
     const R scale = (R)(1.0 / ((double)F[0] * (double)F[1] * (double)F[2]));
+    if (which == PASSES_KERNEL) return NDCONV_OK;
 
     if (cp.astar == 2) {
         RowArgs<T> fr = cp.rk;
@@ -1212,13 +1225,14 @@ int conv_fft_passes(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, co
 template <typename T>
 int conv_fft_wave(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, const T *x, const T *k, T *y,
                   const T *const *xs, const T *const *ks, T *const *ys, int64_t base, int cnt,
-                  typename FftConvPlan<T>::C *Kh, typename FftConvPlan<T>::C *S, cudaStream_t st) {
+                  typename FftConvPlan<T>::C *Kh, typename FftConvPlan<T>::C *S, cudaStream_t st,
+                  int which = PASSES_ALL) {
     using C = typename FftConvPlan<T>::C;
     return conv_fft_passes<T>(
         g, reverse, cp, x, k, y, xs, ks, ys, base, cnt, Kh, S,
         [&](RowArgs<T> &A, int n) { return launch_row<T>(A, st, n); },
         [&](ColArgs<C> &A, int n) { return launch_col<C>(A, st, n); },
-        [&](RowArgs<T> &A, RowArgs<T> &B, int n) { return launch_row_pair<T>(A, B, st, n); });
+        [&](RowArgs<T> &A, RowArgs<T> &B, int n) { return launch_row_pair<T>(A, B, st, n); }, which);
 }
 
 // bytes of spectra a wave may keep so that they stay in L2 between passes
@@ -1231,6 +1245,23 @@ size_t wave_budget_bytes() {
     return v;
 }
 }  // namespace
+
+// bytes that identify a geometry for a baked kernel spectrum
+template <typename T> std::vector<unsigned char> bake_key(const Geom3<T> &g, int reverse) {
+    std::vector<unsigned char> key(sizeof(Geom3<T>) + sizeof(int) + 1);
+    Geom3<T> gz;
+    memset(&gz, 0, sizeof(gz));
+    for (int a = 0; a < 3; a++) {
+        gz.ax[a] = g.ax[a];
+        gz.ax[a].xs = 0;  // data strides do not change the kernel spectrum
+        gz.cf[a] = g.cf[a];
+        gz.cb[a] = g.cb[a];
+    }
+    memcpy(key.data(), &gz, sizeof(gz));
+    memcpy(key.data() + sizeof(gz), &reverse, sizeof(int));
+    key.back() = (unsigned char)sizeof(T);
+    return key;
+}
 
 template <typename T>
 int conv_fft_run(const Geom3<T> &g, int reverse, const T *x, const T *k, T *y,
@@ -1249,7 +1280,38 @@ int conv_fft_run(const Geom3<T> &g, int reverse, const T *x, const T *k, T *y,
     }
     C *Kh = reinterpret_cast<C *>(base);
     C *S = Kh + cp.nK;
+    if (proc && proc->kbuf && proc->kptr == (const void *)k && variant == FFTV_AUTO &&
+        proc->kkey == bake_key<T>(g, reverse))
+        return conv_fft_wave<T>(g, reverse, cp, x, k, y, nullptr, nullptr, nullptr, 0, 1,
+                                static_cast<C *>(proc->kbuf), S, st, PASSES_DATA);
     return conv_fft_wave<T>(g, reverse, cp, x, k, y, nullptr, nullptr, nullptr, 0, 1, Kh, S, st);
+}
+
+template <typename T>
+int conv_fft_bake(const Geom3<T> &g, int reverse, const T *k, ndconv_fft_processor *proc, cudaStream_t st) {
+    using C = typename FftConvPlan<T>::C;
+    FftConvPlan<T> cp;
+    int s = make_conv_plan(g, cp, FFTV_AUTO);
+    if (s) return s;
+    const size_t bytes = sizeof(C) * cp.nK + 256;
+    if (proc->kbuf_bytes < bytes) {
+        if (proc->kbuf) {
+            NDCONV_CUDA_OK(cudaStreamSynchronize(st));
+            cudaFree(proc->kbuf);
+            proc->kbuf = nullptr;
+            proc->kbuf_bytes = 0;
+        }
+        NDCONV_CUDA_OK(cudaMalloc(&proc->kbuf, bytes));
+        proc->kbuf_bytes = bytes;
+    }
+    proc->kptr = nullptr;
+    proc->kkey.clear();
+    s = conv_fft_wave<T>(g, reverse, cp, nullptr, k, nullptr, nullptr, nullptr, nullptr, 0, 1,
+                         static_cast<C *>(proc->kbuf), nullptr, st, PASSES_KERNEL);
+    if (s) return s;
+    proc->kptr = k;
+    proc->kkey = bake_key<T>(g, reverse);
+    return NDCONV_OK;
 }
 
 template <typename T>
@@ -1302,7 +1364,8 @@ template <typename T> size_t conv_fft_scratch_bytes(const Geom3<T> &g, int varia
     template int conv_fft_batch_run<T>(const Geom3<T> &, int, int64_t, const T *const *,          \
                                        const T *const *, T *const *, ndconv_fft_processor *,      \
                                        cudaStream_t, int);                                         \
-    template size_t conv_fft_scratch_bytes<T>(const Geom3<T> &, int);
+    template size_t conv_fft_scratch_bytes<T>(const Geom3<T> &, int);                              \
+    template int conv_fft_bake<T>(const Geom3<T> &, int, const T *, ndconv_fft_processor *, cudaStream_t);
 NDCONV_INST_FFT(float)
 NDCONV_INST_FFT(double)
 NDCONV_INST_FFT(c32)
@@ -1472,10 +1535,9 @@ extern "C" int ndconv_fft_processor_create(int32_t dtype, ndconv_fft_processor *
 
 extern "C" int ndconv_fft_processor_destroy(ndconv_fft_processor *p) {
     if (!p) return NDCONV_OK;
-    if (p->ws) {
-        cudaDeviceSynchronize();
-        cudaFree(p->ws);
-    }
+    if (p->ws || p->kbuf) cudaDeviceSynchronize();
+    if (p->ws) cudaFree(p->ws);
+    if (p->kbuf) cudaFree(p->kbuf);
     delete p;
     return NDCONV_OK;
 }
@@ -1532,8 +1594,8 @@ __device__ __forceinline__ int ld_acquire(const int *p) {
 // get NaN everywhere, like the reference's sums.
 __global__ void __launch_bounds__(256) batch_fixup_kernel(const DirectParams<float> *__restrict__ dargs,
                                                           const int *__restrict__ fix) {
-    const DirectParams<float> &P = dargs[fix[blockIdx.x]];
-    dead_tap_fixup_block<float>(P.k1, P.y1, P, 0, 1);
+    const DirectParams<float> &P = dargs[fix[blockIdx.y]];
+    dead_tap_fixup_block<float>(P.k1, P.y1, P, blockIdx.x, gridDim.x);
 }
 
 __global__ void __launch_bounds__(256) persistent_kernel(const Task *__restrict__ tasks, int ntasks,
@@ -1639,6 +1701,8 @@ struct ndconv_batch_plan {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int64_t n_fft = 0, n_direct = 0, n_standalone = 0;
+    cudaStream_t side = nullptr;  // ordinary launches beside the persistent kernel
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 namespace ndconv {
@@ -1998,6 +2062,12 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
         B->grid = std::max(1, per_sm) * sms;
         if ((int64_t)B->grid > (int64_t)B->tasks.size()) B->grid = (int)std::max<size_t>(1, B->tasks.size());
     }
+    if (B->n_standalone > 0) {
+        cudaError_t e = cudaStreamCreateWithFlags(&B->side, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&B->ev_fork, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&B->ev_join, cudaEventDisableTiming);
+        if (e != cudaSuccess) return fail(ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e)));
+    }
     *outp = B;
     return NDCONV_OK;
 }
@@ -2041,8 +2111,17 @@ int run_standalone(ndconv_batch_plan *B, cudaStream_t st) {
 // One execution: reset the queue, standalone instances, persistent kernel.
 int enqueue(ndconv_batch_plan *B, cudaStream_t st) {
     NDCONV_CUDA_OK(cudaMemsetAsync(B->d_ctrs, 0, sizeof(int) * (size_t)(B->nctrs + 2), st));
-    int s = run_standalone(B, st);
+    // ordinary launches (other element types, folded and oversized instances)
+    // on a side stream, forked from and joined back into st, so they run
+    // beside the persistent kernel instead of before it
+    const bool side = B->n_standalone > 0 && B->side && B->ev_fork && B->ev_join;
+    if (side) {
+        NDCONV_CUDA_OK(cudaEventRecord(B->ev_fork, st));
+        NDCONV_CUDA_OK(cudaStreamWaitEvent(B->side, B->ev_fork, 0));
+    }
+    int s = run_standalone(B, side ? B->side : st);
     if (s) return s;
+    if (side) NDCONV_CUDA_OK(cudaEventRecord(B->ev_join, B->side));
     if (!B->tasks.empty()) {
         persistent_kernel<<<B->grid, 256, B->smem, st>>>(
             (const Task *)B->d_tasks, (int)B->tasks.size(), (const RowArgs<float> *)B->d_rargs,
@@ -2051,9 +2130,11 @@ int enqueue(ndconv_batch_plan *B, cudaStream_t st) {
         ndconv_count_launch();
         NDCONV_CUDA_OK(cudaGetLastError());
     }
+    if (side) NDCONV_CUDA_OK(cudaStreamWaitEvent(st, B->ev_join, 0));
     if (!B->fix.empty()) {
-        batch_fixup_kernel<<<(unsigned)B->fix.size(), 256, 0, st>>>((const DirectParams<float> *)B->d_dargs,
-                                                                    (const int *)B->d_fix);
+        // parts per instance: kernel rows over 8 CTAs at most
+        batch_fixup_kernel<<<dim3(8, (unsigned)B->fix.size()), 256, 0, st>>>((const DirectParams<float> *)B->d_dargs,
+                                                                             (const int *)B->d_fix);
         ndconv_count_launch();
         NDCONV_CUDA_OK(cudaGetLastError());
     }
@@ -2172,6 +2253,9 @@ extern "C" int ndconv_batch_destroy(ndconv_batch_plan *B) {
     cudaFree(B->d_fix);
     cudaFree(B->d_ctrs);
     cudaFree(B->ws);
+    if (B->ev_fork) cudaEventDestroy(B->ev_fork);
+    if (B->ev_join) cudaEventDestroy(B->ev_join);
+    if (B->side) cudaStreamDestroy(B->side);
     delete B;
     return NDCONV_OK;
 }

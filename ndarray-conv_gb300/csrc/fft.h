@@ -19,6 +19,11 @@ int conv_fft_run(const Geom3<T> &g, int reverse, const T *x, const T *k, T *y,
                  ndconv_fft_processor *proc, cudaStream_t st, void *scratch, size_t scratch_bytes,
                  int variant = FFTV_AUTO);
 template <typename T> size_t conv_fft_scratch_bytes(const Geom3<T> &g, int variant = FFTV_AUTO);
+// Transform kernel k for geometry g into proc's baked spectrum; later
+// conv_fft_run calls with proc, the same geometry and the same k pointer
+// skip the kernel transform.
+template <typename T>
+int conv_fft_bake(const Geom3<T> &g, int reverse, const T *k, ndconv_fft_processor *proc, cudaStream_t st);
 // n instances sharing the geometry; xs / ks / ys are device arrays of n
 // device pointers.  Runs in waves whose spectra fit a share of L2.
 template <typename T>

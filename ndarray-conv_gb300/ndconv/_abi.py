@@ -88,6 +88,7 @@ def lib():
         "ndconv_conv_fft_noalloc": (ctypes.c_int, [pp, vp, vp, vp, vp]),
         "ndconv_conv_algo": (ctypes.c_int, [pp, i32, vp, vp, vp, vp]),
         "ndconv_conv_batch_host": (ctypes.c_int, [pp, i32, ctypes.c_int64, vp, vp, vp, vp, vp]),
+        "ndconv_fft_processor_bake": (ctypes.c_int, [vp, pp, vp, vp]),
         "ndconv_conv_batch": (ctypes.c_int, [pp, ctypes.c_int64, vp, vp, vp, vp]),
         "ndconv_conv_fft_batch": (ctypes.c_int, [pp, ctypes.c_int64, vp, vp, vp, vp, vp]),
         "ndconv_fft_processor_create": (ctypes.c_int, [i32, ctypes.POINTER(vp)]),

@@ -118,6 +118,23 @@ class FftProcessor:
         except Exception:
             pass
 
+    def bake(self, data_like, kernel, conv_mode, padding_mode, stream=None):
+        """Keep the kernel's spectrum for this geometry (the crate's sketched
+        "baked" processor): later conv_fft_with_processor calls with the same
+        geometry and the same kernel tensor skip the kernel transform.  The
+        kernel must be a CUDA tensor; bake again after changing its contents."""
+        kwd = into_kernel_with_dilation(kernel)
+        if not (isinstance(kwd.kernel, torch.Tensor) and kwd.kernel.is_cuda):
+            raise TypeError("bake needs the kernel as a CUDA tensor (its address is the key)")
+        x = data_like if isinstance(data_like, torch.Tensor) else torch.empty(
+            tuple(np.shape(data_like)), dtype=kwd.kernel.dtype)
+        p = build_problem(dtype_code(kwd.kernel.dtype), tuple(x.shape), kwd, conv_mode, padding_mode,
+                          kernel_strides=kwd.kernel.stride())
+        st = _abi.lib().ndconv_fft_processor_bake(self._handle, ctypes.byref(p),
+                                                  ctypes.c_void_p(kwd.kernel.data_ptr()), _stream_ptr(stream))
+        raise_for_status(st, p, 1)
+        self._baked = kwd.kernel  # keep the keyed tensor alive
+
     def _cdtype(self):
         return torch.complex64 if self.dtype in (_abi.F32, _abi.C32) else torch.complex128
 
