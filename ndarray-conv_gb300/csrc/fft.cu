@@ -384,6 +384,10 @@ __device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsi
         rinfo[b] = ri;
     }
     __syncthreads();
+    // blockDim is a multiple of nb, so a thread always works on the same row
+    // b = tid mod nb of the CTA: its row facts live in registers
+    const int bt = threadIdx.x & (nb - 1);
+    const RowInfo rit = rinfo[bt];
 
     constexpr bool fwd = (MODE == ROW_FWD_DATA || MODE == ROW_FWD_KERNEL || MODE == ROW_FUSED ||
                           MODE == ROW_FWD_PLAIN);
@@ -399,8 +403,8 @@ __device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsi
                 const int u = u0 + q * T_;
                 v[q] = C{0, 0};
                 if (u < total) {
-                    const int b = u & (nb - 1), i = u >> lognb;
-                    const RowInfo &ri = rinfo[b];
+                    const int b = bt, i = u >> lognb;
+                    const RowInfo &ri = rit;
                     if (ri.valid) {
                         const int64_t r = rbase + b;
                         if (A.kind == RK_REAL_EVEN) {
@@ -433,11 +437,8 @@ __device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsi
         const int H = (int)A.H;
         if constexpr (MODE != ROW_FUSED) {
             const int tot = H << lognb;
-            for (int u = threadIdx.x; u < tot; u += blockDim.x) {
-                const int b = u & (nb - 1), k = u >> lognb;
-                const RowInfo &ri = rinfo[b];
-                if (ri.valid) spec[ri.soff + k] = res[sx<C>(u)];
-            }
+            if (rit.valid)
+                for (int u = threadIdx.x; u < tot; u += blockDim.x) spec[rit.soff + (u >> lognb)] = res[sx<C>(u)];
             return;
         }
         // ---- fused: multiply by the kernel spectrum, back to the time domain
@@ -473,9 +474,9 @@ __device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsi
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
                     const int u = u0 + q * T_;
-                    const int b = u & (nb - 1), k = u >> lognb;
-                    ok[q] = u < tot && rinfo[b].valid;
-                    soff[q] = ok[q] ? rinfo[b].soff + k : 0;
+                    const int k = u >> lognb;
+                    ok[q] = u < tot && rit.valid;
+                    soff[q] = ok[q] ? rit.soff + k : 0;
                     koff[q] = ok[q] ? k : 0;
                     acc[q] = C{0, 0};
                 }
@@ -513,11 +514,8 @@ __device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsi
                 }
             }
         } else {
-            for (int u = threadIdx.x; u < tot; u += blockDim.x) {
-                const int b = u & (nb - 1), k = u >> lognb;
-                const RowInfo &ri = rinfo[b];
-                dst[sx<C>(u)] = ri.valid ? ldcg_c(spec + ri.soff + k) : C{0, 0};
-            }
+            for (int u = threadIdx.x; u < tot; u += blockDim.x)
+                dst[sx<C>(u)] = rit.valid ? ldcg_c(spec + rit.soff + (u >> lognb)) : C{0, 0};
         }
         __syncthreads();
         if (A.kind == RK_REAL_ODD) {
@@ -541,10 +539,10 @@ __device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsi
     const int n_out = (int)(plain ? A.F : A.out_n);
     const int tot = n_out << lognb;
     const int coff = (int)A.crop_off, cstep = (int)A.crop_step;
+    if (!rit.valid) return;
     for (int u = threadIdx.x; u < tot; u += blockDim.x) {
-        const int b = u & (nb - 1), o = u >> lognb;
-        const RowInfo &ri = rinfo[b];
-        if (!ri.valid) continue;
+        const int b = bt, o = u >> lognb;
+        const RowInfo &ri = rit;
         const int p = plain ? o : (coff + o * cstep);
         R vr, vi;
         if (A.kind == RK_REAL_EVEN) {

@@ -28,7 +28,7 @@
 namespace ndconv {
 
 namespace {
-constexpr int FBM = 64, FBN = 64, FBK = 16;
+constexpr int FBM = 128, FBN = 64;
 
 // border-mapped index of tap t for output o on an axis (-1: padding zero)
 __device__ __forceinline__ int64_t fmap(const AxisGeom &A, int64_t o, int64_t t) {
@@ -110,16 +110,21 @@ __global__ void fold_scan_kernel(const T *__restrict__ x, const T *__restrict__ 
     if (bad) atomicOr(flag, 1);
 }
 
-// Y[om][co] = sum over kk = (ci, tm) of X[om][kk] W[co][kk]; 64 x 64 tile,
-// 4 x 4 outputs per thread, K in steps of 16 staged in shared memory.
+// Y[om][co] = sum over kk = (ci, tm) of X[om][kk] W[co][kk]: a 128 x 64
+// tile per CTA, 8 x 4 outputs per thread, K in steps of 16 staged in shared
+// memory.  The K slice's tap position and data offset (which depend on kk
+// only) are tabulated once per step, so the data gather is one border map
+// and one load per element.
 template <typename T>
 __global__ void __launch_bounds__(256) fold_gemm_kernel(const T *__restrict__ x, const T *__restrict__ W,
                                                         T *__restrict__ y, FoldParams F, const int *flag,
                                                         const T *__restrict__ k, DirectParams<T> fb) {
     using E = Elem<T>;
     using Acc = typename E::Acc;
+    constexpr int FBK = sizeof(T) > 8 ? 8 : 16;  // keeps 16-byte types under 48 KB of static smem
     __shared__ T As[FBK][FBM + 1];
     __shared__ T Bs[FBK][FBN + 1];
+    __shared__ int64_t kpos[FBK], koff[FBK];
     const AxisGeom &Am = F.ax[F.m], &A0 = F.ax[F.f0], &A1 = F.ax[F.f1];
     const int64_t bm = (int64_t)blockIdx.x * FBM, bn = (int64_t)blockIdx.y * FBN;
     const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
@@ -136,48 +141,58 @@ __global__ void __launch_bounds__(256) fold_gemm_kernel(const T *__restrict__ x,
         }
         return;
     }
-    Acc acc[4][4];
+    Acc acc[8][4];
 #pragma unroll
-    for (int i = 0; i < 4; i++)
+    for (int i = 0; i < 8; i++)
 #pragma unroll
         for (int j = 0; j < 4; j++) acc[i][j] = E::zero();
     const int64_t kdim = F.cin * F.km;
     const int km = (int)F.km, n1 = (int)A1.n;
     for (int64_t k0 = 0; k0 < kdim; k0 += FBK) {
+        if (tid < FBK) {
+            const int64_t kg = k0 + tid;
+            const int ci = (int)(kg / km), tm = (int)(kg - (int64_t)ci * km);
+            kpos[tid] = (F.tlo_m + tm) * Am.d;
+            koff[tid] = (kg < kdim) ? (int64_t)(ci / n1) * A0.xs + (int64_t)(ci % n1) * A1.xs : -1;
+        }
+        __syncthreads();
 #pragma unroll
-        for (int r = 0; r < 4; r++) {
+        for (int r = 0; r < FBM * FBK / 256; r++) {
             const int idx = tid + r * 256;
             const int kk = idx % FBK, row = idx / FBK;
-            const int64_t kg = k0 + kk, om = bm + row;
+            const int64_t om = bm + row;
             T v = E::zero();
-            if (kg < kdim && om < Am.out) {
-                const int ci = (int)(kg / km), tm = (int)(kg - (int64_t)ci * km);
-                const int64_t mi = fmap(Am, om, F.tlo_m + tm);
-                if (mi >= 0) v = x[mi * Am.xs + (ci / n1) * A0.xs + (ci % n1) * A1.xs];
+            if (koff[kk] >= 0 && om < Am.out) {
+                const int64_t mi = axis_map(Am, om * Am.s + kpos[kk]);
+                if (mi >= 0) v = x[mi * Am.xs + koff[kk]];
             }
             As[kk][row] = v;
-            const int col = idx / FBK;
-            const int64_t co = bn + col;
+        }
+#pragma unroll
+        for (int r = 0; r < FBN * FBK / 256; r++) {
+            const int idx = tid + r * 256;
+            const int kk = idx % FBK, col = idx / FBK;
+            const int64_t kg = k0 + kk, co = bn + col;
             Bs[kk][col] = (kg < kdim && co < F.cout) ? W[co * kdim + kg] : E::zero();
         }
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < FBK; kk++) {
-            T a[4], b[4];
+            T a[8], b[4];
 #pragma unroll
-            for (int i = 0; i < 4; i++) a[i] = As[kk][ty * 4 + i];
+            for (int i = 0; i < 8; i++) a[i] = As[kk][ty * 8 + i];
 #pragma unroll
             for (int j = 0; j < 4; j++) b[j] = Bs[kk][tx * 4 + j];
 #pragma unroll
-            for (int i = 0; i < 4; i++)
+            for (int i = 0; i < 8; i++)
 #pragma unroll
                 for (int j = 0; j < 4; j++) E::mac(acc[i][j], a[i], b[j]);
         }
         __syncthreads();
     }
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const int64_t om = bm + ty * 4 + i;
+    for (int i = 0; i < 8; i++) {
+        const int64_t om = bm + ty * 8 + i;
         if (om >= Am.out) continue;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
