@@ -114,13 +114,20 @@ template <typename C> int get_twiddles(int L, const C **out) {
 // Radix factorisation: 8s, 4, 2, 3s, 5s, then other primes (generic
 // butterfly up to kMaxGenericRadix).  Returns false if a prime factor is
 // larger than that.
+// Radices: 16s for the power of two (one radix-10 stage takes a factor 2
+// with a factor 5, then 8 / 4 / 2 for the rest), then odd factors.  Fewer,
+// wider stages mean fewer shared-memory round trips and barriers.
 bool make_plan(int L, FftPlanDev &pl) {
     pl.L = L;
     pl.nst = 0;
     int r = L;
-    while (r % 8 == 0) { pl.rad[pl.nst++] = 8; r /= 8; }
+    const bool ten = (r % 10 == 0) && (r % 4 != 0 || r % 32 == 0);
+    if (ten) r /= 10;
+    while (r % 16 == 0) { pl.rad[pl.nst++] = 16; r /= 16; }
+    if (r % 8 == 0) { pl.rad[pl.nst++] = 8; r /= 8; }
     if (r % 4 == 0) { pl.rad[pl.nst++] = 4; r /= 4; }
     if (r % 2 == 0) { pl.rad[pl.nst++] = 2; r /= 2; }
+    if (ten) pl.rad[pl.nst++] = 10;
     for (int f = 3; r > 1; f += 2) {
         while (r % f == 0) {
             if (f > kMaxGenericRadix || pl.nst >= kMaxStages) return false;
@@ -145,6 +152,8 @@ bool make_plan(int L, FftPlanDev &pl) {
 // one shared-memory round trip; larger radices do more arithmetic).
 static double stage_cost(int r) {
     switch (r) {
+    case 16: return 1.25;
+    case 10: return 1.2;
     case 8: return 1.0;
     case 4: return 0.75;
     case 2: return 0.6;
@@ -1234,11 +1243,19 @@ int conv_fft_wave(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, cons
 }
 
 // bytes of spectra a wave may keep so that they stay in L2 between passes
+// Spectra bytes one wave of a batch may hold.  Large waves win: the two
+// launches of a wave fill the GPU with many CTAs (short tails), and the
+// spectra that spill from L2 cost little next to the transforms (measured
+// on the 2-D case: 387 / 398 / 436 / 465 GB/s at 24 / 48 / 128 / 512 MB).
+// Capped by a quarter of the device memory free at first use.
 size_t wave_budget_bytes() {
     static size_t v = 0;
     if (!v) {
         const char *e = getenv("NDCONV_WAVE_MB");
-        v = (size_t)((e && atoi(e) > 0) ? atoi(e) : 48) << 20;
+        v = (size_t)((e && atoi(e) > 0) ? atoi(e) : 1024) << 20;
+        size_t fr = 0, tot = 0;
+        if (!(e && atoi(e) > 0) && cudaMemGetInfo(&fr, &tot) == cudaSuccess && fr / 4 < v) v = fr / 4;
+        if (v < ((size_t)16 << 20)) v = (size_t)16 << 20;
     }
     return v;
 }

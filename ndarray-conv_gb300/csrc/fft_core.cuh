@@ -175,6 +175,69 @@ template <bool INV, typename C> __device__ __forceinline__ void dft8(C *v) {
     v[7] = csub(e3, o3);
 }
 
+// radix 10 = 2 x 5: X[k] = E[k] + w10^k O[k], X[k + 5] = E[k] - w10^k O[k]
+// (E, O: 5-point transforms of the even and odd samples)
+template <bool INV, typename C> __device__ __forceinline__ void dft10(C *v) {
+    using R = decltype(v[0].re);
+    C e[5], o[5];
+#pragma unroll
+    for (int m = 0; m < 5; m++) {
+        e[m] = v[2 * m];
+        o[m] = v[2 * m + 1];
+    }
+    dft5<INV>(e);
+    dft5<INV>(o);
+    // w10^k = exp(-+ 2 pi i k / 10), k = 1..4
+    const R c1 = (R)0.80901699437494742410, s1 = (R)0.58778525229247312917;
+    const R c2 = (R)0.30901699437494742410, s2 = (R)0.95105651629515357212;
+    const R sg = INV ? (R)1 : (R)-1;
+    const C w[5] = {C{1, 0}, C{c1, sg * s1}, C{c2, sg * s2}, C{-c2, sg * s2}, C{-c1, sg * s1}};
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const C t = (k == 0) ? o[0] : cmul(o[k], w[k]);
+        v[k] = cadd(e[k], t);
+        v[k + 5] = csub(e[k], t);
+    }
+}
+
+// radix 16 = 4 x 4: four 4-point transforms over stride-4 samples, the
+// twiddles w16^(n2 k1), four 4-point transforms across them; X[k1 + 4 k2]
+template <bool INV, typename C> __device__ __forceinline__ void dft16(C *v) {
+    using R = decltype(v[0].re);
+    C y[4][4];
+#pragma unroll
+    for (int n2 = 0; n2 < 4; n2++) {
+        C a0 = v[n2], a1 = v[n2 + 4], a2 = v[n2 + 8], a3 = v[n2 + 12];
+        dft4<INV>(a0, a1, a2, a3);
+        y[n2][0] = a0;
+        y[n2][1] = a1;
+        y[n2][2] = a2;
+        y[n2][3] = a3;
+    }
+    // w16^m = exp(-+ 2 pi i m / 16) for the products m = n2 k1
+    const R c = (R)0.92387953251128675613, s = (R)0.38268343236508977173, h = (R)0.70710678118654752440;
+    const R sg = INV ? (R)1 : (R)-1;
+    const C w1 = C{c, sg * s}, w2 = C{h, sg * h}, w3 = C{s, sg * c}, w6 = C{-h, sg * h}, w9 = C{-c, -sg * s};
+    y[1][1] = cmul(y[1][1], w1);
+    y[1][2] = cmul(y[1][2], w2);
+    y[1][3] = cmul(y[1][3], w3);
+    y[2][1] = cmul(y[2][1], w2);
+    y[2][2] = mul_mi<INV>(y[2][2]);  // w16^4 = -+ i
+    y[2][3] = cmul(y[2][3], w6);
+    y[3][1] = cmul(y[3][1], w3);
+    y[3][2] = cmul(y[3][2], w6);
+    y[3][3] = cmul(y[3][3], w9);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; k1++) {
+        C a0 = y[0][k1], a1 = y[1][k1], a2 = y[2][k1], a3 = y[3][k1];
+        dft4<INV>(a0, a1, a2, a3);
+        v[k1] = a0;
+        v[k1 + 4] = a1;
+        v[k1 + 8] = a2;
+        v[k1 + 12] = a3;
+    }
+}
+
 template <bool INV, typename C>
 __device__ __forceinline__ C twiddle(const C *__restrict__ tw, int e) {
     C w = tw[e];
@@ -214,6 +277,8 @@ __device__ __forceinline__ void stockham_stage(const C *src, C *dst, int L, int 
         else if constexpr (RAD == 5) dft5<INV>(v);
         else if constexpr (RAD == 7) dft7<INV>(v);
         else if constexpr (RAD == 8) dft8<INV>(v);
+        else if constexpr (RAD == 10) dft10<INV>(v);
+        else if constexpr (RAD == 16) dft16<INV>(v);
         const int base = q * Ns * RAD + t;
 #pragma unroll
         for (int r = 0; r < RAD; r++) dst[sx<C>(((base + r * Ns) << lognb) + b)] = v[r];
@@ -264,6 +329,8 @@ __device__ C *block_fft(C *a, C *b, int nb, int lognb, const FftPlanDev &pl, con
         case 5: stockham_stage<INV, 5>(src, dst, pl.L, nb, lognb, pl.ns[s], tw); break;
         case 7: stockham_stage<INV, 7>(src, dst, pl.L, nb, lognb, pl.ns[s], tw); break;
         case 8: stockham_stage<INV, 8>(src, dst, pl.L, nb, lognb, pl.ns[s], tw); break;
+        case 10: stockham_stage<INV, 10>(src, dst, pl.L, nb, lognb, pl.ns[s], tw); break;
+        case 16: stockham_stage<INV, 16>(src, dst, pl.L, nb, lognb, pl.ns[s], tw); break;
         default: stockham_stage_generic<INV>(src, dst, pl.L, nb, lognb, pl.ns[s], R, tw); break;
         }
         __syncthreads();
