@@ -250,6 +250,7 @@ template <typename T> struct RowArgs {
     int mk0, mk1;            // INV_MAC: leading-axis taps
     int64_t mbase0, mbase1;  // INV_MAC: spectrum offset per output index (stride x row pitch)
     int64_t mstep0, mstep1;  // INV_MAC: spectrum offset per tap (dilation x row pitch)
+    int64_t mpitch;          // INV_MAC: row pitch of both spectra (even: bin pairs load as one vector)
 };
 
 // kernel-buffer value at padded position j of one axis: tap index or -1
@@ -473,10 +474,61 @@ __device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsi
             // (tz, ty) times data row (o0 s0 + tz d0, o1 s1 + ty d1); four bins
             // per thread at a time so that eight loads are in flight per tap
             const int mk0 = A.mk0, mk1 = A.mk1;
-            const int64_t st0 = A.mstep0, st1 = A.mstep1, Hh = A.H;
+            const int64_t st0 = A.mstep0, st1 = A.mstep1, Hh = A.mpitch;
             const bool l2 = A.l2only;
             const int T_ = blockDim.x;
-            for (int u0 = threadIdx.x; u0 < tot; u0 += 4 * T_) {
+            bool vec_done = false;
+            if constexpr (sizeof(C) == 8) {
+                if (nb == 1 && (Hh & 1) == 0) {
+                    // one row per CTA, even pitch: bins (2p, 2p + 1) as one 16-byte
+                    // load of each spectrum (half the requests in flight for the same bytes)
+                    const int npair = (H + 1) >> 1;
+                    const float4 *kv4 = reinterpret_cast<const float4 *>(kspec);
+                    const float4 *sv4 = reinterpret_cast<const float4 *>(spec + rit.soff);
+                    for (int p0 = threadIdx.x; p0 < npair; p0 += 4 * T_) {
+                        float4 acc[4];
+                        int pq[4];
+#pragma unroll
+                        for (int q = 0; q < 4; q++) {
+                            const int pp = p0 + q * T_;
+                            pq[q] = (pp < npair && rit.valid) ? pp : 0;
+                            acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+                        }
+                        auto taps = [&](auto load) {
+                            for (int tz = 0; tz < mk0; tz++) {
+                                for (int ty = 0; ty < mk1; ty++) {
+                                    const int64_t so = (tz * st0 + ty * st1) >> 1, ko = ((int64_t)(tz * mk1 + ty) * Hh) >> 1;
+                                    float4 kv[4], dv[4];
+#pragma unroll
+                                    for (int q = 0; q < 4; q++) {
+                                        kv[q] = load(kv4 + ko + pq[q]);
+                                        dv[q] = load(sv4 + so + pq[q]);
+                                    }
+#pragma unroll
+                                    for (int q = 0; q < 4; q++) {
+                                        acc[q].x = fmaf(kv[q].x, dv[q].x, fmaf(-kv[q].y, dv[q].y, acc[q].x));
+                                        acc[q].y = fmaf(kv[q].x, dv[q].y, fmaf(kv[q].y, dv[q].x, acc[q].y));
+                                        acc[q].z = fmaf(kv[q].z, dv[q].z, fmaf(-kv[q].w, dv[q].w, acc[q].z));
+                                        acc[q].w = fmaf(kv[q].z, dv[q].w, fmaf(kv[q].w, dv[q].z, acc[q].w));
+                                    }
+                                }
+                            }
+                        };
+                        if (l2) taps([](const float4 *p) { return __ldcg(p); });
+                        else taps([](const float4 *p) { return __ldg(p); });
+#pragma unroll
+                        for (int q = 0; q < 4; q++) {
+                            const int pp = p0 + q * T_;
+                            if (pp >= npair) continue;
+                            const bool v = rit.valid;
+                            dst[sx<C>(2 * pp)] = v ? C{acc[q].x, acc[q].y} : C{0, 0};
+                            if (2 * pp + 1 < H) dst[sx<C>(2 * pp + 1)] = v ? C{acc[q].z, acc[q].w} : C{0, 0};
+                        }
+                    }
+                    vec_done = true;
+                }
+            }
+            for (int u0 = threadIdx.x; !vec_done && u0 < tot; u0 += 4 * T_) {
                 C acc[4];
                 int64_t soff[4], koff[4];
                 bool ok[4];
@@ -977,8 +1029,9 @@ template <typename T> int make_conv_plan(const Geom3<T> &g, FftConvPlan<T> &cp, 
                          (variant == FFTV_AUTO && rs_preferred(g, cp));
     if (cp.astar < 2 && want_rs) {
         cp.rs = 1;
-        cp.nK = (size_t)g.ax[0].K * g.ax[1].K * cp.H;
-        cp.nS = (size_t)cp.P[0] * cp.P[1] * cp.H;
+        const int64_t Hp = (cp.H + 1) & ~(int64_t)1;  // even row pitch (bin pairs as one vector)
+        cp.nK = (size_t)g.ax[0].K * g.ax[1].K * Hp;
+        cp.nS = (size_t)cp.P[0] * cp.P[1] * Hp;
     }
     return NDCONV_OK;
 }
@@ -1004,6 +1057,7 @@ int conv_fft_passes(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, co
     int s;
 
     if (cp.rs) {
+        const int64_t Hp = (H + 1) & ~(int64_t)1;  // row pitch of both spectra
         // ---- row-spectral form: kernel rows Kh[K0][K1][H] (tap order) and
         // padded data rows S[P0][P1][H] in one pass, then per output row the
         // sum over leading taps, inverse, crop
@@ -1018,8 +1072,8 @@ int conv_fft_passes(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, co
         kr.n1 = A1.K;
         kr.n_rows = A0.K * A1.K;
         kr.spec = Kh;
-        kr.spec_s0 = A1.K * H;
-        kr.spec_s1 = H;
+        kr.spec_s0 = A1.K * Hp;
+        kr.spec_s1 = Hp;
         kr.spec_is = K_is;
         kr.scale = 1;
         RowArgs<T> dr = cp.rk;
@@ -1031,8 +1085,8 @@ int conv_fft_passes(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, co
         dr.n1 = P[1];
         dr.n_rows = P[0] * P[1];
         dr.spec = S;
-        dr.spec_s0 = P[1] * H;
-        dr.spec_s1 = H;
+        dr.spec_s0 = P[1] * Hp;
+        dr.spec_s1 = Hp;
         dr.spec_is = S_is;
         dr.scale = 1;
         if (which == PASSES_KERNEL) return emit_row(kr, cnt);
@@ -1048,10 +1102,11 @@ int conv_fft_passes(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, co
         ir.kspec_is = K_is;
         ir.mk0 = (int)A0.K;
         ir.mk1 = (int)A1.K;
-        ir.mbase0 = A0.s * P[1] * H;
-        ir.mbase1 = A1.s * H;
-        ir.mstep0 = A0.d * P[1] * H;
-        ir.mstep1 = A1.d * H;
+        ir.mbase0 = A0.s * P[1] * Hp;
+        ir.mbase1 = A1.s * Hp;
+        ir.mstep0 = A0.d * P[1] * Hp;
+        ir.mstep1 = A1.d * Hp;
+        ir.mpitch = Hp;
         ir.y = y;
         ir.ys = ys;
         ir.inst_base = base;
@@ -1368,8 +1423,8 @@ template <typename T> size_t conv_fft_scratch_bytes(const Geom3<T> &g, int varia
     const int astar = F[0] > 1 ? 0 : (F[1] > 1 ? 1 : 2);
     const size_t nK = (size_t)F[0] * F[1] * H;
     const size_t nS = (astar == 2) ? 0 : (size_t)P[0] * F[1] * H;
-    // the row-spectral form: kernel rows and padded data rows
-    const size_t rs = (astar == 2) ? 0 : (size_t)(g.ax[0].K * g.ax[1].K + P[0] * P[1]) * H;
+    // the row-spectral form: kernel rows and padded data rows (even row pitch)
+    const size_t rs = (astar == 2) ? 0 : (size_t)(g.ax[0].K * g.ax[1].K + P[0] * P[1]) * ((H + 1) & ~(int64_t)1);
     return sizeof(C) * std::max(nK + nS, rs) + 256;
 }
 

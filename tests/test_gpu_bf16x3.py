@@ -46,7 +46,7 @@ def test_bf16x3_vs_oracle(shape, kshape, dil, mode, pm):
 
 
 @pytest.mark.parametrize("cplx", [False])
-def test_bf16x3_config3(cplx):
+def test_bf16x3_3d_case(cplx):
     x, kw, mode, pm = _c3(cplx)
     y64 = _oracle64(x, kw, mode, pm)
     assert normwise_err(ndconv.conv_algo(x, kw, mode, pm, BF), y64) <= TOL32

@@ -243,7 +243,7 @@ def test_processor_vs_oracle(shape, dt):
     assert normwise_err(back, x) < tol
 
 
-# ---- BASELINE configs at full size ----------------------------------------------------------
+# ---- the three benchmark cases at full size ---------------------------------------------------
 def _c1():
     rng = np.random.default_rng(1)
     x = rng.random(5000).astype(np.float32)
@@ -286,7 +286,7 @@ def _oracle64(x, kw, mode, pm):
 
 @pytest.mark.parametrize("cfg", ["c1", "c2", "c3", "c3_complex"])
 @pytest.mark.parametrize("algo", ["direct", "fft"])
-def test_baseline_configs(cfg, algo):
+def test_benchmark_cases(cfg, algo):
     x, kw, mode, pm = {"c1": _c1, "c2": _c2, "c3": _c3, "c3_complex": lambda: _c3(True)}[cfg]()
     y64 = _oracle64(x, kw, mode, pm)
     f = ndconv.conv if algo == "direct" else ndconv.conv_fft
