@@ -160,7 +160,9 @@ int ndconv_conv_batch_host(const ndconv_problem *p, int32_t algo, int64_t n, con
  * f64.  Unit stride along the middle canonical axis only (else
  * NDCONV_ERR_UNSUPPORTED); non-finite inputs fall back to the FP32 loop so
  * NaN / Inf propagate as in the reference.  Same as
- * ndconv_conv_algo(p, NDCONV_ALGO_DIRECT_BF16X3, ...); synchronises stream. */
+ * ndconv_conv_algo(p, NDCONV_ALGO_DIRECT_BF16X3, ...).  Asynchronous on
+ * stream; a tensor-core pipeline wait that runs out (bounded at ~1 s, not
+ * expected) leaves NaN in the affected output tile. */
 int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, const void *kernel, void *out, void *stream);
 
 /* Batched ConvExt::conv / ConvFFTExt::conv_fft over n instances that share

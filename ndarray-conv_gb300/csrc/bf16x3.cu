@@ -16,7 +16,8 @@
 // the padded data (border map applied once, split into hi / lo) and the
 // Toeplitz bands.  One thread issues TMA, one issues tcgen05.mma, all four
 // warps drain TMEM with tcgen05.ld.  Every mbarrier wait is bounded; a
-// timeout sets bit 1 of the status word and the CTA still releases TMEM.
+// timeout (not expected) sets bit 1 of the status word, writes NaN to the
+// tile's outputs and the CTA still releases TMEM.
 // Non-finite inputs (bit 0, found by the pre-pass) make every CTA compute its
 // tile with the FP32 direct loop instead, like the reference's sums.
 #include <cuda.h>
@@ -36,13 +37,16 @@ namespace ndconv {
 namespace bf16x3 {
 
 constexpr int BM = 128;  // outputs along the contiguous axis per tile (TMEM lanes)
-constexpr int BN = 64;   // output rows per tile (TMEM columns)
 constexpr int KC = 64;   // bf16 per K chunk: one 128-byte swizzled row
-constexpr int STAGES = 4;
 constexpr int A_BYTES = BM * KC * 2;
-constexpr int B_BYTES = BN * KC * 2;
-constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+// BN output rows per tile (TMEM columns): 64, or 32 for problems whose
+// 64-row tiles would leave SMs idle
+template <int BN> struct Tile {
+    static constexpr int B_BYTES = BN * KC * 2;
+    static constexpr int STAGES = BN >= 64 ? 4 : 5;
+    static constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+};
 constexpr long long kWaitCycles = 2000000000LL;  // ~1 s of polling before a wait gives up
 constexpr int kThreads = 128;
 
@@ -187,10 +191,12 @@ __global__ void toeplitz_kernel(const float *__restrict__ k, Geom3<float> g, int
 }
 
 // ---- main kernel ----------------------------------------------------------
+template <int BN>
 __global__ void __launch_bounds__(kThreads, 1)
     conv_kernel(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant__ CUtensorMap tA_lo,
                 const __grid_constant__ CUtensorMap tB_hi, const __grid_constant__ CUtensorMap tB_lo,
                 const __grid_constant__ Params P) {
+    constexpr int STAGES = Tile<BN>::STAGES, STAGE_BYTES = Tile<BN>::STAGE_BYTES, B_BYTES = Tile<BN>::B_BYTES;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *base = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -283,7 +289,15 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (tid == 0 && !mbar_wait(done, 0)) atomicOr(bad, 1);
     __syncthreads();
     const bool good = (*reinterpret_cast<volatile int *>(bad) == 0);
-    if (!good && tid == 0) atomicOr(P.status, 2);
+    if (!good) {
+        // a pipeline wait ran out (not expected): the tile's outputs become NaN
+        // and the status word keeps the event
+        if (tid == 0) atomicOr(P.status, 2);
+        for (int u = tid; u < BM * BN; u += kThreads) {
+            const int64_t ox = (int64_t)q * BM + (u % BM), oy = oy0 + u / BM;
+            if (ox < P.out2 && oy < P.out1) P.y[oz * P.ys0 + oy * P.ys1 + ox] = __int_as_float(0x7fc00000);
+        }
+    }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (good) {
         const int m = warp * 32 + lane;  // TMEM lane = output along the contiguous axis
@@ -379,6 +393,9 @@ extern "C" int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, con
         cudaFreeAsync(ws, st);
         return code;
     };
+    // 64-row tiles, or 32 when 64 would give fewer than two CTAs per SM
+    const int64_t nseg = (A[2].out + BM - 1) / BM;
+    const int BN = (nseg * ((A[1].out + 63) / 64) * A[0].out < 2 * 152) ? 32 : 64;
     CUtensorMap mAh, mAl, mBh, mBl;
     {
         const cuuint64_t dA[2] = {(cuuint64_t)Cpad, (cuuint64_t)(L * BM)};
@@ -386,7 +403,7 @@ extern "C" int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, con
         const cuuint32_t bA[2] = {KC, BM};
         const cuuint64_t dB[3] = {(cuuint64_t)W, (cuuint64_t)A[1].L, (cuuint64_t)A[0].L};
         const cuuint64_t sB[2] = {(cuuint64_t)W * 2, (cuuint64_t)(W * A[1].L * 2)};
-        const cuuint32_t bB[3] = {KC, BN, 1};
+        const cuuint32_t bB[3] = {KC, (cuuint32_t)BN, 1};
         if ((s = make_map(&mAh, th, 2, dA, sA, bA)) || (s = make_map(&mAl, tl, 2, dA, sA, bA)) ||
             (s = make_map(&mBh, xh, 3, dB, sB, bB)) || (s = make_map(&mBl, xl, 3, dB, sB, bB)))
             return fail(s);
@@ -416,17 +433,16 @@ extern "C" int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, con
     Q.k = static_cast<const float *>(kernel);
     const int64_t gx = (int64_t)Q.nseg * ((A[1].out + BN - 1) / BN);
     if (gx > 0x7fffffff || A[0].out > 65535) return fail(ndconv_fail(NDCONV_ERR_UNSUPPORTED, "grid too large"));
-    cudaError_t e = ndconv_allow_smem((const void *)conv_kernel, SMEM_BYTES);
+    const void *fn = BN == 32 ? (const void *)conv_kernel<32> : (const void *)conv_kernel<64>;
+    const int smem = BN == 32 ? Tile<32>::SMEM_BYTES : Tile<64>::SMEM_BYTES;
+    cudaError_t e = ndconv_allow_smem(fn, smem);
     if (e != cudaSuccess) return fail(ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e)));
-    conv_kernel<<<dim3((unsigned)gx, (unsigned)A[0].out), kThreads, SMEM_BYTES, st>>>(mAh, mAl, mBh, mBl, Q);
+    const dim3 grid((unsigned)gx, (unsigned)A[0].out);
+    if (BN == 32) conv_kernel<32><<<grid, kThreads, smem, st>>>(mAh, mAl, mBh, mBl, Q);
+    else conv_kernel<64><<<grid, kThreads, smem, st>>>(mAh, mAl, mBh, mBl, Q);
     ndconv_count_launch();
     e = cudaGetLastError();
-    if (e != cudaSuccess) return fail(ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e)));
-    int hs = 0;
-    cudaMemcpyAsync(&hs, status, sizeof(int), cudaMemcpyDeviceToHost, st);
-    e = cudaStreamSynchronize(st);
-    cudaFreeAsync(ws, st);
+    cudaFreeAsync(ws, st);  // stream-ordered: after the launch has finished with it
     if (e != cudaSuccess) return ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e));
-    if (hs & 2) return ndconv_fail(NDCONV_ERR_TIMEOUT, "3xBF16 path: a pipeline wait ran out");
     return NDCONV_OK;
 }
