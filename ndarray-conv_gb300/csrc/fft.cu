@@ -1626,6 +1626,8 @@ int32_t ndconv_proc_dtype(const ndconv_fft_processor *p) { return p->dtype; }
 // A task only waits for tasks with smaller tickets, which running CTAs have
 // already claimed, so the queue always makes progress.
 #include "direct_blocks.cuh"
+#include "fold.h"
+#include "fold_blocks.cuh"
 #include "geometry.h"
 
 namespace ndconv {
@@ -1642,7 +1644,21 @@ enum TaskKind : int32_t {
     TK_ROW_FUSED = 13,
     TK_ROW_INV_MAC = 14,
     TK_COL = 20,
+    TK_FOLD_SCAN = 30,  // axis-folding form: non-finite scan, chunk bx
+    TK_FOLD_F1 = 31,    // first folded axis, chunk bx
+    TK_FOLD_F0 = 32,    // second folded axis, chunk bx
+    TK_FOLD_GEMM = 33,  // GEMM tile (bx, by)
 };
+
+// one instance of the axis-folding form inside the queue
+struct FoldTaskArgs {
+    FoldParams F;
+    const float *x, *k;
+    float *y, *W, *T1;
+    int flag;  // index of its non-finite flag among the queue counters
+    DirectParams<float> fb;
+};
+constexpr int64_t kFoldChunk = 256 * 8;  // elements per weight-folding / scan task
 
 struct Task {
     int32_t kind, arg;
@@ -1668,10 +1684,17 @@ __global__ void __launch_bounds__(256) batch_fixup_kernel(const DirectParams<flo
     dead_tap_fixup_block<float>(P.k1, P.y1, P, blockIdx.x, gridDim.x);
 }
 
+// a separate function so that the GEMM tile's registers do not raise the
+// other task kinds' register pressure
+__device__ __noinline__ void fold_gemm_task(const FoldTaskArgs *A, int bx, int by, int *ctrs, unsigned char *smem) {
+    foldk::gemm_tile<float>(A->x, A->W, A->y, A->F, ctrs + A->flag, A->k, A->fb, bx, by, smem, true);
+}
+
 __global__ void __launch_bounds__(256) persistent_kernel(const Task *__restrict__ tasks, int ntasks,
                                                          const RowArgs<float> *__restrict__ rargs,
                                                          const ColArgs<c32> *__restrict__ cargs,
                                                          const DirectParams<float> *__restrict__ dargs,
+                                                         const FoldTaskArgs *__restrict__ fargs,
                                                          int *ctrs, int *ticket, int *status) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_ticket;
@@ -1726,6 +1749,30 @@ __global__ void __launch_bounds__(256) persistent_kernel(const Task *__restrict_
             col_block<c32>(A, tk.bx, tk.by, A.n_outer, 0, smem_raw);
             break;
         }
+        case TK_FOLD_SCAN: {
+            const FoldTaskArgs &A = fargs[tk.arg];
+            const int64_t e = min((int64_t)(tk.bx + 1) * kFoldChunk, foldk::scan_count(A.F));
+            bool bad = false;
+            for (int64_t u = (int64_t)tk.bx * kFoldChunk + threadIdx.x; u < e; u += blockDim.x)
+                bad |= foldk::scan_elem<float>(A.x, A.k, A.F, u);
+            if (bad) atomicOr(ctrs + A.flag, 1);
+            break;
+        }
+        case TK_FOLD_F1: {
+            const FoldTaskArgs &A = fargs[tk.arg];
+            const int64_t e = min((int64_t)(tk.bx + 1) * kFoldChunk, foldk::f1_count<float>(A.F));
+            for (int64_t u = (int64_t)tk.bx * kFoldChunk + threadIdx.x; u < e; u += blockDim.x)
+                foldk::f1_elem<float>(A.k, A.F, A.T1, u);
+            break;
+        }
+        case TK_FOLD_F0: {
+            const FoldTaskArgs &A = fargs[tk.arg];
+            const int64_t e = min((int64_t)(tk.bx + 1) * kFoldChunk, foldk::f0_count<float>(A.F));
+            for (int64_t u = (int64_t)tk.bx * kFoldChunk + threadIdx.x; u < e; u += blockDim.x)
+                foldk::f0_elem<float>(A.T1, A.F, A.W, u, true);
+            break;
+        }
+        case TK_FOLD_GEMM: fold_gemm_task(fargs + tk.arg, tk.bx, tk.by, ctrs, smem_raw); break;
         default: break;
         }
         __threadfence();  // this CTA's results visible GPU-wide before the counter moves
@@ -1739,6 +1786,7 @@ struct HostInst {
     int algo;        // 0 direct, 1 FFT
     int fv;          // FFT plan variant (FftVariant)
     int standalone;  // runs as ordinary launches before the persistent kernel
+    int fold;        // f32 direct instance in the axis-folding form, inside the queue
     Plan3 P;
     const void *x, *k;
     void *y;
@@ -1758,13 +1806,14 @@ struct ndconv_batch_plan {
     std::vector<ndconv::RowArgs<float>> rargs;
     std::vector<ndconv::ColArgs<c32>> cargs;
     std::vector<ndconv::DirectParams<float>> dargs;
+    std::vector<ndconv::batch::FoldTaskArgs> fargs;
     std::vector<int> fix;  // direct instances with skipped taps (non-finite fix-up after the queue)
     void *d_fix = nullptr;
     int64_t graph_kernels = 0;
     int nctrs = 0;
     size_t smem = 0;
     int grid = 0;
-    void *d_tasks = nullptr, *d_rargs = nullptr, *d_cargs = nullptr, *d_dargs = nullptr;
+    void *d_tasks = nullptr, *d_rargs = nullptr, *d_cargs = nullptr, *d_dargs = nullptr, *d_fargs = nullptr;
     int *d_ctrs = nullptr;  // nctrs counters, then ticket, then status
     void *ws = nullptr;
     size_t ws_bytes = 0;
@@ -1899,6 +1948,7 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
         h.k = kernel[i];
         h.y = out[i];
         h.standalone = (h.P.dtype != NDCONV_F32);
+        h.fold = 0;
         h.ws_off = 0;
         h.ws_bytes = 0;
         if (h.algo == 1) {
@@ -1915,8 +1965,9 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
             else if (fs) return fail(fs);
         }
         if (h.algo == 0) {
-            // direct instances taken by the axis-folding form run as ordinary
-            // launches with their scratch in the plan's workspace
+            // direct instances taken by the axis-folding form keep their
+            // folded weights in the plan's workspace; f32 ones run as queue
+            // tasks, others as ordinary launches
             switch (h.P.dtype) {
             case NDCONV_F32: h.ws_bytes = direct_scratch_bytes<float>(h.P.direct<float>()); break;
             case NDCONV_F64: h.ws_bytes = direct_scratch_bytes<double>(h.P.direct<double>()); break;
@@ -1925,7 +1976,7 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
             default: h.ws_bytes = direct_scratch_bytes<c64>(h.P.direct<c64>()); break;
             }
             if (h.ws_bytes) {
-                h.standalone = 1;
+                h.fold = !h.standalone;
                 h.ws_off = ws;
                 ws += (h.ws_bytes + 255) / 256 * 256;
             }
@@ -2063,11 +2114,61 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
         max_levels = std::max(max_levels, (int)lv.size());
         B->n_fft++;
     }
+    // ---- axis-folding instances: scan and first folding (level 0), second
+    // folding (level 1), GEMM tiles (level 2)
+    for (int64_t i = 0; i < n; i++) {
+        HostInst &h = B->inst[(size_t)i];
+        if (!h.fold) continue;
+        DirectParams<float> full = h.P.direct<float>();
+        full.xs = nullptr;
+        full.ks = nullptr;
+        full.ys = nullptr;
+        full.x1 = static_cast<const float *>(h.x);
+        full.k1 = static_cast<const float *>(h.k);
+        full.y1 = static_cast<float *>(h.y);
+        DirectParams<float> D = full;
+        restrict_live_taps(D);
+        FoldTaskArgs fa;
+        if (!plan_fold(D, fa.F)) return fail(ndconv_fail(NDCONV_ERR_INVALID, "axis-folding plan changed"));
+        const FoldParams &F = fa.F;
+        fa.x = full.x1;
+        fa.k = full.k1;
+        fa.y = full.y1;
+        fa.W = reinterpret_cast<float *>(static_cast<unsigned char *>(B->ws) + h.ws_off);
+        fa.T1 = fa.W + F.cout * F.cin * F.km;
+        fa.flag = B->nctrs++;
+        fa.fb = full;
+        const int arg = (int)B->fargs.size();
+        B->fargs.push_back(fa);
+        std::vector<Level> &lv = per_inst[(size_t)i];
+        auto chunks = [](int64_t cnt) { return (cnt + kFoldChunk - 1) / kFoldChunk; };
+        lv.push_back(Level{i, B->nctrs++, {}});
+        for (int64_t b = 0; b < chunks(foldk::scan_count(F)); b++)
+            lv.back().tasks.push_back(Task{TK_FOLD_SCAN, arg, (int32_t)b, 0, 0, lv.back().ctr, -1, 0});
+        for (int64_t b = 0; b < chunks(foldk::f1_count<float>(F)); b++)
+            lv.back().tasks.push_back(Task{TK_FOLD_F1, arg, (int32_t)b, 0, 0, lv.back().ctr, -1, 0});
+        lv.push_back(Level{i, B->nctrs++, {}});
+        for (int64_t b = 0; b < chunks(foldk::f0_count<float>(F)); b++)
+            lv.back().tasks.push_back(Task{TK_FOLD_F0, arg, (int32_t)b, 0, 0, lv.back().ctr, -1, 0});
+        lv.push_back(Level{i, B->nctrs++, {}});
+        const int64_t gx = (F.ax[F.m].out + foldk::FBM - 1) / foldk::FBM, gy = (F.cout + foldk::FBN - 1) / foldk::FBN;
+        for (int64_t by = 0; by < gy; by++)
+            for (int64_t bx = 0; bx < gx; bx++)
+                lv.back().tasks.push_back(Task{TK_FOLD_GEMM, arg, (int32_t)bx, (int32_t)by, 0, lv.back().ctr, -1, 0});
+        for (size_t l = 1; l < lv.size(); l++)
+            for (Task &t : lv[l].tasks) {
+                t.wait_ctr = lv[l - 1].ctr;
+                t.wait_need = (int32_t)lv[l - 1].tasks.size();
+            }
+        max_levels = std::max(max_levels, (int)lv.size());
+        B->smem = std::max(B->smem, foldk::gemm_smem<float>());
+        B->n_direct++;
+    }
     // ---- direct tiles, largest instances first, with a work estimate per task
     std::vector<std::pair<double, int64_t>> order;
     for (int64_t i = 0; i < n; i++) {
         HostInst &h = B->inst[(size_t)i];
-        if (h.algo != 0 || h.standalone) continue;
+        if (h.algo != 0 || h.standalone || h.fold) continue;
         const AxisGeom *A = h.P.ax;
         const double work = (double)(A[0].out * A[1].out * A[2].out) * (double)(A[0].K * A[1].K * A[2].K);
         order.push_back({-work, i});
@@ -2114,7 +2215,7 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
     int s;
     if ((s = upload(B->tasks, &B->d_tasks)) || (s = upload(B->rargs, &B->d_rargs)) ||
         (s = upload(B->cargs, &B->d_cargs)) || (s = upload(B->dargs, &B->d_dargs)) ||
-        (s = upload(B->fix, &B->d_fix)))
+        (s = upload(B->fargs, &B->d_fargs)) || (s = upload(B->fix, &B->d_fix)))
         return fail(s);
     {
         cudaError_t e = cudaMalloc((void **)&B->d_ctrs, sizeof(int) * (size_t)(B->nctrs + 2));
@@ -2195,8 +2296,8 @@ int enqueue(ndconv_batch_plan *B, cudaStream_t st) {
     if (!B->tasks.empty()) {
         persistent_kernel<<<B->grid, 256, B->smem, st>>>(
             (const Task *)B->d_tasks, (int)B->tasks.size(), (const RowArgs<float> *)B->d_rargs,
-            (const ColArgs<c32> *)B->d_cargs, (const DirectParams<float> *)B->d_dargs, B->d_ctrs,
-            B->d_ctrs + B->nctrs, B->d_ctrs + B->nctrs + 1);
+            (const ColArgs<c32> *)B->d_cargs, (const DirectParams<float> *)B->d_dargs,
+            (const FoldTaskArgs *)B->d_fargs, B->d_ctrs, B->d_ctrs + B->nctrs, B->d_ctrs + B->nctrs + 1);
         ndconv_count_launch();
         NDCONV_CUDA_OK(cudaGetLastError());
     }
@@ -2320,6 +2421,7 @@ extern "C" int ndconv_batch_destroy(ndconv_batch_plan *B) {
     cudaFree(B->d_rargs);
     cudaFree(B->d_cargs);
     cudaFree(B->d_dargs);
+    cudaFree(B->d_fargs);
     cudaFree(B->d_fix);
     cudaFree(B->d_ctrs);
     cudaFree(B->ws);

@@ -100,3 +100,44 @@ def test_fold_in_batch_plan_equals_single():
         for i in range(len(shapes)):
             assert torch.equal(plan.outs[i], refs[i]), (graph, i)
     plan.close()
+
+
+def test_fold_in_batch_queue_mixed_and_nonfinite():
+    """Folded instances run as queue tasks beside FFT levels and direct tiles;
+    a non-finite input switches only its own instance to the tap-by-tap sums."""
+    import torch
+    from ndconv.batch import BatchPlan
+    g = torch.Generator(device="cuda").manual_seed(7)
+    shapes = [((300, 6, 5), (9, 21, 17)), ((100, 5, 4), (7, 15, 13)), ((100, 5, 4), (7, 15, 13)),
+              ((150, 4, 9), (11, 13, 25)), ((200, 700), (11, 31)), ((64, 300), (5, 9))]
+    algos = [0, 0, 0, 0, 1, 0]
+    xs = [torch.rand(s, generator=g, device="cuda") for s, _ in shapes]
+    ks = [torch.rand(k, generator=g, device="cuda") for _, k in shapes]
+    xs[1][40, 2, 1] = float("inf")
+    ks[2][3, 0, 12] = float("nan")
+    kws = [with_dilation(k, 1) for k in ks]
+    modes = [(_mode(k, 1, 1), PaddingMode.Reflect if i in (1, 2) else PaddingMode.Replicate)
+             for i, (_, k) in enumerate(shapes)]
+    plan = BatchPlan(modes, xs, kws, algos=algos)
+    assert plan.info()["n_standalone"] == 0
+    refs = [ndconv.conv_algo(xs[i], kws[i], *modes[i], algos[i]) for i in range(len(shapes))]
+    for graph in (False, True):
+        for y in plan.outs:
+            y.fill_(-1.0)
+        plan.run(graph=graph)
+        plan.check()
+        torch.cuda.synchronize()
+        for i in range(len(shapes)):
+            y, r = plan.outs[i].cpu().numpy(), refs[i].cpu().numpy()
+            assert np.array_equal(np.isnan(y), np.isnan(r)) and np.array_equal(np.isinf(y), np.isinf(r)), (graph, i)
+            if algos[i] == 0:
+                assert np.array_equal(y, r, equal_nan=True), (graph, i)
+            else:
+                assert normwise_err(y, r) <= TOL32, (graph, i)
+    for i in (1, 2):
+        x64 = xs[i].double().cpu().numpy()
+        k64 = ks[i].double().cpu().numpy()
+        st, y64 = O.conv(problem(F64, x64, kws[i], *modes[i]), x64, k64)
+        y = plan.outs[i].cpu().numpy()
+        assert np.array_equal(np.isnan(y), np.isnan(y64)) and np.array_equal(np.isinf(y), np.isinf(y64))
+    plan.close()
