@@ -251,6 +251,12 @@ template <typename T> struct RowArgs {
     int64_t mbase0, mbase1;  // INV_MAC: spectrum offset per output index (stride x row pitch)
     int64_t mstep0, mstep1;  // INV_MAC: spectrum offset per tap (dilation x row pitch)
     int64_t mpitch;          // INV_MAC: row pitch of both spectra (even: bin pairs load as one vector)
+    // overlap-save segments along the contiguous axis (seg_n <= 1: whole rows).
+    // Row r is (r / seg_n, segment r % seg_n); segment g transforms padded
+    // samples [g seg_len, g seg_len + F) and keeps the outputs whose padded
+    // position (crop_off + o crop_step) falls in [g seg_len + crop_off,
+    // (g + 1) seg_len + crop_off), where the circular sum has no wrap.
+    int64_t seg_n, seg_len, spec_sg;
 };
 
 // kernel-buffer value at padded position j of one axis: tap index or -1
@@ -286,6 +292,8 @@ struct RowInfo {
     int64_t yoff;    // output row offset
     int64_t m0, m1;  // data: border-mapped leading indices
     int64_t t0, t1;  // kernel: tap indices of the leading axes (-1: zero row)
+    int64_t j0;      // padded position of the segment's first sample
+    int o_lo, o_hi;  // outputs [o_lo, o_hi) of the row come from this segment
     int valid, interior;
 };
 
@@ -303,6 +311,7 @@ __device__ __forceinline__ T row_sample(const RowArgs<T> &A, const T *__restrict
     } else {
         // data (FWD_DATA / FUSED): zero beyond the padded extent
         const AxisGeom &a2 = A.g.ax[2];
+        j += ri.j0;
         if (ri.interior && j >= a2.p0 && j < a2.p0 + a2.n) return x[ri.xoff + (j - a2.p0) * a2.xs];
         if (j >= a2.L) return Elem<T>::zero();
         return resolve_padded<T>(x, A.g, ri.m0, ri.m1, axis_map(a2, j));
@@ -370,11 +379,23 @@ __device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsi
 
     for (int b = threadIdx.x; b < nb; b += blockDim.x) {
         const int64_t r = rbase + b;
-        const int64_t i0 = r / A.n1, i1 = r - (r / A.n1) * A.n1;
+        const int64_t sn = A.seg_n > 1 ? A.seg_n : 1;
+        const int64_t rr = r / sn, seg = r - rr * sn;
+        const int64_t i0 = rr / A.n1, i1 = rr - i0 * A.n1;
         RowInfo ri{};
         ri.valid = r < A.n_rows;
-        ri.soff = i0 * A.spec_s0 + i1 * A.spec_s1;
+        ri.soff = i0 * A.spec_s0 + i1 * A.spec_s1 + seg * A.spec_sg;
         ri.yoff = i0 * A.y_s0 + i1 * A.y_s1;
+        if (sn > 1) {
+            const int64_t cs = A.crop_step;
+            ri.j0 = seg * A.seg_len;
+            ri.o_lo = (int)((seg * A.seg_len + cs - 1) / cs);
+            ri.o_hi = (int)min(A.out_n, ((seg + 1) * A.seg_len + cs - 1) / cs);
+        } else {
+            ri.j0 = 0;
+            ri.o_lo = 0;
+            ri.o_hi = (int)A.out_n;
+        }
         if constexpr (MODE == ROW_FWD_DATA || MODE == ROW_FUSED) {
             ri.m0 = axis_map(A.g.ax[0], i0);
             ri.m1 = axis_map(A.g.ax[1], i1);
@@ -389,7 +410,7 @@ __device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsi
                 ri.t1 = kbuf_tap(A.g.ax[1], i1, A.reverse);
             }
         } else if constexpr (MODE == ROW_INV_MAC) {
-            ri.soff = i0 * A.mbase0 + i1 * A.mbase1;
+            ri.soff = i0 * A.mbase0 + i1 * A.mbase1 + seg * A.spec_sg;
         }
         rinfo[b] = ri;
     }
@@ -597,13 +618,17 @@ __device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsi
     }
     // ---- store time-domain samples (scaled; cropped + strided for INV_OUT / FUSED)
     constexpr bool plain = (MODE == ROW_INV_PLAIN);
-    const int n_out = (int)(plain ? A.F : A.out_n);
+    const bool segs = !plain && A.seg_n > 1;
+    // outputs per row (per segment: at most ceil(seg_len / crop_step))
+    const int n_out = (int)(plain ? A.F : segs ? (A.seg_len + A.crop_step - 1) / A.crop_step : A.out_n);
     const int tot = n_out << lognb;
-    const int coff = (int)A.crop_off, cstep = (int)A.crop_step;
+    const int coff = (int)(A.crop_off - rit.j0), cstep = (int)A.crop_step;
     if (!rit.valid) return;
     for (int u = threadIdx.x; u < tot; u += blockDim.x) {
-        const int b = bt, o = u >> lognb;
+        const int b = bt;
         const RowInfo &ri = rit;
+        const int o = plain ? (u >> lognb) : ri.o_lo + (u >> lognb);
+        if (!plain && o >= ri.o_hi) continue;
         const int p = plain ? o : (coff + o * cstep);
         R vr, vi;
         if (A.kind == RK_REAL_EVEN) {
@@ -974,34 +999,75 @@ template <typename T> struct FftConvPlan {
     int64_t P[3], F[3], H;
     int astar;
     int rs;  // row-spectral form: FFT along the contiguous axis only
+    int64_t seg_n, seg_len;  // overlap-save segments of the contiguous axis (seg_n 1: whole rows)
     RowArgs<T> rk;  // row plan (kind, pl, tw, twF, F, H)
     FftPlanDev pl0, pl1;
     const C *tw0, *tw1;
     size_t nK, nS;  // complex elements of Kh and S per instance
 };
 
-// Row-spectral form vs full N-d FFT, by a flop model (an FFT of length n
-// ~ 5 n log2 n flops, half for a real row; a spectral tap ~ 16 flop-equivalents
-// with its two loads; a spectrum byte through HBM ~ 4.4 flop-equivalents).
-// The row-spectral form skips the column transforms and their spectrum
-// round trips at the price of |K0 x K1| complex MACs per output bin.
+// Row-spectral form vs full N-d FFT.  The row-spectral form skips the
+// column transforms and their spectrum round trips (two launches instead of
+// up to six) at the price of |K0 x K1| complex MACs per output bin, whose
+// kernel spectra stop fitting in L2 as the leading kernel axes grow.  The
+// choice is a linear model of log2(t_rs / t_nd) in log2 sizes, least-squares
+// fitted to the measured times of both forms over 8,852 random f32 problems
+// (2-D and 3-D, kernels up to 127 per axis); its picks cost 1.7 % over the
+// faster form's total, where a flop model cost 2.7x.
 template <typename T> bool rs_preferred(const Geom3<T> &g, const FftConvPlan<T> &cp) {
     const AxisGeom &A0 = g.ax[0], &A1 = g.ax[1];
-    auto lg = [](double n) { return n > 1 ? std::log2(n) : 0.0; };
+    auto l = [](double v) { return v > 1 ? std::log2(v) : 0.0; };
+    const double z = -3.1795 + 0.6571 * l((double)A0.K * A1.K) - 0.0275 * l((double)A0.out * A1.out) +
+                     0.0556 * l((double)cp.H) - 0.5778 * l((double)cp.P[0] * cp.P[1]) +
+                     0.5565 * l((double)cp.F[0] * cp.F[1]) - 0.1077 * l((double)A0.keff * A1.keff);
+    return z < 0;
+}
+
+// A row pass holds a row of F samples in shared memory with one row per CTA?
+template <typename T> bool row_len_fits(int64_t F) {
+    using C = typename CplxT<typename Elem<T>::Real>::type;
+    const bool even_real = !Elem<T>::kComplex && F % 2 == 0;
+    const int64_t M = even_real ? F / 2 : F;
+    if (M >= (1 << 28)) return false;
+    const size_t bytes = ((sizeof(RowInfo) + 15) / 16) * 16 + sizeof(C) * 2 * padded_slots<C>(even_real ? M + 1 : M);
+    return bytes <= kFftSmemMax;
+}
+
+// Overlap-save segments for a contiguous axis too long for one row pass:
+// the transform length F (7-smooth, or a power of two) that minimises the
+// modelled cost of all segments, seg_len = F - keff + 1 new outputs per
+// segment.  False when even the longest row that fits holds no output
+// beyond the kernel's extent.
+template <typename T> bool seg_plan(const AxisGeom &a2, bool pow2, int64_t &F, int64_t &nseg, int64_t &len) {
     const bool real = !Elem<T>::kComplex;
-    const double F0 = (double)cp.F[0], F1 = (double)cp.F[1], F2 = (double)cp.F[2], H = (double)cp.H;
-    const double rowc = (real ? 2.5 : 5.0) * F2 * lg(F2);
-    const double common = rowc * ((double)cp.P[0] * cp.P[1] + (double)A0.out * A1.out);
-    const double taps = (double)A0.K * A1.K;
-    const double rs = common + rowc * taps + 16.0 * (double)A0.out * A1.out * H * taps;
-    double col = common + rowc * (double)A0.keff * A1.keff;
-    const double vol = F0 * F1 * H;
-    if (cp.F[1] > 1) col += 5.0 * F1 * lg(F1) * H * ((double)A0.keff + cp.P[0] + 2.0 * A0.out);
-    if (cp.F[0] > 1) col += 5.0 * F0 * lg(F0) * F1 * H * 3.0;
-    const double csz = (double)sizeof(typename FftConvPlan<T>::C);
-    const int passes = (cp.F[0] > 1 ? 2 : 0) + (cp.F[1] > 1 ? 2 : 0);
-    col += 4.4 * csz * vol * (2.0 * passes + 2.0);
-    return rs < col;
+    const int64_t need = (a2.out - 1) * a2.s + 1;  // padded positions from keff - 1 that outputs read
+    static const int odd[] = {1, 3, 5, 7, 9, 15, 21, 25, 27, 35, 45, 49, 63, 75, 81, 105};
+    double best = -1;
+    for (int c : odd) {
+        if (pow2 && c != 1) break;
+        for (int64_t f = (int64_t)c * 2; f <= (int64_t)1 << 26; f *= 2) {
+            if (f <= a2.keff) continue;
+            if (!row_len_fits<T>(f)) break;
+            FftPlanDev pl;
+            const int64_t L = real ? f / 2 : f;
+            if (!make_plan((int)L, pl)) continue;
+            double stages = 0;
+            for (int q = 0; q < pl.nst; q++) stages += stage_cost(pl.rad[q]);
+            const int64_t l = f - a2.keff + 1;
+            const int64_t n = (need + l - 1) / l;
+            // forward + inverse transform, plus loads, stores and the spectral product
+            double c_seg = 2.0 * (double)L * stages + 3.0 * (double)f;
+            if (f > 8192) c_seg *= 1.15;  // fewer CTAs resident per SM
+            const double cost = (double)n * c_seg;
+            if (best < 0 || cost < best) {
+                best = cost;
+                F = f;
+                nseg = n;
+                len = l;
+            }
+        }
+    }
+    return best >= 0;
 }
 
 template <typename T> int make_conv_plan(const Geom3<T> &g, FftConvPlan<T> &cp, int variant = FFTV_AUTO) {
@@ -1013,25 +1079,39 @@ template <typename T> int make_conv_plan(const Geom3<T> &g, FftConvPlan<T> &cp, 
         cp.F[a] = (cp.P[a] == 1) ? 1 : (pow2 ? pow2_size(cp.P[a], real && a == 2) : smooth_size(cp.P[a], real && a == 2));
     }
     cp.astar = cp.F[0] > 1 ? 0 : (cp.F[1] > 1 ? 1 : 2);
+    cp.seg_n = 1;
+    cp.seg_len = 0;
+    if (!row_len_fits<T>(cp.F[2])) {
+        // rows too long for one CTA: overlap-save segments, row-spectral form
+        if (variant == FFTV_ND || variant == FFTV_ND_POW2)
+            return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "FFT row length exceeds shared memory");
+        if (!seg_plan<T>(g.ax[2], pow2, cp.F[2], cp.seg_n, cp.seg_len))
+            return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "FFT kernel row too long for overlap-save segments");
+    }
     cp.rk = RowArgs<T>{};
     int s = row_plan<T>(cp.F[2], real, cp.rk);
     if (s) return s;
     cp.H = cp.rk.H;
-    cp.pl0 = FftPlanDev{};
-    cp.pl1 = FftPlanDev{};
-    cp.tw0 = cp.tw1 = nullptr;
-    if (cp.F[0] > 1 && (s = plan_with_tw<C>(cp.F[0], cp.pl0, &cp.tw0))) return s;
-    if (cp.F[1] > 1 && (s = plan_with_tw<C>(cp.F[1], cp.pl1, &cp.tw1))) return s;
     cp.nK = (size_t)cp.F[0] * cp.F[1] * cp.H;
     cp.nS = (cp.astar == 2) ? 0 : (size_t)cp.P[0] * cp.F[1] * cp.H;
     cp.rs = 0;
-    const bool want_rs = (variant == FFTV_RS || variant == FFTV_RS_POW2) ||
+    // (leading axes too long for one column pass: the N-d form reports it and
+    // conv_fft runs the direct kernels, which skip the taps that read only
+    // padding; the row-spectral form would sum every one of them per bin)
+    const bool want_rs = (variant == FFTV_RS || variant == FFTV_RS_POW2) || cp.seg_n > 1 ||
                          (variant == FFTV_AUTO && rs_preferred(g, cp));
     if (cp.astar < 2 && want_rs) {
         cp.rs = 1;
         const int64_t Hp = (cp.H + 1) & ~(int64_t)1;  // even row pitch (bin pairs as one vector)
         cp.nK = (size_t)g.ax[0].K * g.ax[1].K * Hp;
-        cp.nS = (size_t)cp.P[0] * cp.P[1] * Hp;
+        cp.nS = (size_t)cp.P[0] * cp.P[1] * cp.seg_n * Hp;
+    }
+    cp.pl0 = FftPlanDev{};
+    cp.pl1 = FftPlanDev{};
+    cp.tw0 = cp.tw1 = nullptr;
+    if (!cp.rs) {
+        if (cp.F[0] > 1 && (s = plan_with_tw<C>(cp.F[0], cp.pl0, &cp.tw0))) return s;
+        if (cp.F[1] > 1 && (s = plan_with_tw<C>(cp.F[1], cp.pl1, &cp.tw1))) return s;
     }
     return NDCONV_OK;
 }
@@ -1076,6 +1156,8 @@ int conv_fft_passes(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, co
         kr.spec_s1 = Hp;
         kr.spec_is = K_is;
         kr.scale = 1;
+        // data spectra S[P0][P1][segment][H] (one segment unless the rows are long)
+        const int64_t sn = cp.seg_n, Hs = sn * Hp;
         RowArgs<T> dr = cp.rk;
         dr.mode = ROW_FWD_DATA;
         dr.g = g;
@@ -1083,10 +1165,13 @@ int conv_fft_passes(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, co
         dr.xs = xs;
         dr.inst_base = base;
         dr.n1 = P[1];
-        dr.n_rows = P[0] * P[1];
+        dr.n_rows = P[0] * P[1] * sn;
+        dr.seg_n = sn;
+        dr.seg_len = cp.seg_len;
         dr.spec = S;
-        dr.spec_s0 = P[1] * Hp;
-        dr.spec_s1 = Hp;
+        dr.spec_s0 = P[1] * Hs;
+        dr.spec_s1 = Hs;
+        dr.spec_sg = Hp;
         dr.spec_is = S_is;
         dr.scale = 1;
         if (which == PASSES_KERNEL) return emit_row(kr, cnt);
@@ -1095,17 +1180,20 @@ int conv_fft_passes(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, co
         ir.mode = ROW_INV_MAC;
         ir.g = g;
         ir.n1 = A1.out;
-        ir.n_rows = A0.out * A1.out;
+        ir.n_rows = A0.out * A1.out * sn;
+        ir.seg_n = sn;
+        ir.seg_len = cp.seg_len;
+        ir.spec_sg = Hp;
         ir.spec = S;
         ir.spec_is = S_is;
         ir.kspec = Kh;
         ir.kspec_is = K_is;
         ir.mk0 = (int)A0.K;
         ir.mk1 = (int)A1.K;
-        ir.mbase0 = A0.s * P[1] * Hp;
-        ir.mbase1 = A1.s * Hp;
-        ir.mstep0 = A0.d * P[1] * Hp;
-        ir.mstep1 = A1.d * Hp;
+        ir.mbase0 = A0.s * P[1] * Hs;
+        ir.mbase1 = A1.s * Hs;
+        ir.mstep0 = A0.d * P[1] * Hs;
+        ir.mstep1 = A1.d * Hs;
         ir.mpitch = Hp;
         ir.y = y;
         ir.ys = ys;
@@ -1175,7 +1263,9 @@ int conv_fft_passes(const Geom3<T> &g, int reverse, const FftConvPlan<T> &cp, co
         fr.ys = ys;
         fr.inst_base = base;
         fr.n1 = 1;
-        fr.n_rows = 1;
+        fr.n_rows = cp.seg_n;
+        fr.seg_n = cp.seg_n;
+        fr.seg_len = cp.seg_len;
         fr.kspec = Kh;
         fr.kspec_is = K_is;
         fr.y_s0 = 0;
@@ -1419,13 +1509,17 @@ template <typename T> size_t conv_fft_scratch_bytes(const Geom3<T> &g, int varia
     int64_t P[3] = {g.ax[0].L, g.ax[1].L, g.ax[2].L}, F[3];
     for (int a = 0; a < 3; a++)
         F[a] = (P[a] == 1) ? 1 : (pow2 ? pow2_size(P[a], real && a == 2) : smooth_size(P[a], real && a == 2));
-    const int64_t H = real ? F[2] / 2 + 1 : F[2];
     const int astar = F[0] > 1 ? 0 : (F[1] > 1 ? 1 : 2);
+    int64_t sn = 1, sl = 0;
+    if (!row_len_fits<T>(F[2])) {
+        if (!seg_plan<T>(g.ax[2], pow2, F[2], sn, sl)) return 256;  // unsupported: the plan reports it
+    }
+    const int64_t H = real ? F[2] / 2 + 1 : F[2];
     const size_t nK = (size_t)F[0] * F[1] * H;
     const size_t nS = (astar == 2) ? 0 : (size_t)P[0] * F[1] * H;
-    // the row-spectral form: kernel rows and padded data rows (even row pitch)
-    const size_t rs = (astar == 2) ? 0 : (size_t)(g.ax[0].K * g.ax[1].K + P[0] * P[1]) * ((H + 1) & ~(int64_t)1);
-    return sizeof(C) * std::max(nK + nS, rs) + 256;
+    // the row-spectral form: kernel rows and padded data rows (segments) (even row pitch)
+    const size_t rs = (astar == 2) ? 0 : (size_t)(g.ax[0].K * g.ax[1].K + P[0] * P[1] * sn) * ((H + 1) & ~(int64_t)1);
+    return sizeof(C) * std::max(sn > 1 ? nK : nK + nS, rs) + 256;
 }
 
 #define NDCONV_INST_FFT(T)                                                                          \
@@ -2478,17 +2572,38 @@ extern "C" int ndconv_plan_info(const ndconv_problem *p, double out[8]) {
     out[6] = (double)F[2];
     const int csz = (P.dtype == NDCONV_F64 || P.dtype == NDCONV_C64) ? 16 : 8;
     const double budget = 100.0 * 1024;  // persistent kernel share
-    bool fits = true;
-    const int64_t M = real ? F[2] / 2 : F[2];
-    if ((double)csz * 2 * (M + 1) * 1.07 > budget) fits = false;
-    for (int a = 0; a < 2; a++)
-        if (F[a] > 1 && (double)csz * 2 * F[a] * 1.07 > budget) fits = false;
-    if (P.dtype == NDCONV_I32) fits = false;
-    if (!fits) {
+    if (P.dtype == NDCONV_I32) {
         out[1] = 1e30;
         out[7] = 0;
         return NDCONV_OK;
     }
+    // rows too long for one CTA: overlap-save segments of the row-spectral form
+    int64_t sn = 1, sl = 0;
+    int64_t M = real ? F[2] / 2 : F[2];
+    bool rs = false;
+    if ((double)csz * 2 * (M + 1) * 1.07 > budget) {
+        bool ok = false;
+        switch (P.dtype) {
+        case NDCONV_F32: ok = seg_plan<float>(A[2], false, F[2], sn, sl); break;
+        case NDCONV_F64: ok = seg_plan<double>(A[2], false, F[2], sn, sl); break;
+        case NDCONV_C32: ok = seg_plan<c32>(A[2], false, F[2], sn, sl); break;
+        default: ok = seg_plan<c64>(A[2], false, F[2], sn, sl); break;
+        }
+        if (!ok) {
+            out[1] = 1e30;
+            out[7] = 0;
+            return NDCONV_OK;
+        }
+        out[6] = (double)F[2];
+        M = real ? F[2] / 2 : F[2];
+        rs = true;
+    }
+    for (int a = 0; a < 2; a++)
+        if (!rs && F[a] > 1 && (double)csz * 2 * F[a] * 1.07 > budget) {
+            out[1] = 1e30;  // columns too long for the N-d form: conv_fft runs the direct kernels
+            out[7] = 0;
+            return NDCONV_OK;
+        }
     auto stages = [](int64_t L) {
         FftPlanDev pl;
         if (L <= 1 || !make_plan((int)L, pl)) return 0.0;
@@ -2497,11 +2612,23 @@ extern "C" int ndconv_plan_info(const ndconv_problem *p, double out[8]) {
         return c;
     };
     const double H = real ? (double)(F[2] / 2 + 1) : (double)F[2];
+    const double dram_base = bytes;
+    if (rs && (A[0].L > 1 || A[1].L > 1 || sn > 1)) {
+        // row transforms (data rows and segments, kernel rows, output rows)
+        // plus the spectral tap sums through L2
+        const double rows = (double)A[0].L * A[1].L * sn + (double)A[0].K * A[1].K + (double)A[0].out * A[1].out * sn;
+        const double smem_bytes = rows * H * (stages(M) + 1) * 16.0;
+        const double mac_bytes = (double)A[0].out * A[1].out * sn * H * (double)(A[0].K * A[1].K) * 2.0 * csz;
+        const double dram = dram_base + 2.0 * (double)A[0].L * A[1].L * sn * H * csz;
+        out[1] = smem_bytes / 40e12 + mac_bytes / 20e12 + dram / 6.8e12 + 12e-6;
+        out[7] = 1;
+        return NDCONV_OK;
+    }
     const double vol = (double)F[0] * F[1] * H;  // spectrum elements
     // kernel + data forward, inverse: ~3 transforms, each stage a smem round trip (16 B/elem)
     const double st = stages(M) + stages(F[1]) + stages(F[0]) + 1;
     const double smem_bytes = 3.0 * vol * st * 16.0;
-    const double dram = bytes + 4.0 * vol * csz;
+    const double dram = dram_base + 4.0 * vol * csz;
     out[1] = smem_bytes / 40e12 + dram / 6.8e12 + 12e-6;
     out[7] = 1;
     return NDCONV_OK;
