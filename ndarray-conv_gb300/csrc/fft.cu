@@ -622,11 +622,13 @@ __device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsi
     // outputs per row (per segment: at most ceil(seg_len / crop_step))
     const int n_out = (int)(plain ? A.F : segs ? (A.seg_len + A.crop_step - 1) / A.crop_step : A.out_n);
     const int tot = n_out << lognb;
-    const int coff = (int)(A.crop_off - rit.j0), cstep = (int)A.crop_step;
-    if (!rit.valid) return;
+    // the row's output facts are read back from shared memory here rather
+    // than kept in registers through the transforms and the tap sums
+    const RowInfo &ri = rinfo[bt];
+    const int coff = (int)(A.crop_off - ri.j0), cstep = (int)A.crop_step;
+    if (!ri.valid) return;
     for (int u = threadIdx.x; u < tot; u += blockDim.x) {
         const int b = bt;
-        const RowInfo &ri = rit;
         const int o = plain ? (u >> lognb) : ri.o_lo + (u >> lognb);
         if (!plain && o >= ri.o_hi) continue;
         const int p = plain ? o : (coff + o * cstep);
@@ -647,7 +649,7 @@ __device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsi
 }
 
 template <typename T, int MODE>
-__global__ void __launch_bounds__(512) row_kernel(const __grid_constant__ RowArgs<T> A) {
+__global__ void __launch_bounds__(512, 2) row_kernel(const __grid_constant__ RowArgs<T> A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     row_block<T, MODE>(A, blockIdx.x, blockIdx.y, smem_raw);
 }
@@ -850,7 +852,7 @@ template <typename T> int launch_row(RowArgs<T> A, cudaStream_t st, int n_inst =
 // Two independent forward row passes in one launch (the kernel rows and the
 // data rows of the row-spectral form): CTAs [0, ga) take pass A, the rest B.
 template <typename T>
-__global__ void __launch_bounds__(512) row_pair_kernel(const __grid_constant__ RowArgs<T> A,
+__global__ void __launch_bounds__(512, 2) row_pair_kernel(const __grid_constant__ RowArgs<T> A,
                                                             const __grid_constant__ RowArgs<T> B, unsigned ga) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     if (blockIdx.x < ga) row_block<T, ROW_FWD_KERNEL>(A, blockIdx.x, blockIdx.y, smem_raw);
