@@ -2545,11 +2545,19 @@ extern "C" int ndconv_plan_info(const ndconv_problem *p, double out[8]) {
     const double nx = (double)(A[0].n * A[1].n * A[2].n);
     double taps = (double)(A[0].K * A[1].K * A[2].K);
     double sw_slots = -1;  // issue slots of the sliding-window kernel, if it applies
+    double fold_macs = -1, fold_prep = 0;  // the axis-folding form's GEMM and weight folding, if it applies
     {
         // the direct kernels only loop over taps that can see data
         DirectParams<float> D = P.direct<float>();
         restrict_live_taps(D);
         taps = (double)(D.t_n[0] * D.t_n[1] * D.t_n[2]);
+        FoldParams F;
+        if (plan_fold(D, F)) {
+            const AxisGeom *FA = F.ax;
+            fold_macs = (double)FA[F.m].out * (double)F.cout * (double)F.cin * (double)F.km;
+            fold_prep = (double)F.km * FA[F.f0].K * FA[F.f1].out * FA[F.f1].n * FA[F.f1].K +
+                        (double)F.cout * F.cin * F.km * FA[F.f0].K;
+        }
         permute_axes_for_tiles(D);
         if (plan_sw(D, 8)) sw_slots = sw_cost(D, 8, 16);
     }
@@ -2564,6 +2572,13 @@ extern "C" int ndconv_plan_info(const ndconv_problem *p, double out[8]) {
                                          : 3.0 * macs / 40e12;
     out[0] = t_fma + bytes / 6.8e12 + 4e-6;
     out[2] = macs;
+    if (fold_macs >= 0) {
+        // the direct entry point takes the axis-folding form: a gathered
+        // CUDA-core GEMM (~10 T multiply-adds/s) after the weight folding
+        const double cm = (P.dtype == NDCONV_C32 || P.dtype == NDCONV_C64) ? 4 : 1;
+        out[0] = cm * fold_macs / 10e12 + fold_prep / 2e12 + bytes / 6.8e12 + 10e-6;
+        out[2] = cm * fold_macs;
+    }
     out[3] = bytes;
     // FFT: sizes, shared-memory fit, smem-traffic model
     const bool real = !(P.dtype == NDCONV_C32 || P.dtype == NDCONV_C64);
