@@ -648,8 +648,12 @@ __device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsi
     }
 }
 
-template <typename T, int MODE>
-__global__ void __launch_bounds__(512, 2) row_kernel(const __grid_constant__ RowArgs<T> A) {
+// MAXT 512 caps registers at 64 (4 CTAs of 256 threads per SM: launches of
+// many CTAs, throughput-bound); MAXT 384 allows 85, so that a launch of few
+// CTAs (latency-bound, at most two per SM) keeps more values in registers
+// instead of spilling.
+template <typename T, int MODE, int MAXT>
+__global__ void __launch_bounds__(MAXT, 2) row_kernel(const __grid_constant__ RowArgs<T> A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     row_block<T, MODE>(A, blockIdx.x, blockIdx.y, smem_raw);
 }
@@ -765,6 +769,8 @@ __global__ void transpose_kernel(const C *__restrict__ in, C *__restrict__ out, 
 namespace {
 constexpr int kThreads = 256;
 constexpr size_t kFftSmemMax = 200 * 1024;
+constexpr int64_t kFewCtas = 4 * 152;  // launches up to this many CTAs are latency-bound
+constexpr int kFewThreads = 384;        // their widest CTA
 
 int ilog2(int v) {
     int l = 0;
@@ -794,23 +800,36 @@ int pick_nb(int64_t len, int64_t rows, size_t per_row_bytes) {
 }
 
 // Threads per row-pass CTA.  A launch of few CTAs is latency-bound: one
-// radix-8 (or the widest) butterfly per thread in a single round where that
-// fits 128..512 threads (e.g. 320 for a 2560-point transform).  A launch of
-// many CTAs is throughput-bound: 256, which keeps more CTAs resident.
+// butterfly of the stage with the most butterflies per thread in a single
+// round where that fits 128..384 threads (e.g. 256 for a 2560-point
+// transform of radices 16, 16, 10).  A launch of many CTAs is
+// throughput-bound: 256, which keeps more CTAs resident.
 template <typename T> int row_threads(const RowArgs<T> &A, int64_t ctas) {
-    if (ctas > 4 * 152) return kThreads;
+    if (ctas > kFewCtas) return kThreads;
     int maxw = 0;
     for (int i = 0; i < A.pl.nst; i++) maxw = std::max(maxw, (A.pl.L / A.pl.rad[i]) << A.lognb);
-    if (maxw < 128 || maxw > 512) return kThreads;
+    if (maxw < 128 || maxw > kFewThreads) return kThreads;
     return (maxw + 31) / 32 * 32;
 }
 
 // n_inst instances (grid.y); A.spec_is etc. describe their spacing
 template <typename T, int MODE> int launch_row_mode(const RowArgs<T> &A, size_t sm, unsigned grid, int n_inst,
                                                     cudaStream_t st) {
-    int st_ = ensure_smem(row_kernel<T, MODE>);
+    const int64_t ctas = (int64_t)grid * n_inst;
+    const int threads = row_threads(A, ctas);
+    if constexpr (std::is_same<T, float>::value) {
+        if (ctas <= kFewCtas) {
+            int st1 = ensure_smem(row_kernel<T, MODE, kFewThreads>);
+            if (st1) return st1;
+            row_kernel<T, MODE, kFewThreads><<<dim3(grid, (unsigned)n_inst), threads, sm, st>>>(A);
+            ndconv_count_launch();
+            NDCONV_CUDA_OK(cudaGetLastError());
+            return NDCONV_OK;
+        }
+    }
+    int st_ = ensure_smem(row_kernel<T, MODE, 512>);
     if (st_) return st_;
-    row_kernel<T, MODE><<<dim3(grid, (unsigned)n_inst), row_threads(A, (int64_t)grid * n_inst), sm, st>>>(A);
+    row_kernel<T, MODE, 512><<<dim3(grid, (unsigned)n_inst), threads, sm, st>>>(A);
     ndconv_count_launch();
     NDCONV_CUDA_OK(cudaGetLastError());
     return NDCONV_OK;
@@ -851,8 +870,8 @@ template <typename T> int launch_row(RowArgs<T> A, cudaStream_t st, int n_inst =
 
 // Two independent forward row passes in one launch (the kernel rows and the
 // data rows of the row-spectral form): CTAs [0, ga) take pass A, the rest B.
-template <typename T>
-__global__ void __launch_bounds__(512, 2) row_pair_kernel(const __grid_constant__ RowArgs<T> A,
+template <typename T, int MAXT>
+__global__ void __launch_bounds__(MAXT, 2) row_pair_kernel(const __grid_constant__ RowArgs<T> A,
                                                             const __grid_constant__ RowArgs<T> B, unsigned ga) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     if (blockIdx.x < ga) row_block<T, ROW_FWD_KERNEL>(A, blockIdx.x, blockIdx.y, smem_raw);
@@ -869,11 +888,21 @@ template <typename T> int launch_row_pair(RowArgs<T> A, RowArgs<T> B, cudaStream
     if (s) return s;
     if ((s = prep_row(B, n_inst, gb, sb))) return s;
     if (ga + gb > 0x7fffffff) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "too many FFT rows");
-    if ((s = ensure_smem(row_pair_kernel<T>))) return s;
     const int64_t ctas = (ga + gb) * n_inst;
-    row_pair_kernel<T><<<dim3((unsigned)(ga + gb), (unsigned)n_inst),
-                         std::max(row_threads(A, ctas), row_threads(B, ctas)), std::max(sa, sb), st>>>(
-        A, B, (unsigned)ga);
+    const int threads = std::max(row_threads(A, ctas), row_threads(B, ctas));
+    const dim3 grid((unsigned)(ga + gb), (unsigned)n_inst);
+    bool done = false;
+    if constexpr (std::is_same<T, float>::value) {
+        if (ctas <= kFewCtas) {
+            if ((s = ensure_smem(row_pair_kernel<T, kFewThreads>))) return s;
+            row_pair_kernel<T, kFewThreads><<<grid, threads, std::max(sa, sb), st>>>(A, B, (unsigned)ga);
+            done = true;
+        }
+    }
+    if (!done) {
+        if ((s = ensure_smem(row_pair_kernel<T, 512>))) return s;
+        row_pair_kernel<T, 512><<<grid, threads, std::max(sa, sb), st>>>(A, B, (unsigned)ga);
+    }
     ndconv_count_launch();
     NDCONV_CUDA_OK(cudaGetLastError());
     return NDCONV_OK;
