@@ -1,11 +1,12 @@
 // Batched convolution of instances held in host memory: the library stages
 // chunks of instances through its own device buffers so that host->device
 // copies, the convolution and device->host copies of successive chunks
-// overlap (three streams, double-buffered slots).  No reference counterpart:
-// the crate works on host arrays one call at a time.
+// overlap (three streams, a ring of slots).  No reference counterpart: the
+// crate works on host arrays one call at a time.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <vector>
 
 #include "common.cuh"
@@ -64,30 +65,41 @@ extern "C" int ndconv_conv_batch_host(const ndconv_problem *p, int32_t algo, int
     const size_t bx = es * (size_t)(A[0].n * A[1].n * A[2].n), bk = es * (size_t)(A[0].K * A[1].K * A[2].K);
     const size_t by = es * (size_t)(A[0].out * A[1].out * A[2].out);
     const size_t per = (bx + bk + by + 255) / 256 * 256 + 256;
-    // chunks of ~32 MB of inputs and outputs (at least one instance), two slots
-    int64_t C = (int64_t)((32u << 20) / (bx + by + 1));
+    // chunks of ~chunk_mb MB of inputs and outputs (at least one instance) in
+    // a ring of NS slots: both copy directions stream concurrently (the link
+    // carries ~210 GB/s one way, ~340 GB/s both ways on a GB300), and a ring
+    // deeper than two keeps a chunk's output copy from holding up the next
+    // convolution.  NDCONV_HOST_CHUNK_MB / NDCONV_HOST_SLOTS override.
+    size_t chunk_mb = 16;
+    int NS = 3;
+    if (const char *v = std::getenv("NDCONV_HOST_CHUNK_MB")) chunk_mb = std::max<long>(1, std::atol(v));
+    if (const char *v = std::getenv("NDCONV_HOST_SLOTS")) NS = (int)std::min<long>(8, std::max<long>(2, std::atol(v)));
+    int64_t C = (int64_t)((chunk_mb << 20) / (bx + by + 1));
     C = std::max<int64_t>(1, std::min<int64_t>(C, n));
+    const int64_t n_chunks = (n + C - 1) / C;
+    if (n_chunks < NS) NS = (int)std::max<int64_t>(1, n_chunks);
     cudaStream_t st = (cudaStream_t)stream;
     unsigned char *buf = nullptr;
-    NDCONV_CUDA_OK(cudaMallocAsync((void **)&buf, 2 * (size_t)C * per + 2 * 3 * sizeof(void *) * (size_t)C, st));
-    // device pointer arrays of both slots, written once
-    std::vector<void *> ptrs((size_t)(2 * 3 * C));
-    for (int slot = 0; slot < 2; slot++)
+    NDCONV_CUDA_OK(cudaMallocAsync((void **)&buf, NS * (size_t)C * per + NS * 3 * sizeof(void *) * (size_t)C, st));
+    // device pointer arrays of all slots, written once
+    std::vector<void *> ptrs((size_t)(NS * 3 * C));
+    for (int slot = 0; slot < NS; slot++)
         for (int64_t i = 0; i < C; i++) {
             unsigned char *b = buf + ((size_t)slot * C + i) * per;
             ptrs[(size_t)((slot * 3 + 0) * C + i)] = b;
             ptrs[(size_t)((slot * 3 + 1) * C + i)] = b + (bx + 255) / 256 * 256;
             ptrs[(size_t)((slot * 3 + 2) * C + i)] = b + (bx + 255) / 256 * 256 + (bk + 255) / 256 * 256;
         }
-    void **dptr = reinterpret_cast<void **>(buf + 2 * (size_t)C * per);
+    void **dptr = reinterpret_cast<void **>(buf + NS * (size_t)C * per);
     cudaError_t e = cudaMemcpyAsync(dptr, ptrs.data(), sizeof(void *) * ptrs.size(), cudaMemcpyHostToDevice, st);
     cudaStream_t sin = nullptr, sout = nullptr;
-    cudaEvent_t ev[2][3];  // per slot: inputs landed, convolution done, outputs copied
+    // per slot: inputs landed, convolution done, outputs copied
+    std::vector<cudaEvent_t> evs((size_t)(3 * NS), nullptr);
+    auto ev = [&](int slot, int j) -> cudaEvent_t & { return evs[(size_t)(slot * 3 + j)]; };
     bool made = false;
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sin, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sout, cudaStreamNonBlocking);
-    for (int slot = 0; slot < 2 && e == cudaSuccess; slot++)
-        for (int j = 0; j < 3 && e == cudaSuccess; j++) e = cudaEventCreateWithFlags(&ev[slot][j], cudaEventDisableTiming);
+    for (size_t j = 0; j < evs.size() && e == cudaSuccess; j++) e = cudaEventCreateWithFlags(&evs[j], cudaEventDisableTiming);
     made = (e == cudaSuccess);
     cudaEvent_t start = nullptr;
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&start, cudaEventDisableTiming);
@@ -95,18 +107,18 @@ extern "C" int ndconv_conv_batch_host(const ndconv_problem *p, int32_t algo, int
     if (e == cudaSuccess) e = cudaStreamWaitEvent(sin, start, 0);
     s = (e == cudaSuccess) ? NDCONV_OK : ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e));
     for (int64_t c0 = 0, chunk = 0; c0 < n && s == NDCONV_OK; c0 += C, chunk++) {
-        const int slot = (int)(chunk & 1);
+        const int slot = (int)(chunk % NS);
         const int64_t cnt = std::min<int64_t>(C, n - c0);
         // inputs: the slot's inputs are free once its previous convolution is done
-        if (chunk >= 2) cudaStreamWaitEvent(sin, ev[slot][1], 0);
+        if (chunk >= NS) cudaStreamWaitEvent(sin, ev(slot, 1), 0);
         for (int64_t i = 0; i < cnt; i++) {
             cudaMemcpyAsync(ptrs[(size_t)((slot * 3 + 0) * C + i)], data[c0 + i], bx, cudaMemcpyHostToDevice, sin);
             cudaMemcpyAsync(ptrs[(size_t)((slot * 3 + 1) * C + i)], kernel[c0 + i], bk, cudaMemcpyHostToDevice, sin);
         }
-        cudaEventRecord(ev[slot][0], sin);
+        cudaEventRecord(ev(slot, 0), sin);
         // convolution: after the inputs and after the slot's previous outputs left
-        cudaStreamWaitEvent(st, ev[slot][0], 0);
-        if (chunk >= 2) cudaStreamWaitEvent(st, ev[slot][2], 0);
+        cudaStreamWaitEvent(st, ev(slot, 0), 0);
+        if (chunk >= NS) cudaStreamWaitEvent(st, ev(slot, 2), 0);
         const void *const *dx = (const void *const *)(dptr + (slot * 3 + 0) * C);
         const void *const *dk = (const void *const *)(dptr + (slot * 3 + 1) * C);
         void *const *dy = (void *const *)(dptr + (slot * 3 + 2) * C);
@@ -117,21 +129,20 @@ extern "C" int ndconv_conv_batch_host(const ndconv_problem *p, int32_t algo, int
         case NDCONV_C32: s = run_chunk<c32>(P, algo, cnt, dx, dk, dy, proc, st); break;
         default: s = run_chunk<c64>(P, algo, cnt, dx, dk, dy, proc, st); break;
         }
-        cudaEventRecord(ev[slot][1], st);
+        cudaEventRecord(ev(slot, 1), st);
         // outputs back to the host
-        cudaStreamWaitEvent(sout, ev[slot][1], 0);
+        cudaStreamWaitEvent(sout, ev(slot, 1), 0);
         for (int64_t i = 0; i < cnt; i++)
             cudaMemcpyAsync(out[c0 + i], ptrs[(size_t)((slot * 3 + 2) * C + i)], by, cudaMemcpyDeviceToHost, sout);
-        cudaEventRecord(ev[slot][2], sout);
+        cudaEventRecord(ev(slot, 2), sout);
     }
     // the caller's stream covers everything: wait for the last copies, then free
     if (made) {
-        for (int slot = 0; slot < 2; slot++) cudaStreamWaitEvent(st, ev[slot][2], 0);
+        for (int slot = 0; slot < NS; slot++) cudaStreamWaitEvent(st, ev(slot, 2), 0);
     }
     cudaFreeAsync(buf, st);
-    if (made)
-        for (int slot = 0; slot < 2; slot++)
-            for (int j = 0; j < 3; j++) cudaEventDestroy(ev[slot][j]);
+    for (cudaEvent_t x : evs)
+        if (x) cudaEventDestroy(x);
     if (start) cudaEventDestroy(start);
     if (sin) cudaStreamDestroy(sin);
     if (sout) cudaStreamDestroy(sout);
