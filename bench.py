@@ -32,7 +32,7 @@ import numpy as np  # noqa: E402
 
 # DRAM bytes per instance of the batched FFT path from one ncu capture (one
 # wave of 16 instances, caches flushed between the two launches): an upper bound
-PROFILED_TRAFFIC = {"fft": 12.40e6}
+PROFILED_TRAFFIC = {"fft": 12.27e6}
 
 SHAPE_X = (200, 5000)
 SHAPE_K = (11, 31)
