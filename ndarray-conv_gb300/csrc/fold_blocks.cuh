@@ -13,12 +13,14 @@ namespace ndconv {
 namespace foldk {
 
 constexpr int FBM = 128, FBN = 64;
-template <typename T> constexpr int fbk() { return sizeof(T) > 8 ? 8 : 16; }
+// K step of the GEMM (wider elements take shorter steps: two buffers of both
+// operand tiles stay within the 48 KB of static shared memory)
+template <typename T> constexpr int fbk() { return sizeof(T) > 8 ? 4 : (sizeof(T) > 4 ? 8 : 16); }
+constexpr int FPM = FBM + 4, FPN = FBN + 4;  // padded rows: 16-byte aligned, fewer bank conflicts
 
-// shared memory of one GEMM tile
-template <typename T> constexpr size_t gemm_smem() {
-    return sizeof(T) * (size_t)fbk<T>() * (FBM + 1 + FBN + 1) + 2 * sizeof(int64_t) * fbk<T>();
-}
+// shared memory of one GEMM tile: two buffers of the A (FBK x FPM) and B
+// (FBK x FPN) tiles
+template <typename T> constexpr size_t gemm_smem() { return 2 * sizeof(T) * (size_t)fbk<T>() * (FPM + FPN); }
 
 // border-mapped index of tap t for output o on an axis (-1: padding zero)
 __device__ __forceinline__ int64_t fmap(const AxisGeom &A, int64_t o, int64_t t) {
@@ -107,8 +109,13 @@ __device__ __forceinline__ bool scan_elem(const T *__restrict__ x, const T *__re
 }
 
 // Y[om][co] = sum over kk = (ci, tm) of X[om][kk] W[co][kk] for tile (bx, by):
-// 128 x 64 outputs, 8 x 4 per thread (256 threads), K in steps staged in
-// shared memory with the step's tap positions and data offsets tabulated.
+// 128 x 64 outputs, 8 x 4 per thread (256 threads).  K advances in steps of
+// FBK through two shared-memory buffers: the global loads of step s + 1 are
+// in flight (in registers) while step s is multiplied, one barrier per step.
+// A thread always loads the same K column kk = tid mod FBK of a step, so its
+// tap position and data offset take one division per step.  The data operand
+// is gathered through the border map.  Summation order: k ascending for every
+// output, as in a plain loop.
 // flag != 0 (a non-finite input): the reference's tap-by-tap sums instead.
 template <typename T>
 __device__ __forceinline__ void gemm_tile(const T *__restrict__ x, const T *__restrict__ W, T *__restrict__ y,
@@ -118,10 +125,10 @@ __device__ __forceinline__ void gemm_tile(const T *__restrict__ x, const T *__re
     using E = Elem<T>;
     using Acc = typename E::Acc;
     constexpr int FBK = fbk<T>();
-    T(*As)[FBM + 1] = reinterpret_cast<T(*)[FBM + 1]>(smem);
-    T(*Bs)[FBN + 1] = reinterpret_cast<T(*)[FBN + 1]>(smem + sizeof(T) * FBK * (FBM + 1));
-    int64_t *kpos = reinterpret_cast<int64_t *>(smem + sizeof(T) * FBK * (FBM + 1 + FBN + 1));
-    int64_t *koff = kpos + FBK;
+    constexpr int RA = FBM * FBK / 256, RB = FBN * FBK / 256;  // operand elements per thread and step
+    constexpr int RS = 256 / FBK;                               // row step between a thread's elements
+    T(*As)[FBK][FPM] = reinterpret_cast<T(*)[FBK][FPM]>(smem);
+    T(*Bs)[FBK][FPN] = reinterpret_cast<T(*)[FBK][FPN]>(smem + 2 * sizeof(T) * FBK * FPM);
     const AxisGeom &Am = F.ax[F.m], &A0 = F.ax[F.f0], &A1 = F.ax[F.f1];
     const int64_t bm = bx * FBM, bn = by * FBN;
     const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
@@ -144,53 +151,74 @@ __device__ __forceinline__ void gemm_tile(const T *__restrict__ x, const T *__re
         for (int j = 0; j < 4; j++) acc[i][j] = E::zero();
     const int64_t kdim = F.cin * F.km;
     const int km = (int)F.km, n1 = (int)A1.n;
-    for (int64_t k0 = 0; k0 < kdim; k0 += FBK) {
-        if (tid < FBK) {
-            const int64_t kg = k0 + tid;
-            const int ci = (int)(kg / km), tm = (int)(kg - (int64_t)ci * km);
-            kpos[tid] = (F.tlo_m + tm) * Am.d;
-            koff[tid] = (kg < kdim) ? (int64_t)(ci / n1) * A0.xs + (int64_t)(ci % n1) * A1.xs : -1;
-        }
-        __syncthreads();
+    const int kk = tid % FBK, r0 = tid / FBK;
+    T ra[RA], rb[RB];
+    // this thread's operand elements of the step starting at k0
+    auto fetch = [&](int64_t k0) {
+        const int64_t kg = k0 + kk;
+        const bool kin = kg < kdim;
+        const int ci = kin ? (int)(kg / km) : 0, tm = kin ? (int)(kg - (int64_t)ci * km) : 0;
+        const int64_t kpos = (F.tlo_m + tm) * Am.d;
+        const int64_t koff = (int64_t)(ci / n1) * A0.xs + (int64_t)(ci % n1) * A1.xs;
 #pragma unroll
-        for (int r = 0; r < FBM * FBK / 256; r++) {
-            const int idx = tid + r * 256;
-            const int kk = idx % FBK, row = idx / FBK;
-            const int64_t om = bm + row;
+        for (int r = 0; r < RA; r++) {
+            const int64_t om = bm + r0 + r * RS;
             T v = E::zero();
-            if (koff[kk] >= 0 && om < Am.out) {
-                const int64_t mi = axis_map(Am, om * Am.s + kpos[kk]);
-                if (mi >= 0) v = x[mi * Am.xs + koff[kk]];
+            if (kin && om < Am.out) {
+                const int64_t mi = axis_map(Am, om * Am.s + kpos);
+                if (mi >= 0) v = x[mi * Am.xs + koff];
             }
-            As[kk][row] = v;
+            ra[r] = v;
         }
 #pragma unroll
-        for (int r = 0; r < FBN * FBK / 256; r++) {
-            const int idx = tid + r * 256;
-            const int kk = idx % FBK, col = idx / FBK;
-            const int64_t kg = k0 + kk, co = bn + col;
+        for (int r = 0; r < RB; r++) {
+            const int64_t co = bn + r0 + r * RS;
             T w = E::zero();
-            if (kg < kdim && co < F.cout) {
+            if (kin && co < F.cout) {
                 const T *p = W + co * kdim + kg;
                 if constexpr (std::is_same<T, float>::value) w = l2 ? __ldcg(p) : *p;
                 else w = *p;  // only f32 runs inside the persistent queue
             }
-            Bs[kk][col] = w;
+            rb[r] = w;
         }
-        __syncthreads();
+    };
+    auto stash = [&](int buf) {
 #pragma unroll
-        for (int kk = 0; kk < FBK; kk++) {
+        for (int r = 0; r < RA; r++) As[buf][kk][r0 + r * RS] = ra[r];
+#pragma unroll
+        for (int r = 0; r < RB; r++) Bs[buf][kk][r0 + r * RS] = rb[r];
+    };
+    fetch(0);
+    stash(0);
+    __syncthreads();
+    int cur = 0;
+    for (int64_t k0 = 0; k0 < kdim; k0 += FBK) {
+        const bool more = k0 + FBK < kdim;
+        if (more) fetch(k0 + FBK);
+#pragma unroll
+        for (int q = 0; q < FBK; q++) {
             T a[8], b[4];
+            if constexpr (std::is_same<T, float>::value) {
+                const float4 a0 = *reinterpret_cast<const float4 *>(&As[cur][q][ty * 8]);
+                const float4 a1 = *reinterpret_cast<const float4 *>(&As[cur][q][ty * 8 + 4]);
+                const float4 b0 = *reinterpret_cast<const float4 *>(&Bs[cur][q][tx * 4]);
+                a[0] = a0.x, a[1] = a0.y, a[2] = a0.z, a[3] = a0.w;
+                a[4] = a1.x, a[5] = a1.y, a[6] = a1.z, a[7] = a1.w;
+                b[0] = b0.x, b[1] = b0.y, b[2] = b0.z, b[3] = b0.w;
+            } else {
 #pragma unroll
-            for (int i = 0; i < 8; i++) a[i] = As[kk][ty * 8 + i];
+                for (int i = 0; i < 8; i++) a[i] = As[cur][q][ty * 8 + i];
 #pragma unroll
-            for (int j = 0; j < 4; j++) b[j] = Bs[kk][tx * 4 + j];
+                for (int j = 0; j < 4; j++) b[j] = Bs[cur][q][tx * 4 + j];
+            }
 #pragma unroll
             for (int i = 0; i < 8; i++)
 #pragma unroll
                 for (int j = 0; j < 4; j++) E::mac(acc[i][j], a[i], b[j]);
         }
+        if (more) stash(cur ^ 1);  // the other buffer: its readers finished before the last barrier
         __syncthreads();
+        cur ^= 1;
     }
 #pragma unroll
     for (int i = 0; i < 8; i++) {
