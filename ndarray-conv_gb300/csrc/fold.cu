@@ -73,7 +73,7 @@ template <typename T> bool plan_fold(const DirectParams<T> &P, FoldParams &F) {
     double best = -1;
     for (int m = 0; m < 3; m++) {
         const int f0 = m == 0 ? 1 : 0, f1 = m == 2 ? 1 : 2;
-        if (A[f0].n > 256 || A[f1].n > 256) continue;
+        if (A[f0].n > 256 || A[f1].n > 256 || P.t_n[m] < 1) continue;
         const double cin = (double)A[f0].n * A[f1].n, cout = (double)A[f0].out * A[f1].out, km = (double)P.t_n[m];
         if (cin > 4096 || cout * cin * km > (double)(1 << 26) || cout / FBN > 65535) continue;
         const double gemm = (double)A[m].out * cout * cin * km;

@@ -153,22 +153,34 @@ __device__ __forceinline__ void gemm_tile(const T *__restrict__ x, const T *__re
     const int km = (int)F.km, n1 = (int)A1.n;
     const int kk = tid % FBK, r0 = tid / FBK;
     T ra[RA], rb[RB];
-    // this thread's operand elements of the step starting at k0
-    auto fetch = [&](int64_t k0) {
-        const int64_t kg = k0 + kk;
+    // (channel, main-axis tap) of this thread's K column, advanced by FBK per
+    // step without a division
+    int ci = kk / km, tm = kk - (kk / km) * km;
+    // this thread's operand elements of the step whose column is kg
+    auto fetch = [&](int64_t kg) {
         const bool kin = kg < kdim;
-        const int ci = kin ? (int)(kg / km) : 0, tm = kin ? (int)(kg - (int64_t)ci * km) : 0;
         const int64_t kpos = (F.tlo_m + tm) * Am.d;
         const int64_t koff = (int64_t)(ci / n1) * A0.xs + (int64_t)(ci % n1) * A1.xs;
+        // padded positions of the first and last row of the thread: all
+        // inside the data (the usual case) -> plain strided loads
+        const int64_t om0 = bm + r0, omL = bm + r0 + (RA - 1) * RS;
+        const int64_t j0 = om0 * Am.s + kpos, jL = omL * Am.s + kpos;
+        if (kin && j0 >= Am.p0 && jL < Am.p0 + Am.n && omL < Am.out) {
+            const T *xp = x + (j0 - Am.p0) * Am.xs + koff;
+            const int64_t step = (int64_t)RS * Am.s * Am.xs;
 #pragma unroll
-        for (int r = 0; r < RA; r++) {
-            const int64_t om = bm + r0 + r * RS;
-            T v = E::zero();
-            if (kin && om < Am.out) {
-                const int64_t mi = axis_map(Am, om * Am.s + kpos);
-                if (mi >= 0) v = x[mi * Am.xs + koff];
+            for (int r = 0; r < RA; r++) ra[r] = xp[r * step];
+        } else {
+#pragma unroll
+            for (int r = 0; r < RA; r++) {
+                const int64_t om = om0 + r * RS;
+                T v = E::zero();
+                if (kin && om < Am.out) {
+                    const int64_t mi = axis_map(Am, om * Am.s + kpos);
+                    if (mi >= 0) v = x[mi * Am.xs + koff];
+                }
+                ra[r] = v;
             }
-            ra[r] = v;
         }
 #pragma unroll
         for (int r = 0; r < RB; r++) {
@@ -188,13 +200,23 @@ __device__ __forceinline__ void gemm_tile(const T *__restrict__ x, const T *__re
 #pragma unroll
         for (int r = 0; r < RB; r++) Bs[buf][kk][r0 + r * RS] = rb[r];
     };
-    fetch(0);
+    auto advance = [&]() {
+        tm += FBK;
+        while (tm >= km) {
+            tm -= km;
+            ci++;
+        }
+    };
+    fetch(kk);
     stash(0);
     __syncthreads();
     int cur = 0;
     for (int64_t k0 = 0; k0 < kdim; k0 += FBK) {
         const bool more = k0 + FBK < kdim;
-        if (more) fetch(k0 + FBK);
+        if (more) {
+            advance();
+            fetch(k0 + FBK + kk);
+        }
 #pragma unroll
         for (int q = 0; q < FBK; q++) {
             T a[8], b[4];
