@@ -571,7 +571,8 @@ def main():
             gbs, cores, sample = cpu_baseline(args.cpu_seconds)
             cpu = {"value": gbs, "unit": "GB/s", "cores": cores, "kind": "port", "sample": sample}
         line = {
-            "metric": "conv GB/s (algorithmic bytes 4*(|x|+|k|+|y|)), conv_fft x[200,5000]*k[11,31] dil 2",
+            "metric": "conv GB/s (algorithmic bytes 4*(|x|+|k|+|y|)), "
+                      f"{'conv_fft' if algo else 'conv'} x[200,5000]*k[11,31] dil 2",
             "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded Uniform[0,1), distinct data and kernel per instance)",
