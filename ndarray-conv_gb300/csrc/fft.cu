@@ -2261,6 +2261,20 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
         fa.y = full.y1;
         fa.W = reinterpret_cast<float *>(static_cast<unsigned char *>(B->ws) + h.ws_off);
         fa.T1 = fa.W + F.cout * F.cin * F.km;
+        {
+            // tap tables, built here once and copied behind the folded weights
+            int32_t *dtab = reinterpret_cast<int32_t *>(fa.T1 + F.km * F.ax[F.f0].K * F.ax[F.f1].out * F.ax[F.f1].n);
+            const AxisGeom &G0 = F.ax[F.f0], &G1 = F.ax[F.f1];
+            const int64_t e0 = fold_table_entries(G0), e1 = fold_table_entries(G1);
+            std::vector<int32_t> tab((size_t)(e0 + e1));
+            for (int64_t o = 0; o < G0.out; o++)
+                fold_table_row(G0, o, tab.data() + o * (G0.n + 1), tab.data() + G0.out * (G0.n + 1) + o * G0.K);
+            for (int64_t o = 0; o < G1.out; o++)
+                fold_table_row(G1, o, tab.data() + e0 + o * (G1.n + 1), tab.data() + e0 + G1.out * (G1.n + 1) + o * G1.K);
+            cudaError_t ce = cudaMemcpy(dtab, tab.data(), sizeof(int32_t) * tab.size(), cudaMemcpyHostToDevice);
+            if (ce != cudaSuccess) return fail(ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(ce)));
+            fold_set_tables(fa.F, dtab);
+        }
         fa.flag = B->nctrs++;
         fa.fb = full;
         const int arg = (int)B->fargs.size();

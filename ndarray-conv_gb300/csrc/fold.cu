@@ -31,6 +31,17 @@ namespace ndconv {
 namespace {
 using namespace foldk;
 
+// tap tables of both folded axes: one thread per output index
+__global__ void fold_tables_kernel(FoldParams F, int32_t *t0, int32_t *t1) {
+    const AxisGeom &A0 = F.ax[F.f0], &A1 = F.ax[F.f1];
+    const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u < A0.out) fold_table_row(A0, u, t0 + u * (A0.n + 1), t0 + A0.out * (A0.n + 1) + u * A0.K);
+    else if (u < A0.out + A1.out) {
+        const int64_t o = u - A0.out;
+        fold_table_row(A1, o, t1 + o * (A1.n + 1), t1 + A1.out * (A1.n + 1) + o * A1.K);
+    }
+}
+
 template <typename T>
 __global__ void fold_f1_kernel(const T *__restrict__ k, FoldParams F, T *__restrict__ T1) {
     const int64_t total = f1_count<T>(F);
@@ -102,7 +113,18 @@ template <typename T> bool plan_fold(const DirectParams<T> &P, FoldParams &F) {
 template <typename T> size_t fold_scratch_bytes(const FoldParams &F) {
     const size_t w = (size_t)(F.cout * F.cin * F.km);
     const size_t t1 = (size_t)(F.km * F.ax[F.f0].K * F.ax[F.f1].out * F.ax[F.f1].n);
-    return sizeof(T) * (w + t1) + 256;
+    const size_t tabs = (size_t)(fold_table_entries(F.ax[F.f0]) + fold_table_entries(F.ax[F.f1]));
+    return sizeof(T) * (w + t1) + sizeof(int32_t) * tabs + 256;
+}
+
+void fold_set_tables(FoldParams &F, void *tables) {
+    int32_t *t0 = static_cast<int32_t *>(tables);
+    int32_t *t1 = t0 + fold_table_entries(F.ax[F.f0]);
+    const AxisGeom &A0 = F.ax[F.f0], &A1 = F.ax[F.f1];
+    F.off[0] = t0;
+    F.tap[0] = t0 + A0.out * (A0.n + 1);
+    F.off[1] = t1;
+    F.tap[1] = t1 + A1.out * (A1.n + 1);
 }
 
 template <typename T>
@@ -118,17 +140,26 @@ cudaError_t fold_launch(const T *x, const T *k, T *y, const FoldParams &F, const
     }
     T *W = static_cast<T *>(ws);
     T *T1 = W + F.cout * F.cin * F.km;
-    int *flag = reinterpret_cast<int *>((reinterpret_cast<uintptr_t>(T1 + F.km * F.ax[F.f0].K * F.ax[F.f1].out *
-                                                                          F.ax[F.f1].n) + 15) & ~(uintptr_t)15);
+    int32_t *tabs = reinterpret_cast<int32_t *>(T1 + F.km * F.ax[F.f0].K * F.ax[F.f1].out * F.ax[F.f1].n);
+    const int64_t ntab = fold_table_entries(F.ax[F.f0]) + fold_table_entries(F.ax[F.f1]);
+    int *flag = reinterpret_cast<int *>((reinterpret_cast<uintptr_t>(tabs + ntab) + 15) & ~(uintptr_t)15);
+    FoldParams Ft = F;
+    fold_set_tables(Ft, tabs);
     cudaMemsetAsync(flag, 0, sizeof(int), st);
+    {
+        const int64_t rows = F.ax[F.f0].out + F.ax[F.f1].out;
+        fold_tables_kernel<<<(unsigned)((rows + 127) / 128), 128, 0, st>>>(Ft, tabs,
+                                                                          tabs + fold_table_entries(F.ax[F.f0]));
+        ndconv_count_launch();
+    }
     if (!std::is_same<T, int32_t>::value) {
         fold_scan_kernel<T><<<152 * 4, 256, 0, st>>>(x, k, F, flag);
         ndconv_count_launch();
     }
-    fold_f1_kernel<T><<<152 * 8, 256, 0, st>>>(k, F, T1);
-    fold_f0_kernel<T><<<152 * 8, 256, 0, st>>>(T1, F, W);
+    fold_f1_kernel<T><<<152 * 8, 256, 0, st>>>(k, Ft, T1);
+    fold_f0_kernel<T><<<152 * 8, 256, 0, st>>>(T1, Ft, W);
     dim3 grid((unsigned)((F.ax[F.m].out + FBM - 1) / FBM), (unsigned)((F.cout + FBN - 1) / FBN));
-    fold_gemm_kernel<T><<<grid, 256, 0, st>>>(x, W, y, F, flag, k, full);
+    fold_gemm_kernel<T><<<grid, 256, 0, st>>>(x, W, y, Ft, flag, k, full);
     ndconv_count_launch(3);
     cudaError_t e = cudaGetLastError();
     if (!scratch) cudaFreeAsync(ws, st);

@@ -49,6 +49,7 @@ __host__ __device__ inline int64_t scan_count(const FoldParams &F) {
 }
 
 // T1[tm][t0][of1][if1] = sum over t1 with map_f1(of1, t1) = if1 of kf[tm, t0, t1]
+// (the taps of bucket (of1, if1) of the f1 table, ascending)
 template <typename T>
 __device__ __forceinline__ void f1_elem(const T *__restrict__ k, const FoldParams &F, T *__restrict__ T1, int64_t u) {
     using E = Elem<T>;
@@ -57,9 +58,9 @@ __device__ __forceinline__ void f1_elem(const T *__restrict__ k, const FoldParam
     const int64_t i1 = u % n1, r = u / n1;
     const int64_t o1 = r % o1n, r2 = r / o1n;
     const int64_t t0 = r2 % K0, tm = r2 / K0;
+    const int32_t *off = F.off[1] + o1 * (n1 + 1), *tap = F.tap[1] + o1 * A1.K;
     typename E::Acc acc = E::zero();
-    for (int64_t t1 = 0; t1 < A1.K; t1++)
-        if (fmap(A1, o1, t1) == i1) E::add(acc, kf_at(k, F, tm, t0, t1));
+    for (int e = off[i1], e1 = off[i1 + 1]; e < e1; e++) E::add(acc, kf_at(k, F, tm, t0, (int64_t)tap[e]));
     T1[u] = E::out(acc);
 }
 
@@ -73,15 +74,15 @@ __device__ __forceinline__ void f0_elem(const T *__restrict__ T1, const FoldPara
     const int64_t tm = u % F.km, r = u / F.km;
     const int64_t ci = r % F.cin, co = r / F.cin;
     const int64_t i0 = ci / n1, i1 = ci % n1, o0 = co / o1n, o1 = co % o1n;
+    const int32_t *off = F.off[0] + o0 * (A0.n + 1), *tap = F.tap[0] + o0 * K0;
     typename E::Acc acc = E::zero();
-    for (int64_t t0 = 0; t0 < K0; t0++)
-        if (fmap(A0, o0, t0) == i0) {
-            const T *p = T1 + ((tm * K0 + t0) * o1n + o1) * n1 + i1;
-            T v;
-            if constexpr (std::is_same<T, float>::value) v = l2 ? __ldcg(p) : *p;
-            else v = *p;  // only f32 runs inside the persistent queue
-            E::add(acc, v);
-        }
+    for (int e = off[i0], e1 = off[i0 + 1]; e < e1; e++) {
+        const T *p = T1 + ((tm * K0 + tap[e]) * o1n + o1) * n1 + i1;
+        T v;
+        if constexpr (std::is_same<T, float>::value) v = l2 ? __ldcg(p) : *p;
+        else v = *p;  // only f32 runs inside the persistent queue
+        E::add(acc, v);
+    }
     W[u] = E::out(acc);
 }
 
