@@ -20,6 +20,11 @@ CASES = [
     ((4, 3, 500), (15, 17, 5), 2, 1, PaddingMode.Custom([BorderType.Circular, BorderType.Replicate,
                                                          BorderType.Reflect])),
     ((2, 900), (41, 7), 2, 1, PaddingMode.Replicate),
+    # dilation above the folded extents: several taps per sample, empty buckets
+    ((3, 2, 700), (17, 31, 9), 5, 2, PaddingMode.Circular),
+    ((1, 4, 900), (9, 21, 5), 3, 1, PaddingMode.Replicate),
+    ((2, 700, 3), (23, 5, 41), 4, 3, PaddingMode.Custom([BorderType.Reflect, BorderType.Circular,
+                                                         BorderType.Replicate])),
 ]
 
 

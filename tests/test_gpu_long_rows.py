@@ -114,3 +114,17 @@ def test_kernel_row_beyond_segments_falls_back():
     with pytest.raises(ndconv.ConvError):
         ndconv.conv_algo(x, k, mode, pm, _abi.ALGO_FFT_RS)
     assert normwise_err(ndconv.conv_fft(x, k, mode, pm), y64) <= TOL64
+
+
+def test_long_rows_strided_view():
+    # every other sample of a 120,000-sample row, read in place through its stride
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(17)
+    base = torch.rand((3, 120_000), generator=g, device="cuda")
+    x = base[:, ::2]
+    k = torch.rand((2, 45), generator=g, device="cuda")
+    mode, pm = ConvMode.Same, PaddingMode.Custom([BorderType.Replicate, BorderType.Reflect])
+    y64 = _oracle64(x.contiguous().cpu().numpy(), k.cpu().numpy(), mode, pm)
+    for algo in (_abi.ALGO_FFT, _abi.ALGO_FFT_RS):
+        y = ndconv.conv_algo(x, k, mode, pm, algo)
+        assert normwise_err(y.cpu().numpy(), y64) <= TOL32, algo
