@@ -2042,6 +2042,23 @@ template <typename T> int fft_fits(const Geom3<T> &g, int fv) {
 }
 
 // Build the plan: per-instance tasks, spectra, device copies of everything.
+// Device memory, graph, stream and events of a plan (null members skipped).
+void release(ndconv_batch_plan *B) {
+    if (B->exec) cudaGraphExecDestroy(B->exec);
+    if (B->graph) cudaGraphDestroy(B->graph);
+    cudaFree(B->d_tasks);
+    cudaFree(B->d_rargs);
+    cudaFree(B->d_cargs);
+    cudaFree(B->d_dargs);
+    cudaFree(B->d_fargs);
+    cudaFree(B->d_fix);
+    cudaFree(B->d_ctrs);
+    cudaFree(B->ws);
+    if (B->ev_fork) cudaEventDestroy(B->ev_fork);
+    if (B->ev_join) cudaEventDestroy(B->ev_join);
+    if (B->side) cudaStreamDestroy(B->side);
+}
+
 int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const void *const *data,
            const void *const *kernel, void *const *out, ndconv_batch_plan **outp) {
     auto *B = new ndconv_batch_plan();
@@ -2049,6 +2066,7 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
     B->n = n;
     B->inst.resize((size_t)n);
     auto fail = [&](int st) {
+        release(B);  // nothing of the plan has been launched yet
         delete B;
         return st;
     };
@@ -2554,19 +2572,7 @@ extern "C" int ndconv_batch_info(const ndconv_batch_plan *B, int64_t info[8]) {
 extern "C" int ndconv_batch_destroy(ndconv_batch_plan *B) {
     if (!B) return NDCONV_OK;
     cudaDeviceSynchronize();
-    if (B->exec) cudaGraphExecDestroy(B->exec);
-    if (B->graph) cudaGraphDestroy(B->graph);
-    cudaFree(B->d_tasks);
-    cudaFree(B->d_rargs);
-    cudaFree(B->d_cargs);
-    cudaFree(B->d_dargs);
-    cudaFree(B->d_fargs);
-    cudaFree(B->d_fix);
-    cudaFree(B->d_ctrs);
-    cudaFree(B->ws);
-    if (B->ev_fork) cudaEventDestroy(B->ev_fork);
-    if (B->ev_join) cudaEventDestroy(B->ev_join);
-    if (B->side) cudaStreamDestroy(B->side);
+    ndconv::batch::release(B);
     delete B;
     return NDCONV_OK;
 }
