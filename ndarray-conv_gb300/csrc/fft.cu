@@ -1110,6 +1110,8 @@ template <typename T> int make_conv_plan(const Geom3<T> &g, FftConvPlan<T> &cp, 
         cp.F[a] = (cp.P[a] == 1) ? 1 : (pow2 ? pow2_size(cp.P[a], real && a == 2) : smooth_size(cp.P[a], real && a == 2));
     }
     cp.astar = cp.F[0] > 1 ? 0 : (cp.F[1] > 1 ? 1 : 2);
+    // row positions and output indices of the row kernels are 32-bit
+    if (cp.P[2] >= ((int64_t)1 << 31) - 1) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "FFT row longer than 2^31 samples");
     cp.seg_n = 1;
     cp.seg_len = 0;
     if (!row_len_fits<T>(cp.F[2])) {
