@@ -52,6 +52,25 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def fp32_fma_roofline(out_shape, ms_per_instance, sm_mhz=None):
+    """The direct path's compute roofline: 2 |y| nnz(k) flops per instance
+    (the taps of the 2-D case are all non-zero) against the CUDA cores' FP32
+    FMA peak, 152 SMs x 128 lanes x 2 flops x the SM clock (the measured
+    maximum unless a sampled clock is given)."""
+    flops = 2.0 * float(np.prod(out_shape)) * float(np.prod(SHAPE_K))
+    mhz = sm_mhz
+    if not mhz:
+        try:
+            with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+                mhz = float(json.load(f)["sm_max_mhz"])
+        except Exception:
+            mhz = 2070.0
+    peak = 152 * 128 * 2 * mhz * 1e6 / 1e12
+    achieved = flops / (ms_per_instance * 1e-3) / 1e12
+    return {"bound": "fp32_fma", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "flops_per_instance": flops}
+
+
 def problem_args():
     import ndconv
     from ndconv import BorderType, ConvMode, PaddingMode
@@ -597,6 +616,9 @@ def main():
             "clocks": clk.summary(),
             "normwise_err_vs_f64": err,
         }
+        if not algo:
+            # the direct path is bound by the FP32 FMA rate, not by HBM
+            line["compute_roofline"] = fp32_fma_roofline(out_shape, per_launch_ms, line["clocks"].get("sm_mhz"))
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
