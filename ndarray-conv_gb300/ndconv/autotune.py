@@ -1,6 +1,6 @@
 """Autotuner: times every algorithm variant of an instance on the GPU (CUDA
 events, warm-up first, best of `reps`), keeps the timings in a database,
-and trains / judges the learned dispatcher against them.
+and trains and evaluates the learned dispatcher against them.
 
 The exhaustive autotuner is the ground truth: the dispatcher's regret on a
 held-out set is t(pick) / t(best) - 1 per instance, and the total-time ratio

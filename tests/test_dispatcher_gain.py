@@ -1,4 +1,4 @@
-"""What the trained dispatcher network gains over the cost model, judged by
+"""What the trained dispatcher network gains over the cost model, measured against
 the exhaustive autotuner's timings of 2,000 held-out configurations
 (committed with the network in ndconv/data).
 
