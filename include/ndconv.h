@@ -199,9 +199,9 @@ int ndconv_batch_status(ndconv_batch_plan *plan, void *stream);
 int ndconv_batch_info(const ndconv_batch_plan *plan, int64_t info[8]);
 int ndconv_batch_destroy(ndconv_batch_plan *plan);
 
-/* ndconv_conv_fft for callers that cannot allocate device memory (inside
- * a CUDA graph being captured, hosts that forbid allocation after start-up,
- * plugins whose host owns every allocation).  No counterpart in the
+/* ndconv_conv_fft for callers that cannot allocate device memory (real-time
+ * or embedded hosts that forbid allocation after start-up, plugins whose
+ * host application owns every device allocation).  No counterpart in the
  * reference.  Same arguments and results as ndconv_conv_fft without a
  * processor, but the spectra and twiddle tables live in one fixed 16 MiB
  * device array that the library holds on every GPU where it is loaded; it

@@ -1,10 +1,10 @@
 // ndconv_conv_fft_noalloc: the FFT convolution for callers that cannot
 // allocate device memory.
 //
-// Some callers cannot call cudaMalloc at all: code running inside a CUDA
-// graph that is being captured, real-time or embedded hosts that forbid
-// allocation after start-up, and plugins whose host application owns every
-// device allocation.  This entry point runs the same kernels as
+// Some callers cannot call cudaMalloc at all: real-time or embedded hosts
+// that forbid allocation after start-up (an allocation can block or fail at
+// an arbitrary time), and plugins whose host application owns every device
+// allocation.  This entry point runs the same kernels as
 // ndconv_conv_fft but takes its spectrum buffers and twiddle tables from a
 // fixed, file-scope device array instead of allocating them.  The array
 // (kNoAllocScratchBytes = 16 MiB) is part of the library image: every GPU

@@ -1,8 +1,8 @@
 """float64 numpy restatement of the dispatcher network (forward, masked
 mean-squared-error loss, backward) with the CUDA library's parameter layout.
 
-TEST INFRASTRUCTURE ONLY: the checker for the library's hand-written MLP
-kernels (ndconv_mlp_forward / ndconv_mlp_gradient).  The network has no
+TEST INFRASTRUCTURE ONLY: the oracle against which the library's hand-written
+MLP kernels are tested (ndconv_mlp_forward / ndconv_mlp_gradient).  The network has no
 counterpart in the reference crate; this file follows the library's own
 definition: y = W3 relu(W2 relu(W1 x + b1) + b2) + b3 and
 L = sum_{n,o} m[n,o] (y[n,o] - t[n,o])^2 / (2 sum(m)).

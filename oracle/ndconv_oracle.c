@@ -2,8 +2,8 @@
  * ndconv oracle -- TEST INFRASTRUCTURE ONLY.
  *
  * A plain-C restatement of the reference crate's convolution hot path
- * (ndarray-conv 0.6.1).  It is the checker for the CUDA library and the
- * timed CPU baseline; nothing in the product links or calls it.  Only
+ * (ndarray-conv 0.6.1).  It is the oracle the CUDA library is tested
+ * against and the timed CPU baseline; nothing in the product links or calls it.  Only
  * tests/, __graft_entry__.smoke() and bench.py (cpu baseline / reference
  * arm) load it.
  *

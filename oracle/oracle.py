@@ -1,7 +1,7 @@
 """ctypes wrapper of the C oracle (oracle/ndconv_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
-CPU-baseline / reference legs of bench.py as the checker and the timed CPU
+CPU-baseline / reference legs of bench.py as the oracle and the timed CPU
 restatement of the reference.  The product never imports it.
 
 Functions take a problem structure whose leading fields have the layout of

@@ -1,8 +1,8 @@
 """ndconv_conv_fft_noalloc: FFT convolution for callers that cannot allocate.
 
-Callers inside a CUDA graph capture, hosts that forbid device allocation
-after start-up, and plugins whose host owns every allocation cannot let the
-library call cudaMalloc.  This entry point uses a fixed 16 MiB device array
+Real-time hosts that forbid device allocation after start-up, and plugins
+whose host application owns every allocation, cannot let the library call
+cudaMalloc.  This entry point uses a fixed 16 MiB device array
 inside the library instead.  Its results must match ndconv_conv_fft (the
 allocating entry point) within the tests' f32 tolerance, on two calls in a
 row (the array keeps the previous call's contents), and oversize problems
