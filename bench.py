@@ -34,6 +34,10 @@ import numpy as np  # noqa: E402
 # wave of 16 instances, caches flushed between the two launches): an upper bound
 PROFILED_TRAFFIC = {"fft": 12.27e6}
 
+# the benchmark's metric; every line (both arms, both workloads) reports it
+METRIC = "conv GB/s & % HBM roofline, batched+tuned vs plain GPU, err ≤1e-5 vs FP64"
+METRIC_DETAIL = "GB/s of algorithmic bytes 4*(|x|+|k|+|y|) per instance"
+
 SHAPE_X = (200, 5000)
 SHAPE_K = (11, 31)
 DIL = 2
@@ -160,7 +164,7 @@ def run_reference(args, rank, world):
     if rank != 0:
         return
     steps, warm = args.steps, args.warmup
-    # each step: a bounded sample (`per_step_s` of CPU work) of the workload
+    # each step: a bounded sample (--ref-instances instances) of the workload
     from oracle import oracle as O
     from ndconv import _abi, build_problem, with_dilation
     mode, pm, _ = problem_args()
@@ -179,13 +183,14 @@ def run_reference(args, rank, world):
     el = time.perf_counter() - t0
     gbs = algorithmic_bytes(y.shape) * per_step * steps / el / 1e9
     sample = f"{per_step} instance(s) of x[200,5000]*k[11,31] per step (conv_fft_par port, f32)"
-    line = {"metric": "conv GB/s (algorithmic bytes 4*(|x|+|k|+|y|)), conv_fft x[200,5000]*k[11,31] dil 2",
+    line = {"metric": METRIC,
             "value": gbs, "unit": "GB/s", "n_gpus": world, "steps": steps, "warmup": warm,
             "ms_per_step": el / steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Uniform[0,1))",
             "impl": "reference",
             "config": {"workload": "2-D f32 x[200,5000] * k[11,31] dilation 2, Same, "
-                                   "Custom([Reflect, Circular]); conv_fft"},
+                                   "Custom([Reflect, Circular]); conv_fft",
+                       "metric_detail": METRIC_DETAIL},
             "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": nth, "kind": "port", "sample": sample},
             "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -339,13 +344,14 @@ def bench_uneven(args, world, rank, local_rank):
         if not args.no_cpu_baseline:
             cpu = cpu_baseline_uneven(specs, args.cpu_seconds)
         line = {
-            "metric": "conv GB/s (algorithmic bytes 4*(|x|+|k|+|y|)), uneven batch",
+            "metric": METRIC,
             "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded; uneven-batch distribution)",
             "config": {"workload": f"uneven batch: {len(specs)} instances (rank 1/2/3 = 60/35/5%, "
                                    "2^8..2^20 elements, odd kernels 3..127, dilation/stride 1|2, "
                                    "Zeros/Reflect/Replicate/Circular), one persistent launch + CUDA graph",
+                       "metric_detail": METRIC_DETAIL,
                        "instances_per_gpu": len(specs), "algos": {"direct": int(sum(a == 0 for a in algos)),
                                                                   "fft": int(sum(a != 0 for a in algos))},
                        "dispatcher": {"mlp": "trained network (ndconv/data/dispatcher_mlp.json)",
@@ -590,16 +596,17 @@ def main():
             gbs, cores, sample = cpu_baseline(args.cpu_seconds)
             cpu = {"value": gbs, "unit": "GB/s", "cores": cores, "kind": "port", "sample": sample}
         line = {
-            "metric": "conv GB/s (algorithmic bytes 4*(|x|+|k|+|y|)), "
-                      f"{'conv_fft' if algo else 'conv'} x[200,5000]*k[11,31] dil 2",
+            "metric": METRIC,
             "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded Uniform[0,1), distinct data and kernel per instance)",
             "config": {"workload": f"{B} x 2-D f32 x[200,5000] * k[11,31] dilation 2, Same, "
                                    f"Custom([Reflect, Circular]); {'conv_fft' if algo else 'conv'}, "
                                    f"{args.form} submission",
+                       "metric_detail": METRIC_DETAIL,
                        "batch_per_gpu": B, "algo": args.algo, "form": args.form,
                        "plain_per_instance_gbs": (bytes_step * world / (plain_ms * 1e-3) / 1e9) if plain_ms else None,
+                       "batched_over_plain": (plain_ms / ms) if plain_ms else None,
                        "l2": "inputs (256 MB per GPU) larger than L2, no flush"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,
