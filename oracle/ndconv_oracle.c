@@ -88,6 +88,11 @@ static long prod(const int64_t *s, int n) {
     for (int i = 0; i < n; i++) p *= (long)s[i];
     return p;
 }
+/* shape of rank <= 3 as three extents, leading axes filled with `fill` */
+static void to3(const int64_t *shape, int rank, long fill, long *s3) {
+    for (int i = 0; i < 3; i++) s3[i] = fill;
+    for (int i = 0; i < rank; i++) s3[3 - rank + i] = (long)shape[i];
+}
 static void cstrides(const int64_t *shape, int rank, long *st) {
     long a = 1;
     for (int i = rank - 1; i >= 0; i--) { st[i] = a; a *= (long)shape[i]; }
@@ -218,21 +223,18 @@ int orc_padding(const orc_problem *p, const int64_t pad[3][2], const double *x, 
     if (p->pmode == PM_CONST && !fft_style) { pre[0] = p->cval[0]; pre[1] = p->cval[1]; }
     for (long i = 0; i < total; i++)
         for (int c = 0; c < nc; c++) out[i * nc + c] = pre[c];
-    /* padding_const: copy the input into [p0, p0+n) on every axis (mod.rs:175-200) */
+    /* padding_const: copy the input into [p0, p0+n) on every axis
+     * (mod.rs:175-200), one contiguous last-axis row at a time */
     {
-        long xst[3], ost[3];
-        cstrides(p->xs, rank, xst);
-        cstrides(L, rank, ost);
-        long nx = prod(p->xs, rank);
-        for (long f = 0; f < nx; f++) {
-            long o = 0, r = f;
-            for (int i = 0; i < rank; i++) {
-                long idx = r / xst[i];
-                r %= xst[i];
-                o += (idx + pad[i][0]) * ost[i];
-            }
-            for (int c = 0; c < nc; c++) out[o * nc + c] = x[f * nc + c];
-        }
+        long n3[3], L3[3], p3[3];
+        to3(p->xs, rank, 1, n3);
+        to3(L, rank, 1, L3);
+        for (int i = 0; i < 3; i++) p3[i] = 0;
+        for (int i = 0; i < rank; i++) p3[3 - rank + i] = pad[i][0];
+        for (long i0 = 0; i0 < n3[0]; i0++)
+            for (long i1 = 0; i1 < n3[1]; i1++)
+                memcpy(out + (((i0 + p3[0]) * L3[1] + (i1 + p3[1])) * L3[2] + p3[2]) * nc,
+                       x + ((i0 * n3[1] + i1) * n3[2]) * nc, sizeof(double) * (size_t)(n3[2] * nc));
     }
     hbuf b = {out, rank, L, nc};
     int st = ORC_OK;

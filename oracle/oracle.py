@@ -25,9 +25,9 @@ _lib = None
 
 
 def build(force=False):
-    """Compile the oracle with its Makefile (gcc, portable flags)."""
-    if force or not os.path.exists(LIB):
-        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    """Compile the oracle with its Makefile (gcc, portable flags); make
+    rebuilds it whenever a source, header or the Makefile is newer."""
+    subprocess.run(["make", "-s"] + (["-B"] if force else []) + ["-C", HERE], check=True)
 
 
 def lib():

@@ -39,10 +39,34 @@ typedef struct {
     CPLX **work;
 } FN(rows_ctx);
 
+/* Rows [lo, hi) in blocks of ORC_BATCH through the batched transform (rows
+ * gathered into the split element-major layout and scattered back); plans
+ * with a Bluestein stage, and fewer than four rows, go row by row. */
 static void FN(rows_c2c_worker)(void *vc, long lo, long hi, int tid) {
     FN(rows_ctx) *c = (FN(rows_ctx) *)vc;
-    for (long r = lo; r < hi; r++)
-        FN(orc_fft_exec)(c->plan, c->in + r * c->len, c->out + r * c->len, c->work[tid], c->sign);
+    const long len = c->len;
+    if (c->plan->m || len < 2 || hi - lo < 4) {
+        for (long r = lo; r < hi; r++)
+            FN(orc_fft_exec)(c->plan, c->in + r * len, c->out + r * len, c->work[tid], c->sign);
+        return;
+    }
+    REAL *xb = (REAL *)c->work[tid], *sb = xb + 2 * len * ORC_BATCH;
+    for (long r0 = lo; r0 < hi; r0 += ORC_BATCH) {
+        const int B = (int)(hi - r0 < ORC_BATCH ? hi - r0 : ORC_BATCH);
+        const CPLX *in = c->in + r0 * len;
+        for (long j = 0; j < len; j++)
+            for (int b = 0; b < B; b++) {
+                xb[2 * j * B + b] = in[b * len + j].re;
+                xb[(2 * j + 1) * B + b] = in[b * len + j].im;
+            }
+        FN(fft_batch)(c->plan, xb, sb, B, c->sign);
+        CPLX *out = c->out + r0 * len;
+        for (long j = 0; j < len; j++)
+            for (int b = 0; b < B; b++) {
+                out[b * len + j].re = xb[2 * j * B + b];
+                out[b * len + j].im = xb[(2 * j + 1) * B + b];
+            }
+    }
 }
 
 static CPLX **FN(alloc_work)(int nth, long n) {
@@ -76,15 +100,55 @@ typedef struct {
     CPLX **work;
 } FN(real_ctx);
 
+/* Even-length rows go through the batched half-length transform in blocks
+ * of ORC_BATCH rows; odd lengths, Bluestein plans and fewer than four rows
+ * go row by row. */
+static int FN(real_batched)(const FN(real_ctx) *c, long rows) {
+    return c->n % 2 == 0 && c->n >= 4 && !c->half->m && rows >= 4;
+}
 static void FN(r2c_worker)(void *vc, long lo, long hi, int tid) {
     FN(real_ctx) *c = (FN(real_ctx) *)vc;
-    for (long r = lo; r < hi; r++)
-        FN(orc_rfft)(c->half, c->full, c->n, c->rin + r * c->n, c->cout + r * c->h, c->work[tid]);
+    const long n = c->n, m = n / 2;
+    if (!FN(real_batched)(c, hi - lo)) {
+        for (long r = lo; r < hi; r++)
+            FN(orc_rfft)(c->half, c->full, n, c->rin + r * n, c->cout + r * c->h, c->work[tid]);
+        return;
+    }
+    REAL *zb = (REAL *)c->work[tid], *sb = zb + 2 * m * ORC_BATCH;
+    for (long r0 = lo; r0 < hi; r0 += ORC_BATCH) {
+        const int B = (int)(hi - r0 < ORC_BATCH ? hi - r0 : ORC_BATCH);
+        const REAL *x = c->rin + r0 * n;
+        for (long j = 0; j < m; j++)
+            for (int b = 0; b < B; b++) {
+                zb[2 * j * B + b] = x[b * n + 2 * j];
+                zb[(2 * j + 1) * B + b] = x[b * n + 2 * j + 1];
+            }
+        FN(fft_batch)(c->half, zb, sb, B, -1);
+        for (int b = 0; b < B; b++)
+            FN(rfft_post)(c->full, n, zb + b, zb + B + b, 2 * B, c->cout + (r0 + b) * c->h);
+    }
 }
 static void FN(c2r_worker)(void *vc, long lo, long hi, int tid) {
     FN(real_ctx) *c = (FN(real_ctx) *)vc;
-    for (long r = lo; r < hi; r++)
-        FN(orc_irfft)(c->half, c->full, c->n, c->cin + r * c->h, c->rout + r * c->n, c->work[tid]);
+    const long n = c->n, m = n / 2;
+    if (!FN(real_batched)(c, hi - lo)) {
+        for (long r = lo; r < hi; r++)
+            FN(orc_irfft)(c->half, c->full, n, c->cin + r * c->h, c->rout + r * n, c->work[tid]);
+        return;
+    }
+    REAL *zb = (REAL *)c->work[tid], *sb = zb + 2 * m * ORC_BATCH;
+    for (long r0 = lo; r0 < hi; r0 += ORC_BATCH) {
+        const int B = (int)(hi - r0 < ORC_BATCH ? hi - r0 : ORC_BATCH);
+        for (int b = 0; b < B; b++)
+            FN(irfft_pre)(c->full, n, c->cin + (r0 + b) * c->h, zb + b, zb + B + b, 2 * B);
+        FN(fft_batch)(c->half, zb, sb, B, +1);
+        REAL *x = c->rout + r0 * n;
+        for (long j = 0; j < m; j++)
+            for (int b = 0; b < B; b++) {
+                x[b * n + 2 * j] = zb[2 * j * B + b];
+                x[b * n + 2 * j + 1] = zb[(2 * j + 1) * B + b];
+            }
+    }
 }
 
 /* real::Processor::forward: in shape s -> out (caller allocates prod with
@@ -222,28 +286,33 @@ static int FN(conv_fft)(const orc_problem *p, int is_complex, const REAL *x, con
     free(xd);
     if (st) { free(pd); return st; }
     REAL *dbuf = calloc(nF * nc, sizeof(REAL)), *kbuf = calloc(nF * nc, sizeof(REAL));
-    long pst[3], fst[3], kst[3];
-    cstrides(pds, rank, pst);
-    cstrides(F, rank, fst);
-    cstrides(p->ks, rank, kst);
-    for (long f = 0; f < npd; f++) {
-        long r = f, o = 0;
-        for (int i = 0; i < rank; i++) { long idx = r / pst[i]; r %= pst[i]; o += idx * fst[i]; }
-        for (int c = 0; c < nc; c++) dbuf[o * nc + c] = (REAL)pd[f * nc + c];
-    }
+    /* canonical three-axis forms (leading extents 1) for the row loops below */
+    long P3[3], F3[3], K3[3], D3[3], E3[3];
+    to3(pds, rank, 1, P3);
+    to3(F, rank, 1, F3);
+    to3(p->ks, rank, 1, K3);
+    to3(p->dil, rank, 1, D3);
+    to3(ke, rank, 1, E3);
+    (void)npd;
+    for (long i0 = 0; i0 < P3[0]; i0++)
+        for (long i1 = 0; i1 < P3[1]; i1++) {
+            const double *src = pd + ((i0 * P3[1] + i1) * P3[2]) * nc;
+            REAL *dst = dbuf + ((i0 * F3[1] + i1) * F3[2]) * nc;
+            for (long j = 0; j < P3[2] * nc; j++) dst[j] = (REAL)src[j];
+        }
     free(pd);
     /* padding::kernel (conv_fft/padding.rs:78-111): buf[i*d] = k[i], or at
      * k_eff-1-i*d (negative slice step) when !reverse */
-    for (long f = 0; f < nk; f++) {
-        long r = f, o = 0;
-        for (int i = 0; i < rank; i++) {
-            long idx = r / kst[i];
-            r %= kst[i];
-            long pos = p->reverse ? idx * p->dil[i] : (ke[i] - 1 - idx * p->dil[i]);
-            o += pos * fst[i];
-        }
-        for (int c = 0; c < nc; c++) kbuf[o * nc + c] = k[f * nc + c];
-    }
+    (void)nk;
+    for (long i0 = 0; i0 < K3[0]; i0++)
+        for (long i1 = 0; i1 < K3[1]; i1++)
+            for (long i2 = 0; i2 < K3[2]; i2++) {
+                long q0 = p->reverse ? i0 * D3[0] : E3[0] - 1 - i0 * D3[0];
+                long q1 = p->reverse ? i1 * D3[1] : E3[1] - 1 - i1 * D3[1];
+                long q2 = p->reverse ? i2 * D3[2] : E3[2] - 1 - i2 * D3[2];
+                long o = (q0 * F3[1] + q1) * F3[2] + q2, f = (i0 * K3[1] + i1) * K3[2] + i2;
+                for (int c = 0; c < nc; c++) kbuf[o * nc + c] = k[f * nc + c];
+            }
     int64_t sshape[3];
     CPLX *ds, *ks_;
     long nspec;
@@ -272,16 +341,19 @@ static int FN(conv_fft)(const orc_problem *p, int is_complex, const REAL *x, con
     if (!is_complex) FN(real_backward)(rank, sshape, ds, F[rank - 1], outF, oshape, nth);
     else FN(complex_transform)(rank, sshape, ds, (CPLX *)outF, oshape, 1, nth);
     /* crop + stride: slice [k_eff-1, pds) step s (mod.rs:282-289) */
-    long ny = prod(ys, rank), yst[3];
-    cstrides(ys, rank, yst);
-    for (long f = 0; f < ny; f++) {
-        long r = f, o = 0;
-        for (int i = 0; i < rank; i++) {
-            long idx = r / yst[i];
-            r %= yst[i];
-            o += (ke[i] - 1 + idx * str[i]) * fst[i];
-        }
-        for (int c = 0; c < nc; c++) y[f * nc + c] = outF[o * nc + c];
+    {
+        long Y3[3], S3[3];
+        to3(ys, rank, 1, Y3);
+        to3(str, rank, 1, S3);
+        long f = 0;
+        for (long i0 = 0; i0 < Y3[0]; i0++)
+            for (long i1 = 0; i1 < Y3[1]; i1++) {
+                long row = ((E3[0] - 1 + i0 * S3[0]) * F3[1] + (E3[1] - 1 + i1 * S3[1])) * F3[2];
+                for (long i2 = 0; i2 < Y3[2]; i2++, f++) {
+                    long o = row + E3[2] - 1 + i2 * S3[2];
+                    for (int c = 0; c < nc; c++) y[f * nc + c] = outF[o * nc + c];
+                }
+            }
     }
     free(dbuf); free(kbuf); free(ds); free(ks_); free(outF);
     return ORC_OK;

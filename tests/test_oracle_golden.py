@@ -224,7 +224,10 @@ def test_oracle_fft1d_vs_numpy(n):
                                atol=1e-10 * n)
 
 
-@pytest.mark.parametrize("shape", [(6,), (5,), (2, 4), (3, 3), (3, 5), (4, 8, 8), (3, 5, 7), (2, 3, 4)])
+@pytest.mark.parametrize("shape", [(6,), (5,), (2, 4), (3, 3), (3, 5), (4, 8, 8), (3, 5, 7), (2, 3, 4),
+                                   # many rows: blocks of batched transforms and their remainders,
+                                   # mixed radices 2/3/4/5/7, a Bluestein length (257)
+                                   (37, 60), (21, 210), (3, 37, 30), (18, 257), (6, 35, 18)])
 def test_processor_layout_vs_numpy(shape):
     """Processor::forward's rotated layout: 1-D as is, 2-D (k1, k0), 3-D (k1, k2, k0)."""
     rng = np.random.default_rng(len(shape))
