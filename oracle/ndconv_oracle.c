@@ -412,9 +412,17 @@ static void *pf_run(void *a) {
     if (j->lo < j->hi) j->fn(j->ctx, j->lo, j->hi, j->tid);
     return NULL;
 }
-static void par_for(long n, int nth, pf_fn fn, void *ctx) {
+/* grain: the fewest items worth a thread of their own, so that small
+ * passes run on fewer threads (or inline) instead of paying for thread
+ * start-up, as rayon's splitting does */
+static int pf_count(long n, int nth, long grain) {
+    if (grain < 1) grain = 1;
+    if (nth > n / grain) nth = (int)(n / grain);
+    return nth < 1 ? 1 : nth;
+}
+static void par_for(long n, int nth, long grain, pf_fn fn, void *ctx) {
+    nth = pf_count(n, nth, grain);
     if (nth <= 1 || n < 2) { fn(ctx, 0, n, 0); return; }
-    if (nth > n) nth = (int)n;
     pthread_t th[256];
     pf_job jobs[256];
     if (nth > 256) nth = 256;

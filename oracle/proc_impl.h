@@ -69,6 +69,13 @@ static void FN(rows_c2c_worker)(void *vc, long lo, long hi, int tid) {
     }
 }
 
+/* rows per thread at least: ~32k samples of work, and four rows so that
+ * the batched transforms apply */
+static long FN(row_grain)(long len) {
+    long g = 32768 / (len > 0 ? len : 1);
+    return g < 4 ? 4 : g;
+}
+
 static CPLX **FN(alloc_work)(int nth, long n) {
     CPLX **w = (CPLX **)malloc(sizeof(CPLX *) * nth);
     for (int t = 0; t < nth; t++) w[t] = (CPLX *)malloc(sizeof(CPLX) * FN(work_len)(n));
@@ -82,10 +89,10 @@ static void FN(free_work)(CPLX **w, int nth) {
 /* c2c along the last axis of a [rows][len] array (out-of-place) */
 static void FN(rows_c2c)(const CPLX *in, CPLX *out, long rows, long len, int sign, int nth) {
     PLAN *pl = FN(plan_create)(len);
-    int nt = nth < 1 ? 1 : nth;
+    int nt = pf_count(rows, nth < 1 ? 1 : nth, FN(row_grain)(len));
     CPLX **w = FN(alloc_work)(nt, len);
     FN(rows_ctx) c = {pl, in, out, len, sign, w};
-    par_for(rows, nt, FN(rows_c2c_worker), &c);
+    par_for(rows, nt, FN(row_grain)(len), FN(rows_c2c_worker), &c);
     FN(free_work)(w, nt);
     FN(plan_destroy)(pl);
 }
@@ -157,11 +164,11 @@ static void FN(real_forward)(int rank, const int64_t *s, const REAL *in, CPLX *o
                              int64_t *oshape, int nth) {
     long n = s[rank - 1], h = n / 2 + 1;
     long rows = prod(s, rank - 1);
-    int nt = nth < 1 ? 1 : nth;
+    int nt = pf_count(rows, nth < 1 ? 1 : nth, FN(row_grain)(n));
     PLAN *half = FN(plan_create)(n / 2 > 0 ? n / 2 : 1), *full = FN(plan_create)(n);
     CPLX **w = FN(alloc_work)(nt, n);
     FN(real_ctx) c = {half, full, n, h, in, NULL, NULL, out, w};
-    par_for(rows, nt, FN(r2c_worker), &c);
+    par_for(rows, nt, FN(row_grain)(n), FN(r2c_worker), &c);
     FN(free_work)(w, nt);
     FN(plan_destroy)(half);
     FN(plan_destroy)(full);
@@ -187,7 +194,7 @@ static void FN(real_forward)(int rank, const int64_t *s, const REAL *in, CPLX *o
  * origin_len is the last forward's last-axis length. */
 static void FN(real_backward)(int rank, const int64_t *s, CPLX *in, long origin_len, REAL *out,
                               int64_t *oshape, int nth) {
-    int64_t a[3];
+    int64_t a[3] = {1, 1, 1};
     for (int i = 0; i < rank; i++) a[i] = s[i];
     long tot = prod(a, rank);
     CPLX *buf = (CPLX *)malloc(sizeof(CPLX) * (tot ? tot : 1));
@@ -203,11 +210,11 @@ static void FN(real_backward)(int rank, const int64_t *s, CPLX *in, long origin_
     free(buf);
     long h = a[rank - 1], n = origin_len;
     long rows = tot / h;
-    int nt = nth < 1 ? 1 : nth;
+    int nt = pf_count(rows, nth < 1 ? 1 : nth, FN(row_grain)(n));
     PLAN *half = FN(plan_create)(n / 2 > 0 ? n / 2 : 1), *full = FN(plan_create)(n);
     CPLX **w = FN(alloc_work)(nt, n);
     FN(real_ctx) c = {half, full, n, h, NULL, in, out, NULL, w};
-    par_for(rows, nt, FN(c2r_worker), &c);
+    par_for(rows, nt, FN(row_grain)(n), FN(c2r_worker), &c);
     FN(free_work)(w, nt);
     FN(plan_destroy)(half);
     FN(plan_destroy)(full);
@@ -334,7 +341,7 @@ static int FN(conv_fft)(const orc_problem *p, int is_complex, const REAL *x, con
     }
     {
         FN(mul_ctx) mc = {ds, ks_};
-        par_for(nspec, nth < 1 ? 1 : nth, FN(mul_worker), &mc);
+        par_for(nspec, nth < 1 ? 1 : nth, 32768, FN(mul_worker), &mc);
     }
     int64_t oshape[3];
     REAL *outF = malloc(sizeof(REAL) * nF * nc);
