@@ -341,7 +341,7 @@ def bench_uneven(args, world, rank, local_rank):
                 errs.append(float(np.linalg.norm(y - y64) / max(np.linalg.norm(y64), 1e-300)))
     if rank == 0:
         cpu = None
-        if not args.no_cpu_baseline:
+        if not args.no_cpu_baseline and world == 1:  # host-core baseline at N = 1 only
             cpu = cpu_baseline_uneven(specs, args.cpu_seconds)
         line = {
             "metric": METRIC,
@@ -592,7 +592,7 @@ def main():
 
     if rank == 0:
         cpu = None
-        if not args.no_cpu_baseline:
+        if not args.no_cpu_baseline and world == 1:  # host-core baseline at N = 1 only
             gbs, cores, sample = cpu_baseline(args.cpu_seconds)
             cpu = {"value": gbs, "unit": "GB/s", "cores": cores, "kind": "port", "sample": sample}
         line = {
