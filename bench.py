@@ -419,7 +419,7 @@ def main():
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--form", default="batched", choices=["batched", "plain"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--ref-instances", type=int, default=4)
+    ap.add_argument("--ref-instances", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--config", default="c2", choices=["c2", "c4"])
     ap.add_argument("--n-instances", type=int, default=4096)
