@@ -139,36 +139,75 @@ int orc_unfold(const orc_problem *p, int64_t pad[3][2], int64_t str[3]) {
 }
 
 /* ------------------------------------------------------------ padding --- */
-/* Whole-hyperplane operations along `dim` of a contiguous buffer of shape L
- * with nc doubles per element (1 real, 2 complex): ndarray's
- * index_axis_mut(Axis(dim), j).fill / .assign used by half_dim.rs. */
-typedef struct { double *buf; int rank; const int64_t *L; int nc; } hbuf;
+/* Whole-hyperplane operations along `dim` of a buffer whose logical extents
+ * are L and whose elements sit at the element strides of a possibly larger
+ * allocation (the FFT-sized buffer of padding_in); an element is nc values
+ * of vbytes bytes (8: double, 4: float).  These are ndarray's
+ * index_axis_mut(Axis(dim), j).fill / .assign used by half_dim.rs.  Axes are
+ * held in canonical three-axis form (leading extents 1). */
+typedef struct {
+    unsigned char *buf;
+    int off;          /* 3 - rank: canonical index of axis 0 */
+    long L[3];        /* logical extents */
+    long st[3];       /* element strides of the allocation */
+    int nc, vbytes;
+} hbuf;
 
-static void hp_geom(const hbuf *b, int dim, long *outer, long *inner) {
-    *outer = prod(b->L, dim);
-    *inner = prod(b->L + dim + 1, b->rank - dim - 1) * b->nc;
+static void hb_init(hbuf *b, void *buf, int rank, const int64_t *L, const int64_t *alloc, int nc,
+                    int vbytes) {
+    long A[3];
+    b->buf = (unsigned char *)buf;
+    b->off = 3 - rank;
+    to3(L, rank, 1, b->L);
+    to3(alloc, rank, 1, A);
+    b->st[2] = 1;
+    b->st[1] = A[2];
+    b->st[0] = A[1] * A[2];
+    b->nc = nc;
+    b->vbytes = vbytes;
 }
+static size_t hb_esz(const hbuf *b) { return (size_t)b->nc * (size_t)b->vbytes; }
+static long hb_len(const hbuf *b, int dim) { return b->L[dim + b->off]; }
+static unsigned char *hb_at(const hbuf *b, long i0, long i1, long i2) {
+    return b->buf + (size_t)(i0 * b->st[0] + i1 * b->st[1] + i2 * b->st[2]) * hb_esz(b);
+}
+
 static void hp_fill(const hbuf *b, int dim, long j, const double *c) {
-    long outer, inner;
-    hp_geom(b, dim, &outer, &inner);
-    long Ld = b->L[dim];
-    for (long o = 0; o < outer; o++) {
-        double *d = b->buf + (o * Ld + j) * inner;
-        for (long i = 0; i < inner; i++) d[i] = c[i % b->nc];
+    unsigned char pat[16];
+    for (int k = 0; k < b->nc; k++) {
+        if (b->vbytes == 8) { double v = c[k]; memcpy(pat + 8 * k, &v, 8); }
+        else { float v = (float)c[k]; memcpy(pat + 4 * k, &v, 4); }
     }
+    const size_t esz = hb_esz(b);
+    const int d = dim + b->off;
+    long lo[3] = {0, 0, 0}, hi[3] = {b->L[0], b->L[1], b->L[2]};
+    lo[d] = j;
+    hi[d] = j + 1;
+    for (long i0 = lo[0]; i0 < hi[0]; i0++)
+        for (long i1 = lo[1]; i1 < hi[1]; i1++)
+            for (long i2 = lo[2]; i2 < hi[2]; i2++) memcpy(hb_at(b, i0, i1, i2), pat, esz);
 }
 static void hp_copy(const hbuf *b, int dim, long dst, long src) {
-    long outer, inner;
-    hp_geom(b, dim, &outer, &inner);
-    long Ld = b->L[dim];
-    for (long o = 0; o < outer; o++)
-        memcpy(b->buf + (o * Ld + dst) * inner, b->buf + (o * Ld + src) * inner,
-               sizeof(double) * inner);
+    const size_t esz = hb_esz(b);
+    const int d = dim + b->off;
+    long hi[3] = {b->L[0], b->L[1], b->L[2]};
+    hi[d] = 1;
+    for (long i0 = 0; i0 < hi[0]; i0++)
+        for (long i1 = 0; i1 < hi[1]; i1++) {
+            if (d == 2) {
+                memmove(hb_at(b, i0, i1, dst), hb_at(b, i0, i1, src), esz);
+            } else {
+                /* whole rows along the contiguous last axis */
+                long a0 = i0, a1 = i1, s0 = i0, s1 = i1;
+                if (d == 0) { a0 = dst; s0 = src; } else { a1 = dst; s1 = src; }
+                memmove(hb_at(b, a0, a1, 0), hb_at(b, s0, s1, 0), esz * (size_t)b->L[2]);
+            }
+        }
 }
 
 /* half_dim.rs:30-343, one side of one axis; n = input extent on that axis */
 static int half_front(const hbuf *b, int dim, long n, const int64_t pd[2], int kind, const double *c) {
-    long L = b->L[dim], p0 = pd[0];
+    long L = hb_len(b, dim), p0 = pd[0];
     (void)n;
     switch (kind) {
     case BT_ZEROS: { double z[2] = {0, 0}; for (long j = 0; j < p0; j++) hp_fill(b, dim, j, z); break; }
@@ -189,7 +228,7 @@ static int half_front(const hbuf *b, int dim, long n, const int64_t pd[2], int k
     return ORC_OK;
 }
 static int half_back(const hbuf *b, int dim, long n, const int64_t pd[2], int kind, const double *c) {
-    long L = b->L[dim], p0 = pd[0];
+    long L = hb_len(b, dim), p0 = pd[0];
     long border = L - pd[1] - 1;
     switch (kind) {
     case BT_ZEROS: { double z[2] = {0, 0}; for (long j = n + p0; j < L; j++) hp_fill(b, dim, j, z); break; }
@@ -207,6 +246,37 @@ static int half_back(const hbuf *b, int dim, long n, const int64_t pd[2], int ki
     default: return ORC_INVALID;
     }
     return ORC_OK;
+}
+
+/* The per-axis border passes of PaddingExt::padding (fft_style = 0,
+ * src/padding/mod.rs:84-117; Const was pre-filled) and padding_in
+ * (fft_style = 1, mod.rs:119-153; Const filled per side), on a buffer that
+ * already holds the input at [p0, p0 + n) on every axis: axes 0..rank-1 in
+ * order, front side then back side. */
+static int pad_passes(const orc_problem *p, const int64_t pad[3][2], const hbuf *b, int fft_style) {
+    int st = ORC_OK;
+    for (int d = 0; d < p->rank && st == ORC_OK; d++) {
+        long n = p->xs[d];
+        int kf, kb;
+        const double *cf = NULL, *cb = NULL;
+        switch (p->pmode) {
+        case PM_ZEROS: continue;
+        case PM_CONST:
+            if (!fft_style) continue;           /* pre-filled instead */
+            kf = kb = BT_CONST; cf = cb = p->cval; break;
+        case PM_REFLECT: kf = kb = BT_REFLECT; break;
+        case PM_REPLICATE: kf = kb = BT_REPLICATE; break;
+        case PM_CIRCULAR: kf = kb = BT_CIRCULAR; break;
+        case PM_CUSTOM: kf = kb = p->kinds[d][0]; cf = cb = p->vals[d][0]; break;
+        case PM_EXPLICIT:
+            kf = p->kinds[d][0]; kb = p->kinds[d][1]; cf = p->vals[d][0]; cb = p->vals[d][1];
+            break;
+        default: return ORC_INVALID;
+        }
+        st = half_front(b, d, n, pad[d], kf, cf);
+        if (st == ORC_OK) st = half_back(b, d, n, pad[d], kb, cb);
+    }
+    return st;
 }
 
 /* PaddingExt::padding (fft_style = 0, src/padding/mod.rs:84-117) and
@@ -236,30 +306,9 @@ int orc_padding(const orc_problem *p, const int64_t pad[3][2], const double *x, 
                 memcpy(out + (((i0 + p3[0]) * L3[1] + (i1 + p3[1])) * L3[2] + p3[2]) * nc,
                        x + ((i0 * n3[1] + i1) * n3[2]) * nc, sizeof(double) * (size_t)(n3[2] * nc));
     }
-    hbuf b = {out, rank, L, nc};
-    int st = ORC_OK;
-    for (int d = 0; d < rank && st == ORC_OK; d++) {
-        long n = p->xs[d];
-        int kf, kb;
-        const double *cf = NULL, *cb = NULL;
-        switch (p->pmode) {
-        case PM_ZEROS: continue;
-        case PM_CONST:
-            if (!fft_style) continue;           /* pre-filled instead */
-            kf = kb = BT_CONST; cf = cb = p->cval; break;
-        case PM_REFLECT: kf = kb = BT_REFLECT; break;
-        case PM_REPLICATE: kf = kb = BT_REPLICATE; break;
-        case PM_CIRCULAR: kf = kb = BT_CIRCULAR; break;
-        case PM_CUSTOM: kf = kb = p->kinds[d][0]; cf = cb = p->vals[d][0]; break;
-        case PM_EXPLICIT:
-            kf = p->kinds[d][0]; kb = p->kinds[d][1]; cf = p->vals[d][0]; cb = p->vals[d][1];
-            break;
-        default: return ORC_INVALID;
-        }
-        st = half_front(&b, d, n, pad[d], kf, cf);
-        if (st == ORC_OK) st = half_back(&b, d, n, pad[d], kb, cb);
-    }
-    return st;
+    hbuf b;
+    hb_init(&b, out, rank, L, L, nc, (int)sizeof(double));
+    return pad_passes(p, pad, &b, fft_style);
 }
 
 /* ------------------------------------------------------------ offsets --- */

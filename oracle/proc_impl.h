@@ -286,28 +286,33 @@ static int FN(conv_fft)(const orc_problem *p, int is_complex, const REAL *x, con
     if (!y) return ORC_OK;
 
     long nx = prod(p->xs, rank), nk = prod(p->ks, rank), npd = prod(pds, rank), nF = prod(F, rank);
-    /* padding::data (conv_fft/padding.rs:30-62) */
-    double *xd = malloc(sizeof(double) * nx * nc), *pd = malloc(sizeof(double) * npd * nc);
-    for (long i = 0; i < nx * nc; i++) xd[i] = (double)x[i];
-    st = orc_padding(p, pad, xd, nc, 1, pd);
-    free(xd);
-    if (st) { free(pd); return st; }
     REAL *dbuf = calloc(nF * nc, sizeof(REAL)), *kbuf = calloc(nF * nc, sizeof(REAL));
     /* canonical three-axis forms (leading extents 1) for the row loops below */
-    long P3[3], F3[3], K3[3], D3[3], E3[3];
-    to3(pds, rank, 1, P3);
+    long X3[3], F3[3], K3[3], D3[3], E3[3], Q3[3] = {0, 0, 0};
+    to3(p->xs, rank, 1, X3);
     to3(F, rank, 1, F3);
     to3(p->ks, rank, 1, K3);
     to3(p->dil, rank, 1, D3);
     to3(ke, rank, 1, E3);
+    for (int i = 0; i < rank; i++) Q3[3 - rank + i] = pad[i][0];
     (void)npd;
-    for (long i0 = 0; i0 < P3[0]; i0++)
-        for (long i1 = 0; i1 < P3[1]; i1++) {
-            const double *src = pd + ((i0 * P3[1] + i1) * P3[2]) * nc;
-            REAL *dst = dbuf + ((i0 * F3[1] + i1) * F3[2]) * nc;
-            for (long j = 0; j < P3[2] * nc; j++) dst[j] = (REAL)src[j];
+    (void)nx;
+    /* padding::data (conv_fft/padding.rs:30-62): padding_in on the [0, pds)
+     * box of the zeroed FFT buffer: the input at [p0, p0 + n) on every axis,
+     * then the border passes axis by axis */
+    for (long i0 = 0; i0 < X3[0]; i0++)
+        for (long i1 = 0; i1 < X3[1]; i1++)
+            memcpy(dbuf + (((i0 + Q3[0]) * F3[1] + (i1 + Q3[1])) * F3[2] + Q3[2]) * nc,
+                   x + ((i0 * X3[1] + i1) * X3[2]) * nc, sizeof(REAL) * (size_t)(X3[2] * nc));
+    {
+        hbuf b;
+        hb_init(&b, dbuf, rank, pds, F, nc, (int)sizeof(REAL));
+        if ((st = pad_passes(p, pad, &b, 1))) {
+            free(dbuf);
+            free(kbuf);
+            return st;
         }
-    free(pd);
+    }
     /* padding::kernel (conv_fft/padding.rs:78-111): buf[i*d] = k[i], or at
      * k_eff-1-i*d (negative slice step) when !reverse */
     (void)nk;
