@@ -245,6 +245,42 @@ def test_processor_layout_vs_numpy(shape):
     np.testing.assert_allclose(O.fft_backward(O.DT_C64, specc, 0), xc, atol=1e-10)
 
 
+@pytest.mark.parametrize("shape", [(37, 60), (21, 210), (3, 37, 30), (6, 35, 18)])
+def test_processor_layout_vs_numpy_f32(shape):
+    """The single-precision instantiation of the same transforms (the one the
+    timed CPU baseline runs), batched over many rows."""
+    rng = np.random.default_rng(len(shape) + shape[-1])
+    x = rng.standard_normal(shape)
+    perm = {2: (1, 0), 3: (1, 2, 0)}[len(shape)]
+    spec, ol = O.fft_forward(O.DT_F32, x.astype(np.float32))
+    ref = np.transpose(np.fft.rfftn(x), perm)
+    assert np.linalg.norm(spec - ref) / np.linalg.norm(ref) < 1e-6
+    back = O.fft_backward(O.DT_F32, spec, ol)
+    assert np.abs(back - x).max() < 1e-5
+    xc = x + 1j * rng.standard_normal(shape)
+    specc, _ = O.fft_forward(O.DT_C32, xc.astype(np.complex64))
+    refc = np.transpose(np.fft.fftn(xc), perm)
+    assert np.linalg.norm(specc - refc) / np.linalg.norm(refc) < 1e-6
+
+
+def test_fft_conv_f32_many_rows_vs_direct():
+    """conv_fft in f32 on a case with many rows (batched transforms) against
+    the f64 direct loop, with every border kind on one axis or the other."""
+    rng = np.random.default_rng(11)
+    x = rng.random((64, 300))
+    k = rng.random((7, 9))
+    for pm in (PaddingMode.Zeros, PaddingMode.Reflect, PaddingMode.Circular, PaddingMode.Replicate,
+               PaddingMode.Const(0.5)):
+        kw = with_dilation(k, 2)
+        st, y64 = O.conv(problem(F64, x, kw, ConvMode.Same, pm), x, k)
+        assert st == 0
+        for nth in (1, 4):
+            st, y32 = O.conv_fft(problem(F32, x, kw, ConvMode.Same, pm), x.astype(np.float32),
+                                 k.astype(np.float32), nth)
+            assert st == 0
+            assert np.linalg.norm(y32 - y64) / np.linalg.norm(y64) < 1e-5, (pm, nth)
+
+
 # ---- FFT conv vs direct conv: src/conv_fft/tests.rs:151-618, 799-857 ----------------------
 def fft_vs_direct(x, kw, mode, pmode, dt, tol):
     x = np.array(x)
