@@ -136,28 +136,36 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(seconds=10.0, nthreads=None):
-    """The oracle port of conv_fft_par on the host cores, one instance per
-    call, repeated for ~`seconds`.  Returns (GB/s, cores, sample text)."""
+def cpu_baseline(seconds=10.0, nthreads=None, algo="fft"):
+    """The oracle port on the host cores, one instance per call, repeated for
+    ~`seconds`: conv_fft_par on all cores for the FFT line, the crate's
+    single-threaded direct loop (ConvExt::conv) for the direct line.
+    Returns (GB/s, cores, sample text)."""
     from oracle import oracle as O
     from ndconv import _abi, build_problem, with_dilation
     mode, pm, _ = problem_args()
-    nthreads = nthreads or os.cpu_count() or 1
+    direct = algo == "direct"
+    nthreads = 1 if direct else (nthreads or os.cpu_count() or 1)
     rng = np.random.default_rng(12345)
     x = rng.random(SHAPE_X).astype(np.float32)
     k = rng.random(SHAPE_K).astype(np.float32)
     p = build_problem(_abi.F32, SHAPE_X, with_dilation(k, DIL), mode, pm)
-    st, y = O.conv_fft(p, x, k, nthreads)  # warm-up
+
+    def once():
+        return O.conv(p, x, k) if direct else O.conv_fft(p, x, k, nthreads)
+
+    st, y = once()  # warm-up
     assert st == 0
     n, t0 = 0, time.perf_counter()
     while True:
-        O.conv_fft(p, x, k, nthreads)
+        once()
         n += 1
         el = time.perf_counter() - t0
         if el >= seconds:
             break
     gbs = algorithmic_bytes(y.shape) * n / el / 1e9
-    return gbs, nthreads, f"{n} instances of x[200,5000]*k[11,31] (conv_fft_par port, f32) in {el:.1f} s"
+    what = "conv port, direct loop, 1 thread" if direct else "conv_fft_par port"
+    return gbs, nthreads, f"{n} instances of x[200,5000]*k[11,31] ({what}, f32) in {el:.1f} s"
 
 
 def run_reference(args, rank, world):
@@ -593,7 +601,7 @@ def main():
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline and world == 1:  # host-core baseline at N = 1 only
-            gbs, cores, sample = cpu_baseline(args.cpu_seconds)
+            gbs, cores, sample = cpu_baseline(args.cpu_seconds, algo=args.algo)
             cpu = {"value": gbs, "unit": "GB/s", "cores": cores, "kind": "port", "sample": sample}
         line = {
             "metric": METRIC,
