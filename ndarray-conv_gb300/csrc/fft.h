@@ -39,17 +39,23 @@ int proc_backward(ndconv_fft_processor *proc, int rank, const int64_t *spec_shap
                   cudaStream_t st);
 
 bool make_plan(int L, FftPlanDev &pl);
+// relative cost of one Stockham stage per element, by radix
+double stage_cost(int r);
+// Twiddle table on the current device (cached per length, or carved from
+// the calling thread's TwArena): kind 0: tw[t] = exp(-2 pi i t / L);
+// kind 1: the stage table of *pl (make_plan(L)).
+template <typename C> int get_twiddles(int L, const C **out, int kind = 0, const FftPlanDev *pl = nullptr);
 
 // Optional home for twiddle tables: while a TwArenaScope is alive on the
 // calling thread, tables are carved from `base` and generated on `st`
 // instead of the process-wide cache (which allocates and synchronises).
 struct TwArena {
-    static constexpr int kMaxTables = 8;
+    static constexpr int kMaxTables = 16;
     unsigned char *base;
     size_t cap, used;
     cudaStream_t st;
     int n;
-    int len[kMaxTables], elem[kMaxTables];
+    int len[kMaxTables], elem[kMaxTables], kind[kMaxTables];
     void *table[kMaxTables];
 };
 struct TwArenaScope {

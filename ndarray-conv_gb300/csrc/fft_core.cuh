@@ -6,8 +6,10 @@
 // two buffers: butterfly j reads buf[j + r L/R], applies the twiddles
 // w^(r * (j mod Ns)) with w = exp(-+2 pi i / (Ns R)), does a radix-R DFT in
 // registers and writes to (j / Ns) Ns R + (j mod Ns) + r Ns.  After all
-// stages the result is in natural order.  Twiddles come from a table
-// tw[t] = exp(-2 pi i t / L) evaluated in FP64 on the GPU and rounded once.
+// stages the result is in natural order.  Twiddles come from tables
+// evaluated in FP64 on the GPU and rounded once: per stage, the rows
+// w^(t r) (t < Ns, r < R) that one butterfly applies, loaded as vectors; the
+// generic odd-prime stage uses tw[t] = exp(-2 pi i t / L).
 #pragma once
 #include "common.cuh"
 
@@ -17,7 +19,7 @@ template <typename R> struct CplxT;
 template <> struct CplxT<float> { using type = c32; };
 template <> struct CplxT<double> { using type = c64; };
 
-constexpr int kMaxStages = 40;
+constexpr int kMaxStages = 24;
 constexpr int kMaxGenericRadix = 64;
 
 // n / d for n < 2^31 with a precomputed multiplier: q = umulhi(n, m) >> s
@@ -44,6 +46,12 @@ struct FftPlanDev {
     int nst;
     int rad[kMaxStages];
     FastDiv ns[kMaxStages];  // Ns (product of the previous radices) per stage
+    // stage twiddle table: stage s >= 1 holds the Ns x R entries
+    // w^(t r), w = exp(-2 pi i / (Ns R)), at tws[twoff[s] + t R + r]
+    // (twoff even, so that bin pairs load as one 16-byte vector)
+    int twoff[kMaxStages];
+    int twn;          // entries of the table
+    const void *tws;  // the table on the device (element type of the transform)
 };
 
 // Shared-memory slot of logical element u: one padding slot after every
@@ -244,14 +252,48 @@ __device__ __forceinline__ C twiddle(const C *__restrict__ tw, int e) {
     return INV ? cconj(w) : w;
 }
 
-// One radix-R Stockham stage over nb interleaved transforms.
+// The R - 1 twiddles w^(t r), r = 1..R-1, of a butterfly from its row of the
+// stage table (conjugated for the inverse).  Even radices load entry pairs
+// as 16-byte vectors (the row's first entry, w^0, is loaded and unused).
+template <bool INV, int RAD, typename C>
+__device__ __forceinline__ void stage_twiddles(C (&w)[RAD], const C *__restrict__ row) {
+    if constexpr (sizeof(C) == 8 && RAD % 2 == 0) {
+        const float4 *p = reinterpret_cast<const float4 *>(row);
+#pragma unroll
+        for (int h = 0; h < RAD / 2; h++) {
+            const float4 v = __ldg(p + h);
+            w[2 * h] = C{v.x, INV ? -v.y : v.y};
+            w[2 * h + 1] = C{v.z, INV ? -v.w : v.w};
+        }
+    } else {
+#pragma unroll
+        for (int r = 1; r < RAD; r++) {
+            const C v = ldg_c(row + r);
+            w[r] = INV ? cconj(v) : v;
+        }
+    }
+}
+
+// One radix-R Stockham stage over nb interleaved transforms.  Butterfly j
+// (of transform b) reads logical elements u + r si (u = j nb + b,
+// si = (L / R) nb) and writes uo + r so (so = Ns nb).  When a stride is a
+// multiple of the padded wavefront (16 c32 / 8 c64 elements), or a
+// butterfly's outputs stay inside one wavefront, the padded slot of element
+// r is the first one's plus r times a fixed step, so each access is one add
+// away from the last.
 template <bool INV, int RAD, typename C>
 __device__ __forceinline__ void stockham_stage(const C *src, C *dst, int L, int nb, int lognb,
-                                               const FastDiv &nsd, const C *__restrict__ tw) {
+                                               const FastDiv &nsd, const C *__restrict__ tws) {
     const int Ns = (int)nsd.d;
     const int nr = L / RAD;
-    const int twstep = L / (Ns * RAD);
     const int total = nr << lognb;
+    constexpr int kWf = sizeof(C) <= 8 ? 16 : 8;  // elements per padded wavefront (see sx)
+    constexpr int kSh = sizeof(C) <= 8 ? 4 : 3;
+    const int si = total, so = Ns << lognb;
+    const bool lin_i = (si & (kWf - 1)) == 0;
+    const bool lin_o = (so & (kWf - 1)) == 0 || (kWf % (RAD * so)) == 0;
+    const int psi = si + (si >> kSh);                             // padded input step (lin_i)
+    const int pso = (so & (kWf - 1)) == 0 ? so + (so >> kSh) : so;  // padded output step (lin_o)
 #pragma unroll 2
     for (int u = threadIdx.x; u < total; u += blockDim.x) {
         const int b = u & (nb - 1);
@@ -259,15 +301,17 @@ __device__ __forceinline__ void stockham_stage(const C *src, C *dst, int L, int 
         const int q = (int)fdiv((uint32_t)j, nsd);
         const int t = j - q * Ns;
         C v[RAD];
+        if (lin_i) {
+            const C *s0 = src + sx<C>(u);
 #pragma unroll
-        for (int r = 0; r < RAD; r++) v[r] = src[sx<C>(((j + r * nr) << lognb) + b)];
+            for (int r = 0; r < RAD; r++) v[r] = s0[r * psi];
+        } else {
+#pragma unroll
+            for (int r = 0; r < RAD; r++) v[r] = src[sx<C>(u + r * si)];
+        }
         if (t) {
-            // one table load per butterfly; the other powers by products in
-            // a log-depth tree (w^k from at most three rounded products)
             C w[RAD];
-            w[1] = twiddle<INV>(tw, t * twstep);
-#pragma unroll
-            for (int r = 2; r < RAD; r++) w[r] = (r & 1) ? cmul(w[r - 1], w[1]) : cmul(w[r / 2], w[r / 2]);
+            stage_twiddles<INV, RAD>(w, tws + t * RAD);
 #pragma unroll
             for (int r = 1; r < RAD; r++) v[r] = cmul(v[r], w[r]);
         }
@@ -279,9 +323,15 @@ __device__ __forceinline__ void stockham_stage(const C *src, C *dst, int L, int 
         else if constexpr (RAD == 8) dft8<INV>(v);
         else if constexpr (RAD == 10) dft10<INV>(v);
         else if constexpr (RAD == 16) dft16<INV>(v);
-        const int base = q * Ns * RAD + t;
+        const int uo = ((q * Ns * RAD + t) << lognb) + b;
+        if (lin_o) {
+            C *d0 = dst + sx<C>(uo);
 #pragma unroll
-        for (int r = 0; r < RAD; r++) dst[sx<C>(((base + r * Ns) << lognb) + b)] = v[r];
+            for (int r = 0; r < RAD; r++) d0[r * pso] = v[r];
+        } else {
+#pragma unroll
+            for (int r = 0; r < RAD; r++) dst[sx<C>(uo + r * so)] = v[r];
+        }
     }
 }
 
@@ -320,17 +370,19 @@ __device__ void stockham_stage_generic(const C *src, C *dst, int L, int nb, int 
 template <bool INV, typename C>
 __device__ C *block_fft(C *a, C *b, int nb, int lognb, const FftPlanDev &pl, const C *__restrict__ tw) {
     C *src = a, *dst = b;
+    const C *__restrict__ tws = static_cast<const C *>(pl.tws);
     for (int s = 0; s < pl.nst; s++) {
         const int R = pl.rad[s];
+        const C *tr = tws + pl.twoff[s];
         switch (R) {
-        case 2: stockham_stage<INV, 2>(src, dst, pl.L, nb, lognb, pl.ns[s], tw); break;
-        case 3: stockham_stage<INV, 3>(src, dst, pl.L, nb, lognb, pl.ns[s], tw); break;
-        case 4: stockham_stage<INV, 4>(src, dst, pl.L, nb, lognb, pl.ns[s], tw); break;
-        case 5: stockham_stage<INV, 5>(src, dst, pl.L, nb, lognb, pl.ns[s], tw); break;
-        case 7: stockham_stage<INV, 7>(src, dst, pl.L, nb, lognb, pl.ns[s], tw); break;
-        case 8: stockham_stage<INV, 8>(src, dst, pl.L, nb, lognb, pl.ns[s], tw); break;
-        case 10: stockham_stage<INV, 10>(src, dst, pl.L, nb, lognb, pl.ns[s], tw); break;
-        case 16: stockham_stage<INV, 16>(src, dst, pl.L, nb, lognb, pl.ns[s], tw); break;
+        case 2: stockham_stage<INV, 2>(src, dst, pl.L, nb, lognb, pl.ns[s], tr); break;
+        case 3: stockham_stage<INV, 3>(src, dst, pl.L, nb, lognb, pl.ns[s], tr); break;
+        case 4: stockham_stage<INV, 4>(src, dst, pl.L, nb, lognb, pl.ns[s], tr); break;
+        case 5: stockham_stage<INV, 5>(src, dst, pl.L, nb, lognb, pl.ns[s], tr); break;
+        case 7: stockham_stage<INV, 7>(src, dst, pl.L, nb, lognb, pl.ns[s], tr); break;
+        case 8: stockham_stage<INV, 8>(src, dst, pl.L, nb, lognb, pl.ns[s], tr); break;
+        case 10: stockham_stage<INV, 10>(src, dst, pl.L, nb, lognb, pl.ns[s], tr); break;
+        case 16: stockham_stage<INV, 16>(src, dst, pl.L, nb, lognb, pl.ns[s], tr); break;
         default: stockham_stage_generic<INV>(src, dst, pl.L, nb, lognb, pl.ns[s], R, tw); break;
         }
         __syncthreads();
