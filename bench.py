@@ -1,19 +1,27 @@
 """Benchmark: convolution GB/s and % of HBM roofline on one GB300.
 
-Workload (the reference's 2-D benchmark case, batched): B
+Headline workload (the reference's 2-D benchmark case, batched): B = 64
 independent instances of a 2-D f32 convolution x[200, 5000] with a kernel
 [11, 31] dilated by 2, ConvMode::Same, PaddingMode::Custom([Reflect,
-Circular]); every instance has its own seeded Uniform[0,1) data and kernel.
-A step is one pass of conv_fft (default) or conv over all B instances.
-B = 64 makes the inputs (256 MB) larger than L2, so no flush is needed.
+Circular]); every instance has its own seeded Uniform[0,1) data and kernel
+(numpy PCG64, seed 1000 + rank, the same instances in both arms).  A step is
+one pass of conv_fft over all B instances.  B = 64 makes the inputs (256 MB)
+larger than L2, so no flush is needed.
 
 Metric: algorithmic bytes 4 * (|x| + |k| + |y|) per instance / time.
   value   device-resident inputs, CUDA-event timed (max over ranks)
-  e2e     the same calls with pinned-host inputs: H2D copy + conv + D2H of
-          the outputs inside the timed region
+  e2e     the library's host-memory batch entry point: pinned-host inputs,
+          H2D copy + conv + D2H of the outputs inside the timed region
+The default line also carries, in `config`:
+  direct        the same 64 instances through conv (direct FP32), with its
+                FP32 FMA roofline and the i32 copy's bit-exactness
+  uneven_batch  the uneven batch (4096 instances, one persistent launch +
+                CUDA graph, dispatcher-picked variants) against the plain
+                drop-in (per-instance calls with the library's default picks)
 Reference arm (--impl reference): the oracle port of conv_fft_par (same
-algorithm as the crate, rayon-style threads on all host cores) on a
-bounded sample of the same workload.
+algorithm as the crate, rayon-style threads on all host cores) over the
+same 64 instances per step.  The GPU line's cpu_baseline is that arm run as
+a fresh process for ~--cpu-seconds.
 """
 import argparse
 import ctypes
@@ -30,9 +38,11 @@ sys.path[:0] = [ROOT, os.path.join(ROOT, "ndarray-conv_gb300")]
 
 import numpy as np  # noqa: E402
 
-# DRAM bytes per instance of the batched FFT path from one ncu capture (one
-# wave of 16 instances, caches flushed between the two launches): an upper bound
-PROFILED_TRAFFIC = {"fft": 12.27e6}
+# DRAM bytes (read + write) per instance of the batched FFT path, from one
+# ncu capture of the timed workload: one 64-instance wave (the two row-pass
+# launches of one step), profiles/conv_fft_2d_200x5000_k11x31_batch64_traffic.md
+PROFILED_TRAFFIC = {"fft": 17.594e6}
+PROFILED_TRAFFIC_SOURCE = "profiles/conv_fft_2d_200x5000_k11x31_batch64_traffic.md"
 
 # the benchmark's metric; every line (both arms, both workloads) reports it
 METRIC = "conv GB/s & % HBM roofline, batched+tuned vs plain GPU, err ≤1e-5 vs FP64"
@@ -41,6 +51,22 @@ METRIC_DETAIL = "GB/s of algorithmic bytes 4*(|x|+|k|+|y|) per instance"
 SHAPE_X = (200, 5000)
 SHAPE_K = (11, 31)
 DIL = 2
+SEED_C2 = 1000  # + rank
+WORKLOAD_C2 = ("{B} x 2-D f32 x[200,5000] * k[11,31] dilation 2, Same, Custom([Reflect, Circular]); "
+               "{what}, {form} submission")
+
+
+def c2_inputs(B, seed, dtype=np.float32):
+    """The headline workload's instances: B seeded Uniform[0,1) data and
+    kernels (i32: Uniform{-100..100}), identical in both arms."""
+    rng = np.random.default_rng(seed)
+    if dtype == np.int32:
+        xs = [rng.integers(-100, 101, SHAPE_X, dtype=np.int32) for _ in range(B)]
+        ks = [rng.integers(-100, 101, SHAPE_K, dtype=np.int32) for _ in range(B)]
+    else:
+        xs = [rng.random(SHAPE_X, dtype=np.float32) for _ in range(B)]
+        ks = [rng.random(SHAPE_K, dtype=np.float32) for _ in range(B)]
+    return xs, ks
 
 
 def algorithmic_bytes(out_shape):
@@ -136,69 +162,59 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(seconds=10.0, nthreads=None, algo="fft"):
-    """The oracle port on the host cores, one instance per call, repeated for
-    ~`seconds`: conv_fft_par on all cores for the FFT line, the crate's
-    single-threaded direct loop (ConvExt::conv) for the direct line.
-    Returns (GB/s, cores, sample text)."""
-    from oracle import oracle as O
-    from ndconv import _abi, build_problem, with_dilation
-    mode, pm, _ = problem_args()
-    direct = algo == "direct"
-    nthreads = 1 if direct else (nthreads or os.cpu_count() or 1)
-    rng = np.random.default_rng(12345)
-    x = rng.random(SHAPE_X).astype(np.float32)
-    k = rng.random(SHAPE_K).astype(np.float32)
-    p = build_problem(_abi.F32, SHAPE_X, with_dilation(k, DIL), mode, pm)
-
-    def once():
-        return O.conv(p, x, k) if direct else O.conv_fft(p, x, k, nthreads)
-
-    st, y = once()  # warm-up
-    assert st == 0
-    n, t0 = 0, time.perf_counter()
-    while True:
-        once()
-        n += 1
-        el = time.perf_counter() - t0
-        if el >= seconds:
-            break
-    gbs = algorithmic_bytes(y.shape) * n / el / 1e9
-    what = "conv port, direct loop, 1 thread" if direct else "conv_fft_par port"
-    return gbs, nthreads, f"{n} instances of x[200,5000]*k[11,31] ({what}, f32) in {el:.1f} s"
+def cpu_baseline(seconds, batch):
+    """The reference arm (the oracle port of conv_fft_par over the same
+    instances) run as a fresh process for ~`seconds`, so that its figure is
+    the arm's own and no thread of this GPU process competes for the cores."""
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1000000",
+           "--warmup", "1", "--batch", str(batch), "--ref-seconds", str(seconds)]
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env, timeout=600)
+    if r.returncode:
+        return None
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    cb = dict(line["cpu_baseline"])
+    cb["value"] = line["value"]
+    return cb
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the oracle port of conv_fft_par (threads on all
+    host cores) over the headline workload's instances, each step one pass
+    over all of them.  Rank 0 only."""
     if rank != 0:
         return
     steps, warm = args.steps, args.warmup
-    # each step: a bounded sample (--ref-instances instances) of the workload
     from oracle import oracle as O
     from ndconv import _abi, build_problem, with_dilation
     mode, pm, _ = problem_args()
     nth = os.cpu_count() or 1
-    rng = np.random.default_rng(12345)
-    x = rng.random(SHAPE_X).astype(np.float32)
-    k = rng.random(SHAPE_K).astype(np.float32)
-    p = build_problem(_abi.F32, SHAPE_X, with_dilation(k, DIL), mode, pm)
-    for _ in range(max(1, warm)):
-        st, y = O.conv_fft(p, x, k, nth)
-    per_step = max(1, int(args.ref_instances))
+    B = args.batch
+    xs, ks = c2_inputs(B, SEED_C2)
+    p = build_problem(_abi.F32, SHAPE_X, with_dilation(ks[0], DIL), mode, pm)
+    for w in range(max(1, warm)):
+        st, y = O.conv_fft(p, xs[w % B], ks[w % B], nth)
+        assert st == 0
     t0 = time.perf_counter()
+    done = 0
     for _ in range(steps):
-        for _ in range(per_step):
-            O.conv_fft(p, x, k, nth)
+        for i in range(B):
+            O.conv_fft(p, xs[i], ks[i], nth)
+        done += 1
+        if args.ref_seconds and time.perf_counter() - t0 >= args.ref_seconds:
+            break
     el = time.perf_counter() - t0
-    gbs = algorithmic_bytes(y.shape) * per_step * steps / el / 1e9
-    sample = f"{per_step} instance(s) of x[200,5000]*k[11,31] per step (conv_fft_par port, f32)"
+    gbs = algorithmic_bytes(y.shape) * B * done / el / 1e9
+    sample = (f"{B} distinct instances of x[200,5000]*k[11,31] per step, {done} step(s) in {el:.1f} s "
+              f"(conv_fft_par port, f32)")
     line = {"metric": METRIC,
-            "value": gbs, "unit": "GB/s", "n_gpus": world, "steps": steps, "warmup": warm,
-            "ms_per_step": el / steps * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Uniform[0,1))",
+            "value": gbs, "unit": "GB/s", "n_gpus": world, "steps": done, "warmup": warm,
+            "ms_per_step": el / done * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": f"synthetic (seeded Uniform[0,1), distinct data and kernel per instance, seed {SEED_C2})",
             "impl": "reference",
-            "config": {"workload": "2-D f32 x[200,5000] * k[11,31] dilation 2, Same, "
-                                   "Custom([Reflect, Circular]); conv_fft",
-                       "metric_detail": METRIC_DETAIL},
+            "config": {"workload": WORKLOAD_C2.format(B=B, what="conv_fft", form="batched"),
+                       "metric_detail": METRIC_DETAIL, "batch_per_gpu": B},
             "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": nth, "kind": "port", "sample": sample},
             "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -217,18 +233,12 @@ def flat_views(shapes, dtype, device):
     return buf, views
 
 
-def bench_uneven(args, world, rank, local_rank):
+def measure_uneven(args, world, rank, local_rank, dist):
     """The uneven batch: independent instances in one persistent
     launch (device work queue, CUDA graph), against the same instances
-    through the per-instance entry points (the plain drop-in)."""
+    through the per-instance entry points (the plain drop-in).  Returns the
+    figures of this rank (times max-reduced over ranks)."""
     import torch
-    import __graft_entry__ as g
-    g.build()
-    torch.cuda.set_device(local_rank)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
     from ndconv import _abi, with_dilation
     from ndconv import workloads as W
     from ndconv import shard
@@ -329,65 +339,80 @@ def bench_uneven(args, world, rank, local_rank):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms, plain_ms, e2e_ms, dropin_ms = [float(v) for v in t.tolist()]
     bytes_step = sum(s.bytes() for s in specs)
-    peak, peak_kind = peaks()
-    value = bytes_step * world / (ms * 1e-3) / 1e9
-    # parity spot checks against the f64 oracle (largest direct and FFT instances that stay cheap)
+    # parity spot checks against the f64 oracle: a seeded sample of direct and
+    # FFT instances (the f64 FFT oracle where the direct loop is too slow)
     from oracle import oracle as O
     from ndconv import build_problem
     errs = []
+    rng = np.random.default_rng(99)
     for want in (0, 1):
-        cand = [i for i, s in enumerate(specs) if (algos[i] != 0) == bool(want)]
-        cand.sort(key=lambda i: specs[i].out_shape()[0] * 0 + int(np.prod(specs[i].out_shape())) *
-                  int(np.prod(specs[i].kshape)))
-        for i in cand[len(cand) // 2: len(cand) // 2 + 2]:
+        cand = [i for i in range(len(specs)) if (algos[i] != 0) == bool(want)]
+        for i in rng.permutation(cand)[:4]:
+            i = int(i)
             s = specs[i]
             x0, k0 = xs[i].cpu().numpy().astype(np.float64), ks[i].cpu().numpy().astype(np.float64)
             p = build_problem(_abi.F64, s.shape, with_dilation(k0, s.dilation), s.conv_mode(), s.padding_mode())
-            st, y64 = O.conv(p, x0, k0)
+            cost = float(np.prod(s.out_shape())) * float(np.prod(s.kshape))
+            st, y64 = O.conv(p, x0, k0) if cost < 3e8 else O.conv_fft(p, x0, k0, os.cpu_count() or 1)
             if st == 0:
                 y = ys[i].cpu().numpy().astype(np.float64)
                 errs.append(float(np.linalg.norm(y - y64) / max(np.linalg.norm(y64), 1e-300)))
-    if rank == 0:
-        cpu = None
-        if not args.no_cpu_baseline and world == 1:  # host-core baseline at N = 1 only
-            cpu = cpu_baseline_uneven(specs, args.cpu_seconds)
-        line = {
-            "metric": METRIC,
-            "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic (seeded; uneven-batch distribution)",
-            "config": {"workload": f"uneven batch: {len(specs)} instances (rank 1/2/3 = 60/35/5%, "
-                                   "2^8..2^20 elements, odd kernels 3..127, dilation/stride 1|2, "
-                                   "Zeros/Reflect/Replicate/Circular), one persistent launch + CUDA graph",
-                       "metric_detail": METRIC_DETAIL,
-                       "instances_per_gpu": len(specs), "algos": {"direct": int(sum(a == 0 for a in algos)),
-                                                                  "fft": int(sum(a != 0 for a in algos))},
-                       "dispatcher": {"mlp": "trained network (ndconv/data/dispatcher_mlp.json)",
-                                      "model": "cost model"}[args.dispatch], "plan": info,
-                       "plain_per_instance_gbs": bytes_step * world / (plain_ms * 1e-3) / 1e9,
-                       "batched_over_plain": plain_ms / ms,
-                       "plain_dropin_gbs": bytes_step * world / (dropin_ms * 1e-3) / 1e9,
-                       "batched_tuned_over_plain_dropin": dropin_ms / ms,
-                       "plain_note": "plain = per-instance calls with the same picks; plain drop-in = "
-                                     "per-instance calls with the library's default (cost model) picks",
-                       "l2": f"inputs {xbuf.numel() * 4 / 1e9:.2f} GB per GPU, larger than L2, no flush"},
-            "roofline": {"bound": "hbm", "achieved": bytes_step / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
-                         "frac": bytes_step / (ms * 1e-3) / 1e9 / peak, "traffic": None,
-                         "kernel": "persistent batch kernel (one launch per step, plus standalone launches)",
-                         "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"},
-            "cpu_baseline": cpu,
-            "e2e": {"value": bytes_step * world / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s",
-                    "h2d_bytes_per_step": int((xbuf.numel() + kbuf.numel()) * 4),
-                    "d2h_bytes_per_step": int(ybuf.numel() * 4)},
-            "gpu_launches": int(launches),
-            "clocks": clk.summary(),
-            "normwise_err_vs_f64": max(errs) if errs else None,
-        }
-        print(json.dumps(line), flush=True)
     plan.close()
-    if dist:
-        dist.barrier()
-        dist.destroy_process_group()
+    return {"specs": specs, "algos": algos, "info": info, "ms": ms, "plain_ms": plain_ms, "dropin_ms": dropin_ms,
+            "e2e_ms": e2e_ms, "bytes_step": bytes_step, "launches": int(launches), "clocks": clk.summary(),
+            "err": max(errs) if errs else None, "n_checked": len(errs),
+            "h2d": int((xbuf.numel() + kbuf.numel()) * 4), "d2h": int(ybuf.numel() * 4),
+            "x_gb": xbuf.numel() * 4 / 1e9}
+
+
+def uneven_summary(r, world):
+    """The uneven batch's figures, as the headline line's config.uneven_batch."""
+    def gbs(ms):
+        return r["bytes_step"] * world / (ms * 1e-3) / 1e9
+    return {"workload": f"uneven batch: {len(r['specs'])} instances per GPU (rank 1/2/3 = 60/35/5%, "
+                        "2^8..2^20 elements, odd kernels 3..127, dilation/stride 1|2, "
+                        "Zeros/Reflect/Replicate/Circular), one persistent launch + CUDA graph",
+            "batched_gbs": gbs(r["ms"]), "ms_per_step": r["ms"],
+            "plain_per_instance_gbs": gbs(r["plain_ms"]), "batched_over_plain": r["plain_ms"] / r["ms"],
+            "plain_dropin_gbs": gbs(r["dropin_ms"]), "batched_tuned_over_plain_dropin": r["dropin_ms"] / r["ms"],
+            "e2e_gbs": gbs(r["e2e_ms"]), "normwise_err": r["err"], "err_checked_instances": r["n_checked"],
+            "algos": {"direct": int(sum(a == 0 for a in r["algos"])), "fft": int(sum(a != 0 for a in r["algos"]))},
+            "plan": r["info"], "gpu_launches": r["launches"], "clocks": r["clocks"],
+            "plain_note": "plain = per-instance calls with the same picks; plain drop-in = "
+                          "per-instance calls with the library's default (cost model) picks"}
+
+
+def bench_uneven(args, world, rank, local_rank, dist):
+    """--config c4: the uneven batch as the line's own workload."""
+    r = measure_uneven(args, world, rank, local_rank, dist)
+    if rank != 0:
+        return
+    peak, peak_kind = peaks()
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:  # host-core baseline at N = 1 only
+        cpu = cpu_baseline_uneven(r["specs"], args.cpu_seconds)
+    u = uneven_summary(r, world)
+    achieved = r["bytes_step"] / (r["ms"] * 1e-3) / 1e9
+    line = {
+        "metric": METRIC,
+        "value": u["batched_gbs"], "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded; uneven-batch distribution)",
+        "config": dict(u, metric_detail=METRIC_DETAIL, instances_per_gpu=len(r["specs"]),
+                       dispatcher={"mlp": "trained network (ndconv/data/dispatcher_mlp.json)",
+                                   "model": "cost model"}[args.dispatch],
+                       l2=f"inputs {r['x_gb']:.2f} GB per GPU, larger than L2, no flush"),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "kernel": "persistent batch kernel (one launch per step, plus standalone launches)",
+                     "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": u["e2e_gbs"], "unit": "GB/s", "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"]},
+        "gpu_launches": r["launches"],
+        "clocks": r["clocks"],
+        "normwise_err_vs_f64": r["err"],
+    }
+    print(json.dumps(line), flush=True)
 
 
 def cpu_baseline_uneven(specs, seconds):
@@ -417,53 +442,21 @@ def cpu_baseline_uneven(specs, seconds):
             "sample": f"{n} random instances of the uneven batch (conv_fft_par port, f32) in {el:.1f} s"}
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--algo", default="fft", choices=["fft", "direct"])
-    ap.add_argument("--batch", type=int, default=64)
-    ap.add_argument("--form", default="batched", choices=["batched", "plain"])
-    ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--ref-instances", type=int, default=16)
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--config", default="c2", choices=["c2", "c4"])
-    ap.add_argument("--n-instances", type=int, default=4096)
-    ap.add_argument("--dispatch", default="mlp", choices=["mlp", "model"])
-    args = ap.parse_args()
-
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.impl == "reference":
-        import __graft_entry__  # noqa: F401  (paths)
-        from oracle import oracle as O
-        O.build()
-        return run_reference(args, rank, world)
-
-    if args.config == "c4":
-        return bench_uneven(args, world, rank, local_rank)
+def measure_c2(args, algo, form, world, rank, local_rank, dist):
+    """The 2-D case over B instances: conv_fft (algo 1) or conv (algo 0),
+    batched or one call per instance; device-resident, plain per-instance
+    and end-to-end (host-memory batch) timings, and the f64-oracle error of
+    instance 0 (the i32 copy's bit-exactness for the direct path)."""
     import torch
-    import __graft_entry__ as g
-    g.build()
-    torch.cuda.set_device(local_rank)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
     mode, pm, ndconv = problem_args()
     from ndconv import _abi, build_problem, with_dilation
     L = _abi.lib()
-
     B = args.batch
-    gen = torch.Generator(device="cuda").manual_seed(1000 + rank)
-    xs = [torch.rand(SHAPE_X, generator=gen, device="cuda") for _ in range(B)]
-    ks = [torch.rand(SHAPE_K, generator=gen, device="cuda") for _ in range(B)]
+    xs_np, ks_np = c2_inputs(B, SEED_C2 + rank)
+    xs = [torch.from_numpy(a).cuda() for a in xs_np]
+    ks = [torch.from_numpy(a).cuda() for a in ks_np]
     p = build_problem(_abi.F32, SHAPE_X, with_dilation(ks[0], DIL), mode, pm)
     osh = (ctypes.c_int64 * 3)()
-    algo = 1 if args.algo == "fft" else 0
     st = L.ndconv_output_shape(ctypes.byref(p), algo, osh)
     assert st == 0, _abi.last_error()
     out_shape = (osh[0], osh[1])
@@ -488,48 +481,41 @@ def main():
             if s:
                 raise RuntimeError(_abi.last_error())
 
-    def batched_step_ptrs(px, pk, py):
+    P_X, P_K, P_Y = ptrs(xs), ptrs(ks), ptrs(ys)
+
+    def step():
+        if form == "plain":
+            return plain_step(xs, ks, ys)
         if algo == 1:
-            s = L.ndconv_conv_fft_batch(pp, B, ctypes.c_void_p(px.data_ptr()), ctypes.c_void_p(pk.data_ptr()),
-                                        ctypes.c_void_p(py.data_ptr()), proc._handle, sp)
+            s = L.ndconv_conv_fft_batch(pp, B, ctypes.c_void_p(P_X.data_ptr()), ctypes.c_void_p(P_K.data_ptr()),
+                                        ctypes.c_void_p(P_Y.data_ptr()), proc._handle, sp)
         else:
-            s = L.ndconv_conv_batch(pp, B, ctypes.c_void_p(px.data_ptr()), ctypes.c_void_p(pk.data_ptr()),
-                                    ctypes.c_void_p(py.data_ptr()), sp)
+            s = L.ndconv_conv_batch(pp, B, ctypes.c_void_p(P_X.data_ptr()), ctypes.c_void_p(P_K.data_ptr()),
+                                    ctypes.c_void_p(P_Y.data_ptr()), sp)
         if s:
             raise RuntimeError(_abi.last_error())
 
-    P_X, P_K, P_Y = ptrs(xs), ptrs(ks), ptrs(ys)
-
-    def step(xl, kl, yl):
-        if args.form == "plain":
-            return plain_step(xl, kl, yl)
-        if xl is xs:
-            return batched_step_ptrs(P_X, P_K, P_Y)
-        return batched_step_ptrs(ptrs(xl), ptrs(kl), ptrs(yl))
-
-    for _ in range(args.warmup):
-        step(xs, ks, ys)
-    torch.cuda.synchronize()
-
-    # ---- device-resident timed region
     def barrier():
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
 
+    for _ in range(args.warmup):
+        step()
     barrier()
+    # ---- device-resident timed region
     n0 = L.ndconv_kernel_launches()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local_rank) as clk:
         e0.record(stream)
         for _ in range(args.steps):
-            step(xs, ks, ys)
+            step()
         e1.record(stream)
         barrier()
     launches = L.ndconv_kernel_launches() - n0
     ms = e0.elapsed_time(e1) / args.steps
     plain_ms = None
-    if args.form == "batched":
+    if form == "batched":
         plain_step(xs, ks, ys)
         barrier()
         e0.record(stream)
@@ -538,29 +524,18 @@ def main():
         e1.record(stream)
         barrier()
         plain_ms = e0.elapsed_time(e1) / max(1, args.steps // 2)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    bytes_step = algorithmic_bytes(out_shape) * B
-    value = bytes_step * world / (ms * 1e-3) / 1e9
-    per_launch_ms = ms / B  # one instance's convolution
-    peak, peak_kind = peaks()
-    achieved = algorithmic_bytes(out_shape) / (per_launch_ms * 1e-3) / 1e9
 
     # ---- end to end: pinned host inputs, H2D + conv + D2H per step
-    hx = [x.cpu().pin_memory() for x in xs]
-    hk = [k.cpu().pin_memory() for k in ks]
+    hx = [torch.from_numpy(a).pin_memory() for a in xs_np]
+    hk = [torch.from_numpy(a).pin_memory() for a in ks_np]
     hy = [torch.empty(out_shape).pin_memory() for _ in range(B)]
     dx = [torch.empty_like(x) for x in xs]
     dk = [torch.empty_like(k) for k in ks]
-
-    PD_X, PD_K = ptrs(dx), ptrs(dk)
     arr = ctypes.c_void_p * B
     HX, HK, HY = arr(*[t.data_ptr() for t in hx]), arr(*[t.data_ptr() for t in hk]), arr(*[t.data_ptr() for t in hy])
 
     def e2e_step():
-        if args.form == "batched":
+        if form == "batched":
             # the library's host-memory batch: copies of one chunk overlap the
             # convolution of the previous one
             s = L.ndconv_conv_batch_host(pp, algo, B, HX, HK, HY, proc._handle if algo == 1 else None, sp)
@@ -584,60 +559,139 @@ def main():
     barrier()
     e2e_ms = e0.elapsed_time(e1) / args.steps
     if dist:
-        t = torch.tensor([e2e_ms], device="cuda")
+        t = torch.tensor([ms, e2e_ms, plain_ms or 0.0], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    h2d = 4 * (np.prod(SHAPE_X) + np.prod(SHAPE_K)) * B
-    d2h = 4 * int(np.prod(out_shape)) * B
+        ms, e2e_ms, pm_ = [float(v) for v in t.tolist()]
+        plain_ms = pm_ if plain_ms is not None else None
 
-    # ---- parity spot check on instance 0 against the f64 oracle
+    # ---- parity: instance 0 against the f64 oracle (its host-batch output too)
     from oracle import oracle as O
-    x0, k0 = xs[0].cpu().numpy(), ks[0].cpu().numpy()
-    p64 = build_problem(_abi.F64, SHAPE_X, with_dilation(k0, DIL), mode, pm)
-    stt, y64 = O.conv(p64, x0.astype(np.float64), k0.astype(np.float64))
-    y0 = ys[0].cpu().numpy().astype(np.float64)
-    err = float(np.linalg.norm(y0 - y64) / np.linalg.norm(y64)) if stt == 0 else None
+    p64 = build_problem(_abi.F64, SHAPE_X, with_dilation(ks_np[0], DIL), mode, pm)
+    stt, y64 = O.conv(p64, xs_np[0].astype(np.float64), ks_np[0].astype(np.float64))
+    err = None
+    if stt == 0:
+        err = max(float(np.linalg.norm(y.astype(np.float64) - y64) / np.linalg.norm(y64))
+                  for y in (ys[0].cpu().numpy(), hy[0].numpy()))
+    i32_exact = None
+    if algo == 0:
+        # the case's i32 copy (values Uniform{-100..100}): bit-exact against the oracle's direct loop
+        xi, ki = c2_inputs(1, SEED_C2 + 7 + rank, np.int32)
+        pi = build_problem(_abi.I32, SHAPE_X, with_dilation(ki[0], DIL), mode, pm)
+        yi = ndconv.conv(torch.from_numpy(xi[0]).cuda(), with_dilation(torch.from_numpy(ki[0]).cuda(), DIL), mode, pm)
+        sti, yio = O.conv(pi, xi[0], ki[0])
+        i32_exact = bool(sti == 0 and np.array_equal(yi.cpu().numpy(), yio))
+    return {"ms": ms, "plain_ms": plain_ms, "e2e_ms": e2e_ms, "err": err, "launches": int(launches),
+            "clocks": clk.summary(), "out_shape": out_shape, "i32_exact": i32_exact,
+            "h2d": int(4 * (np.prod(SHAPE_X) + np.prod(SHAPE_K)) * B), "d2h": int(4 * int(np.prod(out_shape)) * B)}
 
-    if rank == 0:
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--algo", default="fft", choices=["fft", "direct"])
+    ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--form", default="batched", choices=["batched", "plain"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ref-seconds", type=float, default=0.0,
+                    help="reference arm: stop after the step that passes this many seconds (0: run --steps)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="headline workload only (no direct and uneven-batch figures in config)")
+    ap.add_argument("--config", default="c2", choices=["c2", "c4"])
+    ap.add_argument("--n-instances", type=int, default=4096)
+    ap.add_argument("--dispatch", default="mlp", choices=["mlp", "model"])
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        import __graft_entry__  # noqa: F401  (paths)
+        from oracle import oracle as O
+        O.build()
+        return run_reference(args, rank, world)
+
+    import torch
+    import __graft_entry__ as g
+    g.build()
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    try:
+        if args.config == "c4":
+            return bench_uneven(args, world, rank, local_rank, dist)
+        algo = 1 if args.algo == "fft" else 0
+        r = measure_c2(args, algo, args.form, world, rank, local_rank, dist)
+        extra_direct = extra_uneven = None
+        if not args.no_extra and algo == 1 and args.form == "batched":
+            extra_direct = measure_c2(args, 0, "batched", world, rank, local_rank, dist)
+            extra_uneven = measure_uneven(args, world, rank, local_rank, dist)
+        if rank != 0:
+            return
+        B = args.batch
+        out_shape = r["out_shape"]
+        bytes_inst = algorithmic_bytes(out_shape)
+
+        def gbs(ms):
+            return bytes_inst * B * world / (ms * 1e-3) / 1e9
+
+        peak, peak_kind = peaks()
+        achieved = bytes_inst / (r["ms"] / B * 1e-3) / 1e9  # one instance's convolution
         cpu = None
-        if not args.no_cpu_baseline and world == 1:  # host-core baseline at N = 1 only
-            gbs, cores, sample = cpu_baseline(args.cpu_seconds, algo=args.algo)
-            cpu = {"value": gbs, "unit": "GB/s", "cores": cores, "kind": "port", "sample": sample}
+        if not args.no_cpu_baseline and world == 1 and algo == 1:  # host-core baseline at N = 1 only
+            cpu = cpu_baseline(args.cpu_seconds, B)
+        traffic = PROFILED_TRAFFIC.get(args.algo) if args.form == "batched" else None
+        config = {"workload": WORKLOAD_C2.format(B=B, what="conv_fft" if algo else "conv", form=args.form),
+                  "metric_detail": METRIC_DETAIL, "batch_per_gpu": B, "algo": args.algo, "form": args.form,
+                  "plain_per_instance_gbs": gbs(r["plain_ms"]) if r["plain_ms"] else None,
+                  "batched_over_plain": (r["plain_ms"] / r["ms"]) if r["plain_ms"] else None,
+                  "l2": "inputs (256 MB per GPU) larger than L2, no flush"}
+        if extra_direct:
+            d = extra_direct
+            fma = fp32_fma_roofline(out_shape, d["ms"] / B, d["clocks"].get("sm_mhz"))
+            config["direct"] = {"workload": WORKLOAD_C2.format(B=B, what="conv (direct FP32)", form="batched"),
+                                "gbs": gbs(d["ms"]), "ms_per_step": d["ms"],
+                                "plain_per_instance_gbs": gbs(d["plain_ms"]),
+                                "batched_over_plain": d["plain_ms"] / d["ms"], "e2e_gbs": gbs(d["e2e_ms"]),
+                                "fp32_tflops": fma["achieved"], "fp32_fma_peak_tflops": fma["peak"],
+                                "fp32_fma_frac": fma["frac"], "normwise_err": d["err"],
+                                "i32_bit_exact": d["i32_exact"], "gpu_launches": d["launches"],
+                                "clocks": d["clocks"]}
+        if extra_uneven:
+            config["uneven_batch"] = uneven_summary(extra_uneven, world)
         line = {
             "metric": METRIC,
-            "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic (seeded Uniform[0,1), distinct data and kernel per instance)",
-            "config": {"workload": f"{B} x 2-D f32 x[200,5000] * k[11,31] dilation 2, Same, "
-                                   f"Custom([Reflect, Circular]); {'conv_fft' if algo else 'conv'}, "
-                                   f"{args.form} submission",
-                       "metric_detail": METRIC_DETAIL,
-                       "batch_per_gpu": B, "algo": args.algo, "form": args.form,
-                       "plain_per_instance_gbs": (bytes_step * world / (plain_ms * 1e-3) / 1e9) if plain_ms else None,
-                       "batched_over_plain": (plain_ms / ms) if plain_ms else None,
-                       "l2": "inputs (256 MB per GPU) larger than L2, no flush"},
+            "value": gbs(r["ms"]), "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32",
+            "data": f"synthetic (seeded Uniform[0,1), distinct data and kernel per instance, seed {SEED_C2} + rank)",
+            "config": config,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak,
-                         "traffic": PROFILED_TRAFFIC.get(args.algo) if args.form == "batched" else None,
-                         "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per instance, "
-                                            "profiles/conv_fft_rowspectral_kernels_full.md")
-                         if args.algo == "fft" and args.form == "batched" else None,
+                         "frac": achieved / peak, "traffic": traffic,
+                         "traffic_source": PROFILED_TRAFFIC_SOURCE if traffic else None,
                          "kernel": "one instance's convolution (all its launches)",
                          "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"},
             "cpu_baseline": cpu,
-            "e2e": {"value": bytes_step * world / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s",
-                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-            "gpu_launches": int(launches),
-            "clocks": clk.summary(),
-            "normwise_err_vs_f64": err,
+            "e2e": {"value": gbs(r["e2e_ms"]), "unit": "GB/s", "h2d_bytes_per_step": r["h2d"],
+                    "d2h_bytes_per_step": r["d2h"]},
+            "gpu_launches": r["launches"],
+            "clocks": r["clocks"],
+            "normwise_err_vs_f64": r["err"],
         }
         if not algo:
             # the direct path is bound by the FP32 FMA rate, not by HBM
-            line["compute_roofline"] = fp32_fma_roofline(out_shape, per_launch_ms, line["clocks"].get("sm_mhz"))
+            line["compute_roofline"] = fp32_fma_roofline(out_shape, r["ms"] / B, r["clocks"].get("sm_mhz"))
+            line["i32_bit_exact"] = r["i32_exact"]
         print(json.dumps(line), flush=True)
-    if dist:
-        dist.barrier()
-        dist.destroy_process_group()
+    finally:
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
 
 
 if __name__ == "__main__":
