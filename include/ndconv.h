@@ -144,13 +144,16 @@ int ndconv_conv_algo(const ndconv_problem *p, int32_t algo, const void *data, co
                      void *stream);
 
 /* conv (algo 0) or conv_fft (algo 1) over n same-geometry instances whose
- * data, kernels and outputs are HOST arrays (contiguous; pinned memory for
- * full speed): chunks of instances are staged through library-owned device
- * buffers so that host->device copies, the convolution and device->host
- * copies of successive chunks overlap.  Asynchronous on `stream`: the host
- * arrays must stay valid, and the outputs are complete, when `stream` has
- * synchronised.  No reference counterpart (the crate converts one host
- * array per call). */
+ * data, kernels and outputs are HOST arrays (contiguous): chunks of
+ * instances are staged through library-owned device buffers so that
+ * host->device copies, the convolution and device->host copies of
+ * successive chunks overlap.  The overlap needs page-locked (pinned) host
+ * arrays: with pageable ones each device->host copy blocks the calling
+ * thread until its chunk's convolution has finished, so the chunks run one
+ * after another (results are the same).  Asynchronous on `stream` for
+ * pinned arrays: they must stay valid, and the outputs are complete, when
+ * `stream` has synchronised.  A failing copy or launch returns its error.
+ * No reference counterpart (the crate converts one host array per call). */
 int ndconv_conv_batch_host(const ndconv_problem *p, int32_t algo, int64_t n, const void *const *data,
                            const void *const *kernel, void *const *out, ndconv_fft_processor *proc,
                            void *stream);
@@ -162,8 +165,13 @@ int ndconv_conv_batch_host(const ndconv_problem *p, int32_t algo, int64_t n, con
  * NaN / Inf propagate as in the reference.  Same as
  * ndconv_conv_algo(p, NDCONV_ALGO_DIRECT_BF16X3, ...).  Asynchronous on
  * stream; a tensor-core pipeline wait that runs out (bounded at ~1 s, not
- * expected) leaves NaN in the affected output tile. */
+ * expected) leaves NaN in the affected output tile and is recorded in a
+ * per-device word that ndconv_bf16x3_status reports. */
 int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, const void *kernel, void *out, void *stream);
+/* Synchronises stream, then reports (NDCONV_ERR_TIMEOUT) and clears the
+ * timeouts of every 3xBF16 launch on the current device since the last
+ * call; NDCONV_OK when there were none.  No reference counterpart. */
+int ndconv_bf16x3_status(void *stream);
 
 /* Batched ConvExt::conv / ConvFFTExt::conv_fft over n instances that share
  * one problem geometry (shapes, dilation, modes); each instance has its
@@ -193,8 +201,19 @@ int ndconv_batch_run(ndconv_batch_plan *plan, int32_t use_graph, void *stream);
 /* The same instances, one per-instance entry point call each (the plain
  * drop-in path), for comparison. */
 int ndconv_batch_run_plain(ndconv_batch_plan *plan, void *stream);
-/* Synchronises stream; NDCONV_ERR_TIMEOUT if a queue wait ran out. */
+/* Synchronises stream; NDCONV_ERR_TIMEOUT if a queue wait ran out (a task
+ * whose predecessors did not finish within the poll bound gives up waiting,
+ * runs, and the kernel returns normally). */
 int ndconv_batch_status(ndconv_batch_plan *plan, void *stream);
+/* Poll bound of the queue's dependency waits for later runs of the plan
+ * (polls <= 0: the default, 2^24 polls, ~1-2 s).  No reference counterpart. */
+int ndconv_batch_set_wait_limit(ndconv_batch_plan *plan, int64_t polls);
+/* Test hook for the timeout path (no reference counterpart): enable = 1 makes
+ * the plan's first waiting task wait on a counter that no task bumps, so
+ * that its wait runs out after the poll bound and ndconv_batch_status
+ * reports NDCONV_ERR_TIMEOUT; enable = 0 restores the task.  No GPU fault:
+ * the task gives up, runs and the queue completes. */
+int ndconv_batch_stall_one_wait(ndconv_batch_plan *plan, int32_t enable);
 /* tasks, grid, shared bytes, #FFT, #direct, #standalone, workspace bytes, counters */
 int ndconv_batch_info(const ndconv_batch_plan *plan, int64_t info[8]);
 int ndconv_batch_destroy(ndconv_batch_plan *plan);
@@ -206,7 +225,12 @@ int ndconv_batch_destroy(ndconv_batch_plan *plan);
  * processor, but the spectra and twiddle tables live in one fixed 16 MiB
  * device array that the library holds on every GPU where it is loaded; it
  * never calls cudaMalloc or cudaFree.  Problems whose spectra need more
- * than 16 MiB get NDCONV_ERR_NO_MEMORY.  The first call on each device
+ * than 16 MiB get NDCONV_ERR_NO_MEMORY.  One exception to "same results":
+ * where no FFT form applies (a kernel row longer than the longest
+ * overlap-save segment, leading axes too long for one column pass, rows of
+ * 2^31 samples or more) ndconv_conv_fft runs the direct kernels, whose
+ * axis-folding form allocates; this entry point returns
+ * NDCONV_ERR_UNSUPPORTED there instead.  The first call on each device
  * looks up the array's address, so make it before any stream capture.
  * Calls share the array: calls whose GPU work overlaps race and must be
  * serialised by the caller. */

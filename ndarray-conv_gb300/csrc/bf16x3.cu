@@ -16,8 +16,10 @@
 // the padded data (border map applied once, split into hi / lo) and the
 // Toeplitz bands.  One thread issues TMA, one issues tcgen05.mma, all four
 // warps drain TMEM with tcgen05.ld.  Every mbarrier wait is bounded; a
-// timeout (not expected) sets bit 1 of the status word, writes NaN to the
-// tile's outputs and the CTA still releases TMEM.
+// timeout (not expected) writes NaN to the tile's outputs, records the event
+// in a library-owned per-device word (read and cleared by
+// ndconv_bf16x3_status), waits (bounded) for the tile's TMA loads and MMAs
+// already in flight, and the CTA still releases TMEM.
 // Non-finite inputs (bit 0, found by the pre-pass) make every CTA compute its
 // tile with the FP32 direct loop instead, like the reference's sums.
 #include <cuda.h>
@@ -49,6 +51,10 @@ template <int BN> struct Tile {
 };
 constexpr long long kWaitCycles = 2000000000LL;  // ~1 s of polling before a wait gives up
 constexpr int kThreads = 128;
+
+// Timeouts of any launch on this device since the last ndconv_bf16x3_status
+// call (a file-scope device variable: one per device that loads the library).
+__device__ int g_timeouts;
 
 struct Params {
     int64_t out0, out1, out2;
@@ -241,6 +247,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t tmem = *tmem_slot;
     const int niter = P.K0 * P.K1 * P.nchunk;
 
+    int issued = 0;  // producer: K steps whose TMA loads were issued
     if (tid == 0) {
         // producer: Toeplitz band tiles and data row tiles
         const int x0 = (int)((int64_t)q * BM * P.s2);
@@ -259,6 +266,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             const int by = (int)(oy0 + (int64_t)ky * P.d1), bz = (int)(oz * P.s0 + (int64_t)kz * P.d0);
             tma_3d(st + 2 * A_BYTES, &tB_hi, x0 + c * KC, by, bz, &full[s]);
             tma_3d(st + 2 * A_BYTES + B_BYTES, &tB_lo, x0 + c * KC, by, bz, &full[s]);
+            issued = i + 1;
         }
     } else if (tid == 32) {
         // MMA issuer: three split products per 16-wide K step
@@ -291,8 +299,16 @@ __global__ void __launch_bounds__(kThreads, 1)
     const bool good = (*reinterpret_cast<volatile int *>(bad) == 0);
     if (!good) {
         // a pipeline wait ran out (not expected): the tile's outputs become NaN
-        // and the status word keeps the event
-        if (tid == 0) atomicOr(P.status, 2);
+        // and the per-device word keeps the event.  Before the shared memory
+        // and TMEM are released, the loads already issued must have landed and
+        // the MMAs already issued must have finished (waits bounded as well).
+        if (tid == 0) {
+            for (int i = issued > STAGES ? issued - STAGES : 0; i < issued; i++)
+                mbar_wait(&full[i % STAGES], (i / STAGES) & 1);
+            mbar_wait(done, 0);
+            atomicOr(P.status, 2);
+            atomicOr(&g_timeouts, 1);
+        }
         for (int u = tid; u < BM * BN; u += kThreads) {
             const int64_t ox = (int64_t)q * BM + (u % BM), oy = oy0 + u / BM;
             if (ox < P.out2 && oy < P.out1) P.y[oz * P.ys0 + oy * P.ys1 + ox] = __int_as_float(0x7fc00000);
@@ -444,5 +460,17 @@ extern "C" int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, con
     e = cudaGetLastError();
     cudaFreeAsync(ws, st);  // stream-ordered: after the launch has finished with it
     if (e != cudaSuccess) return ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e));
+    return NDCONV_OK;
+}
+
+// See include/ndconv.h.  Waits for the stream, then reads and clears the
+// device's timeout word.
+extern "C" int ndconv_bf16x3_status(void *stream) {
+    NDCONV_CUDA_OK(cudaStreamSynchronize((cudaStream_t)stream));
+    int v = 0;
+    const int zero = 0;
+    NDCONV_CUDA_OK(cudaMemcpyFromSymbol(&v, ndconv::bf16x3::g_timeouts, sizeof(int)));
+    if (v) NDCONV_CUDA_OK(cudaMemcpyToSymbol(ndconv::bf16x3::g_timeouts, &zero, sizeof(int)));
+    if (v) return ndconv_fail(NDCONV_ERR_TIMEOUT, "a 3xBF16 tensor-core pipeline wait ran out (its tile holds NaN)");
     return NDCONV_OK;
 }

@@ -79,7 +79,7 @@ struct Task {
     int32_t wait_need;  // value it must reach
 };
 
-constexpr int kSpinLimit = 1 << 24;  // ~1-2 s of polling before giving up
+constexpr int kSpinLimit = 1 << 24;  // default poll bound: ~1-2 s of polling before giving up
 
 __device__ __forceinline__ int ld_acquire(const int *p) {
     int v;
@@ -106,7 +106,8 @@ __global__ void __launch_bounds__(256) persistent_kernel(const Task *__restrict_
                                                          const ColArgs<c32> *__restrict__ cargs,
                                                          const DirectParams<float> *__restrict__ dargs,
                                                          const FoldTaskArgs *__restrict__ fargs,
-                                                         int *ctrs, int *ticket, int *status) {
+                                                         int *ctrs, int *ticket, int *status,
+                                                         const int *poll_limit) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_ticket;
     for (;;) {
@@ -120,7 +121,7 @@ __global__ void __launch_bounds__(256) persistent_kernel(const Task *__restrict_
             if (threadIdx.x == 0) {
                 int it = 0;
                 while (ld_acquire(ctrs + tk.wait_ctr) < tk.wait_need) {
-                    if (++it > kSpinLimit) {
+                    if (++it > *poll_limit) {
                         atomicOr(status, 1);  // dependency never completed: report, do not hang
                         break;
                     }
@@ -225,7 +226,10 @@ struct ndconv_batch_plan {
     size_t smem = 0;
     int grid = 0;
     void *d_tasks = nullptr, *d_rargs = nullptr, *d_cargs = nullptr, *d_dargs = nullptr, *d_fargs = nullptr;
-    int *d_ctrs = nullptr;  // nctrs counters, then ticket, then status
+    int *d_ctrs = nullptr;  // nctrs counters, then ticket, status (reset per run), poll bound
+    int stall_ctr = -1;     // a counter no task bumps (ndconv_batch_stall_one_wait)
+    int64_t stall_task = -1;  // the task redirected to it, -1: none
+    int32_t stall_saved = -1; // that task's own wait counter
     void *ws = nullptr;
     size_t ws_bytes = 0;
     cudaGraph_t graph = nullptr;
@@ -661,8 +665,12 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
         (s = upload(B->fargs, &B->d_fargs)) || (s = upload(B->fix, &B->d_fix)))
         return fail(s);
     {
-        cudaError_t e = cudaMalloc((void **)&B->d_ctrs, sizeof(int) * (size_t)(B->nctrs + 2));
+        B->stall_ctr = B->nctrs++;
+        cudaError_t e = cudaMalloc((void **)&B->d_ctrs, sizeof(int) * (size_t)(B->nctrs + 3));
         if (e != cudaSuccess) return fail(ndconv_fail(NDCONV_ERR_NO_MEMORY, cudaGetErrorString(e)));
+        const int lim = kSpinLimit;
+        e = cudaMemcpy(B->d_ctrs + B->nctrs + 2, &lim, sizeof(int), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return fail(ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e)));
     }
     if (B->smem < 16) B->smem = 16;
     if (B->smem > kBatchSmem) return fail(ndconv_fail(NDCONV_ERR_INVALID, "batch task shared memory above the cap"));
@@ -740,7 +748,8 @@ int enqueue(ndconv_batch_plan *B, cudaStream_t st) {
         persistent_kernel<<<B->grid, 256, B->smem, st>>>(
             (const Task *)B->d_tasks, (int)B->tasks.size(), (const RowArgs<float> *)B->d_rargs,
             (const ColArgs<c32> *)B->d_cargs, (const DirectParams<float> *)B->d_dargs,
-            (const FoldTaskArgs *)B->d_fargs, B->d_ctrs, B->d_ctrs + B->nctrs, B->d_ctrs + B->nctrs + 1);
+            (const FoldTaskArgs *)B->d_fargs, B->d_ctrs, B->d_ctrs + B->nctrs, B->d_ctrs + B->nctrs + 1,
+            B->d_ctrs + B->nctrs + 2);
         ndconv_count_launch();
         NDCONV_CUDA_OK(cudaGetLastError());
     }
@@ -839,6 +848,31 @@ extern "C" int ndconv_batch_status(ndconv_batch_plan *B, void *stream) {
                                    (cudaStream_t)stream));
     NDCONV_CUDA_OK(cudaStreamSynchronize((cudaStream_t)stream));
     if (v) return ndconv_fail(NDCONV_ERR_TIMEOUT, "a batch task waited too long for its predecessors");
+    return NDCONV_OK;
+}
+
+extern "C" int ndconv_batch_set_wait_limit(ndconv_batch_plan *B, int64_t polls) {
+    if (!B) return ndconv_fail(NDCONV_ERR_INVALID, "null plan");
+    const int lim = polls <= 0 ? ndconv::batch::kSpinLimit : (int)std::min<int64_t>(polls, 0x7fffffff);
+    NDCONV_CUDA_OK(cudaMemcpy(B->d_ctrs + B->nctrs + 2, &lim, sizeof(int), cudaMemcpyHostToDevice));
+    return NDCONV_OK;
+}
+
+extern "C" int ndconv_batch_stall_one_wait(ndconv_batch_plan *B, int32_t enable) {
+    if (!B) return ndconv_fail(NDCONV_ERR_INVALID, "null plan");
+    if (B->stall_task < 0) {
+        for (size_t t = 0; t < B->tasks.size(); t++)
+            if (B->tasks[t].wait_ctr >= 0) {
+                B->stall_task = (int64_t)t;
+                B->stall_saved = B->tasks[t].wait_ctr;
+                break;
+            }
+        if (B->stall_task < 0) return ndconv_fail(NDCONV_ERR_INVALID, "no task of this plan waits on another");
+    }
+    ndconv::batch::Task &tk = B->tasks[(size_t)B->stall_task];
+    tk.wait_ctr = enable ? B->stall_ctr : B->stall_saved;
+    NDCONV_CUDA_OK(cudaMemcpy(static_cast<ndconv::batch::Task *>(B->d_tasks) + B->stall_task, &tk,
+                              sizeof(ndconv::batch::Task), cudaMemcpyHostToDevice));
     return NDCONV_OK;
 }
 

@@ -106,19 +106,25 @@ extern "C" int ndconv_conv_batch_host(const ndconv_problem *p, int32_t algo, int
     if (e == cudaSuccess) e = cudaEventRecord(start, st);  // the pointer upload and allocation come first
     if (e == cudaSuccess) e = cudaStreamWaitEvent(sin, start, 0);
     s = (e == cudaSuccess) ? NDCONV_OK : ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e));
+    // every enqueue call is checked; the first failure ends the loop (what
+    // was enqueued still completes before the buffer is released below)
+    auto chk = [&](cudaError_t r) {
+        if (r != cudaSuccess && s == NDCONV_OK) s = ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(r));
+    };
     for (int64_t c0 = 0, chunk = 0; c0 < n && s == NDCONV_OK; c0 += C, chunk++) {
         const int slot = (int)(chunk % NS);
         const int64_t cnt = std::min<int64_t>(C, n - c0);
         // inputs: the slot's inputs are free once its previous convolution is done
-        if (chunk >= NS) cudaStreamWaitEvent(sin, ev(slot, 1), 0);
-        for (int64_t i = 0; i < cnt; i++) {
-            cudaMemcpyAsync(ptrs[(size_t)((slot * 3 + 0) * C + i)], data[c0 + i], bx, cudaMemcpyHostToDevice, sin);
-            cudaMemcpyAsync(ptrs[(size_t)((slot * 3 + 1) * C + i)], kernel[c0 + i], bk, cudaMemcpyHostToDevice, sin);
+        if (chunk >= NS) chk(cudaStreamWaitEvent(sin, ev(slot, 1), 0));
+        for (int64_t i = 0; i < cnt && s == NDCONV_OK; i++) {
+            chk(cudaMemcpyAsync(ptrs[(size_t)((slot * 3 + 0) * C + i)], data[c0 + i], bx, cudaMemcpyHostToDevice, sin));
+            chk(cudaMemcpyAsync(ptrs[(size_t)((slot * 3 + 1) * C + i)], kernel[c0 + i], bk, cudaMemcpyHostToDevice, sin));
         }
-        cudaEventRecord(ev(slot, 0), sin);
+        chk(cudaEventRecord(ev(slot, 0), sin));
         // convolution: after the inputs and after the slot's previous outputs left
-        cudaStreamWaitEvent(st, ev(slot, 0), 0);
-        if (chunk >= NS) cudaStreamWaitEvent(st, ev(slot, 2), 0);
+        chk(cudaStreamWaitEvent(st, ev(slot, 0), 0));
+        if (chunk >= NS) chk(cudaStreamWaitEvent(st, ev(slot, 2), 0));
+        if (s) break;
         const void *const *dx = (const void *const *)(dptr + (slot * 3 + 0) * C);
         const void *const *dk = (const void *const *)(dptr + (slot * 3 + 1) * C);
         void *const *dy = (void *const *)(dptr + (slot * 3 + 2) * C);
@@ -129,12 +135,12 @@ extern "C" int ndconv_conv_batch_host(const ndconv_problem *p, int32_t algo, int
         case NDCONV_C32: s = run_chunk<c32>(P, algo, cnt, dx, dk, dy, proc, st); break;
         default: s = run_chunk<c64>(P, algo, cnt, dx, dk, dy, proc, st); break;
         }
-        cudaEventRecord(ev(slot, 1), st);
+        chk(cudaEventRecord(ev(slot, 1), st));
         // outputs back to the host
-        cudaStreamWaitEvent(sout, ev(slot, 1), 0);
-        for (int64_t i = 0; i < cnt; i++)
-            cudaMemcpyAsync(out[c0 + i], ptrs[(size_t)((slot * 3 + 2) * C + i)], by, cudaMemcpyDeviceToHost, sout);
-        cudaEventRecord(ev(slot, 2), sout);
+        chk(cudaStreamWaitEvent(sout, ev(slot, 1), 0));
+        for (int64_t i = 0; i < cnt && s == NDCONV_OK; i++)
+            chk(cudaMemcpyAsync(out[c0 + i], ptrs[(size_t)((slot * 3 + 2) * C + i)], by, cudaMemcpyDeviceToHost, sout));
+        chk(cudaEventRecord(ev(slot, 2), sout));
     }
     // the caller's stream covers everything: wait for the last copies, then free
     if (made) {

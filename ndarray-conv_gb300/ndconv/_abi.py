@@ -102,6 +102,9 @@ def lib():
         "ndconv_batch_run": (ctypes.c_int, [vp, i32, vp]),
         "ndconv_batch_run_plain": (ctypes.c_int, [vp, vp]),
         "ndconv_batch_status": (ctypes.c_int, [vp, vp]),
+        "ndconv_batch_set_wait_limit": (ctypes.c_int, [vp, ctypes.c_int64]),
+        "ndconv_batch_stall_one_wait": (ctypes.c_int, [vp, i32]),
+        "ndconv_bf16x3_status": (ctypes.c_int, [vp]),
         "ndconv_batch_info": (ctypes.c_int, [vp, i64p]),
         "ndconv_batch_destroy": (ctypes.c_int, [vp]),
         "ndconv_plan_info": (ctypes.c_int, [pp, ctypes.POINTER(ctypes.c_double)]),

@@ -82,6 +82,24 @@ class BatchPlan:
         if st:
             raise RuntimeError(_abi.last_error())
 
+    def status(self, stream=None):
+        """ndconv_batch_status: 0, or the error code (ERR_TIMEOUT when a queue
+        wait ran out), without raising."""
+        s = stream if stream is not None else torch.cuda.current_stream()
+        return _abi.lib().ndconv_batch_status(self._h, ctypes.c_void_p(s.cuda_stream))
+
+    def set_wait_limit(self, polls):
+        """Poll bound of the queue's dependency waits (<= 0: the default)."""
+        st = _abi.lib().ndconv_batch_set_wait_limit(self._h, int(polls))
+        if st:
+            raise RuntimeError(_abi.last_error())
+
+    def stall_one_wait(self, enable):
+        """Test hook: the first waiting task waits on a counter nothing bumps."""
+        st = _abi.lib().ndconv_batch_stall_one_wait(self._h, 1 if enable else 0)
+        if st:
+            raise RuntimeError(_abi.last_error())
+
     def close(self):
         if getattr(self, "_h", None):
             _abi.lib().ndconv_batch_destroy(self._h)
