@@ -26,7 +26,13 @@ extern "C" {
 
 #define NDCONV_MAX_RANK 3
 
-/* element type (InElem / T of the reference traits) */
+/* element type (InElem / T of the reference traits).  The crate's ConvExt
+ * is generic over any T: NumAssign + Copy and any rank N
+ * (src/conv/mod.rs:78-83,118-124); its own tests pad u8 arrays
+ * (src/padding/mod.rs:621-624).  This library runs f32, f64, i32, c32 and
+ * c64 at ranks 1..NDCONV_MAX_RANK; any other element type code (i8, i16,
+ * i64, u8, u32, ...) and any rank above 3 get NDCONV_ERR_UNSUPPORTED from
+ * every entry point (there is no CPU fallback). */
 typedef enum {
     NDCONV_F32 = 0,
     NDCONV_F64 = 1,
@@ -108,6 +114,16 @@ typedef struct ndconv_batch_plan ndconv_batch_plan;
  * paths report zero-size kernels and padding panics in the reference's
  * different orders. */
 int ndconv_output_shape(const ndconv_problem *p, int32_t algo, int64_t out_shape[3]);
+
+/* The padded array that ConvExt::conv convolves, as the crate's
+ * PaddingExt::padding materialises it (src/padding/mod.rs:84-452, dim.rs,
+ * half_dim.rs), from the closed-form border map that every kernel of this
+ * library evaluates in its loads instead of storing a padded copy.  Host
+ * only (no device work).  x: the problem's data on the host as f64 (nc = 1)
+ * or (re, im) pairs (nc = 2), in its element strides; out: the padded
+ * extents (input + both pads per axis), contiguous.  Padding that makes
+ * the crate panic is reported as NDCONV_ERR_PAD_OUT_OF_RANGE. */
+int ndconv_padded_host(const ndconv_problem *p, const double *x, int32_t nc, double *out);
 
 /* ConvExt::conv (src/conv/mod.rs:78-116, impl :128-200).
  * data, kernel: device pointers to p->dtype elements; out: device pointer

@@ -121,8 +121,14 @@ static int borders(const ndconv_problem *p, int ax, int kind[2], double val[2][2
 
 int plan_problem(const ndconv_problem *p, int algo, Plan3 *out) {
     if (!p) return ndconv_fail(NDCONV_ERR_INVALID, "null problem");
-    if (p->rank < 1 || p->rank > 3) return ndconv_fail(NDCONV_ERR_INVALID, "rank must be 1..3");
-    if (p->dtype < NDCONV_F32 || p->dtype > NDCONV_C64) return ndconv_fail(NDCONV_ERR_INVALID, "bad dtype");
+    if (p->rank < 1) return ndconv_fail(NDCONV_ERR_INVALID, "rank must be at least 1");
+    // the crate is generic over any const N and any NumAssign element type
+    // (src/conv/mod.rs:78-83,118-124); this library's kernels take ranks 1..3
+    // and f32 / f64 / i32 / c32 / c64: everything else is refused, never run
+    // on a fallback
+    if (p->rank > 3) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "rank above 3 is not supported (ranks 1..3)");
+    if (p->dtype < NDCONV_F32 || p->dtype > NDCONV_C64)
+        return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "element type not supported (f32, f64, i32, c32, c64)");
     const int r = p->rank;
     for (int i = 0; i < r; i++) {
         if (p->data_shape[i] < 0 || p->kernel_shape[i] < 0)
@@ -222,6 +228,35 @@ extern "C" int ndconv_output_shape(const ndconv_problem *p, int32_t algo, int64_
     if (s) return s;
     if (out_shape)
         for (int i = 0; i < p->rank; i++) out_shape[i] = P.ax[3 - p->rank + i].out;
+    return NDCONV_OK;
+}
+
+extern "C" int ndconv_padded_host(const ndconv_problem *p, const double *x, int32_t nc, double *out) {
+    Plan3 P;
+    int s = plan_problem(p, 0, &P);
+    if (s) return s;
+    if (!x || !out || (nc != 1 && nc != 2)) return ndconv_fail(NDCONV_ERR_INVALID, "null pointer or nc not 1 or 2");
+    const AxisGeom *A = P.ax;
+    int64_t u = 0;
+    for (int64_t i0 = 0; i0 < A[0].L; i0++) {
+        const int64_t m0 = axis_map(A[0], i0);
+        for (int64_t i1 = 0; i1 < A[1].L; i1++) {
+            const int64_t m1 = axis_map(A[1], i1);
+            for (int64_t i2 = 0; i2 < A[2].L; i2++, u++) {
+                const int64_t m2 = axis_map(A[2], i2);
+                // the rule of resolve_padded: the last axis' constant first, then
+                // the middle and leading axes', then pre-fill, else the sample
+                const int64_t m[3] = {m0, m1, m2};
+                const double *v = nullptr;
+                double zero[2] = {0.0, 0.0};
+                for (int a = 2; a >= 0 && !v; a--)
+                    if (m[a] <= MAP_CONST_FRONT) v = P.cval[a][m[a] == MAP_CONST_FRONT ? 0 : 1];
+                if (!v && (m0 < 0 || m1 < 0 || m2 < 0)) v = zero;
+                if (!v) v = x + nc * (m0 * A[0].xs + m1 * A[1].xs + m2 * A[2].xs);
+                for (int c = 0; c < nc; c++) out[nc * u + c] = v[c];
+            }
+        }
+    }
     return NDCONV_OK;
 }
 

@@ -84,6 +84,7 @@ def lib():
     sig = {
         "ndconv_output_shape": (ctypes.c_int, [pp, i32, i64p]),
         "ndconv_conv": (ctypes.c_int, [pp, vp, vp, vp, vp]),
+        "ndconv_padded_host": (ctypes.c_int, [pp, vp, i32, vp]),
         "ndconv_conv_fft": (ctypes.c_int, [pp, vp, vp, vp, vp, vp]),
         "ndconv_conv_fft_noalloc": (ctypes.c_int, [pp, vp, vp, vp, vp]),
         "ndconv_conv_algo": (ctypes.c_int, [pp, i32, vp, vp, vp, vp]),

@@ -184,9 +184,12 @@ _NP_DTYPES = {"float32": _abi.F32, "float64": _abi.F64, "int32": _abi.I32,
 
 
 def dtype_code(dtype):
+    """The ABI element type of a numpy / torch dtype.  Like the C ABI, element
+    types other than f32, f64, i32, c32 and c64 (the crate's generic conv
+    also takes i8, i16, i64, u8, u32, ...) raise Unsupported."""
     name = str(dtype).replace("torch.", "")
     if name not in _NP_DTYPES:
-        raise TypeError(f"unsupported element type {dtype}")
+        raise Unsupported(None, f"element type {dtype} is not supported (f32, f64, i32, c32, c64)")
     return _NP_DTYPES[name]
 
 
@@ -197,8 +200,10 @@ def build_problem(dtype, data_shape, kwd, conv_mode, padding_mode,
     k = kwd.kernel
     if len(k.shape) != rank:
         raise ValueError("data and kernel rank differ")
-    if not 1 <= rank <= 3:
-        raise ValueError("rank must be 1..3")
+    if rank > 3:
+        raise Unsupported(None, "rank above 3 is not supported (ranks 1..3)")
+    if rank < 1:
+        raise ValueError("rank must be at least 1")
     p = _abi.Problem()
     p.dtype = dtype
     p.rank = rank

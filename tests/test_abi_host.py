@@ -81,3 +81,29 @@ def test_last_error_message():
     st, _ = _abi_shape(p, 0)
     assert st == _abi.ERR_MISMATCH_SHAPE
     assert "ConvMode" in _abi.last_error()
+
+
+def test_unsupported_ranks_and_element_types_are_refused():
+    """The crate is generic over rank and element type; the library takes
+    ranks 1..3 and f32/f64/i32/c32/c64 and refuses the rest (no fallback)."""
+    from helpers import with_dilation
+    p = problem(F32, np.ones((4, 5)), np.ones((3, 3)), ConvMode.Same, PaddingMode.Zeros)
+    sh = (ctypes.c_int64 * 3)()
+    q = _abi.Problem.from_buffer_copy(p)
+    q.rank = 4
+    assert _abi.lib().ndconv_output_shape(ctypes.byref(q), 0, sh) == _abi.ERR_UNSUPPORTED
+    assert "rank" in _abi.last_error()
+    for code in (5, 9, 100):  # no such element type in the ABI
+        q = _abi.Problem.from_buffer_copy(p)
+        q.dtype = code
+        assert _abi.lib().ndconv_output_shape(ctypes.byref(q), 0, sh) == _abi.ERR_UNSUPPORTED
+        assert "element type" in _abi.last_error()
+    q = _abi.Problem.from_buffer_copy(p)
+    q.rank = 0
+    assert _abi.lib().ndconv_output_shape(ctypes.byref(q), 0, sh) == _abi.ERR_INVALID
+    for dt in (np.int8, np.int16, np.int64, np.uint8, np.uint32):
+        with pytest.raises(ndconv.Unsupported):
+            ndconv.api.dtype_code(np.dtype(dt))
+    with pytest.raises(ndconv.Unsupported):
+        ndconv.build_problem(F32, (2, 2, 2, 2), with_dilation(np.ones((1, 1, 1, 1)), 1), ConvMode.Same,
+                             PaddingMode.Zeros)
