@@ -274,6 +274,24 @@ __device__ __forceinline__ void stage_twiddles(C (&w)[RAD], const C *__restrict_
     }
 }
 
+// Geometry of one Stockham stage: transform length L, nb interleaved
+// transforms (a power of two, lognb = log2 nb) and Ns, the product of the
+// previous radices.  RtGeo holds them at run time; CtGeo fixes them at
+// compile time for the lengths the row kernels specialise, so that the same
+// stage code folds its index arithmetic into constants.
+struct RtGeo {
+    int L, nb, lognb;
+    FastDiv nsd;
+    __device__ __forceinline__ int ns() const { return (int)nsd.d; }
+    __device__ __forceinline__ int div_ns(int j) const { return (int)fdiv((uint32_t)j, nsd); }
+};
+template <int L_, int NB_, int NS_> struct CtGeo {
+    static_assert(NB_ == 1 || NB_ == 2 || NB_ == 4 || NB_ == 8, "rows per CTA: 1, 2, 4 or 8");
+    static constexpr int L = L_, nb = NB_, lognb = NB_ == 1 ? 0 : NB_ == 2 ? 1 : NB_ == 4 ? 2 : 3;
+    __device__ __forceinline__ static constexpr int ns() { return NS_; }
+    __device__ __forceinline__ static constexpr int div_ns(int j) { return j / NS_; }
+};
+
 // One radix-R Stockham stage over nb interleaved transforms.  Butterfly j
 // (of transform b) reads logical elements u + r si (u = j nb + b,
 // si = (L / R) nb) and writes uo + r so (so = Ns nb).  When a stride is a
@@ -281,24 +299,23 @@ __device__ __forceinline__ void stage_twiddles(C (&w)[RAD], const C *__restrict_
 // butterfly's outputs stay inside one wavefront, the padded slot of element
 // r is the first one's plus r times a fixed step, so each access is one add
 // away from the last.
-template <bool INV, int RAD, typename C>
-__device__ __forceinline__ void stockham_stage(const C *src, C *dst, int L, int nb, int lognb,
-                                               const FastDiv &nsd, const C *__restrict__ tws) {
-    const int Ns = (int)nsd.d;
-    const int nr = L / RAD;
-    const int total = nr << lognb;
+template <bool INV, int RAD, typename C, typename Geo>
+__device__ __forceinline__ void stockham_stage_g(const C *src, C *dst, const Geo &g, const C *__restrict__ tws) {
+    const int Ns = g.ns();
+    const int nr = g.L / RAD;
+    const int total = nr << g.lognb;
     constexpr int kWf = sizeof(C) <= 8 ? 16 : 8;  // elements per padded wavefront (see sx)
     constexpr int kSh = sizeof(C) <= 8 ? 4 : 3;
-    const int si = total, so = Ns << lognb;
+    const int si = total, so = Ns << g.lognb;
     const bool lin_i = (si & (kWf - 1)) == 0;
     const bool lin_o = (so & (kWf - 1)) == 0 || (kWf % (RAD * so)) == 0;
     const int psi = si + (si >> kSh);                             // padded input step (lin_i)
     const int pso = (so & (kWf - 1)) == 0 ? so + (so >> kSh) : so;  // padded output step (lin_o)
 #pragma unroll 2
     for (int u = threadIdx.x; u < total; u += blockDim.x) {
-        const int b = u & (nb - 1);
-        const int j = u >> lognb;
-        const int q = (int)fdiv((uint32_t)j, nsd);
+        const int b = u & (g.nb - 1);
+        const int j = u >> g.lognb;
+        const int q = g.div_ns(j);
         const int t = j - q * Ns;
         C v[RAD];
         if (lin_i) {
@@ -323,7 +340,7 @@ __device__ __forceinline__ void stockham_stage(const C *src, C *dst, int L, int 
         else if constexpr (RAD == 8) dft8<INV>(v);
         else if constexpr (RAD == 10) dft10<INV>(v);
         else if constexpr (RAD == 16) dft16<INV>(v);
-        const int uo = ((q * Ns * RAD + t) << lognb) + b;
+        const int uo = ((q * Ns * RAD + t) << g.lognb) + b;
         if (lin_o) {
             C *d0 = dst + sx<C>(uo);
 #pragma unroll
@@ -333,6 +350,12 @@ __device__ __forceinline__ void stockham_stage(const C *src, C *dst, int L, int 
             for (int r = 0; r < RAD; r++) dst[sx<C>(uo + r * so)] = v[r];
         }
     }
+}
+
+template <bool INV, int RAD, typename C>
+__device__ __forceinline__ void stockham_stage(const C *src, C *dst, int L, int nb, int lognb,
+                                               const FastDiv &nsd, const C *__restrict__ tws) {
+    stockham_stage_g<INV, RAD>(src, dst, RtGeo{L, nb, lognb, nsd}, tws);
 }
 
 // Generic odd-prime radix (O(p^2), runtime p <= kMaxGenericRadix).
@@ -391,6 +414,23 @@ __device__ C *block_fft(C *a, C *b, int nb, int lognb, const FftPlanDev &pl, con
         dst = tmp;
     }
     return src;
+}
+
+// The three-stage transform of a length whose plan (make_plan) is radices
+// R0, R1, R2, over NB interleaved rows, with the geometry fixed at compile
+// time: the same stages and twiddle tables as block_fft, so the results are
+// the same.  Returns the buffer holding the result (b).
+template <bool INV, int L, int NB, int R0, int R1, int R2, typename C>
+__device__ C *block_fft_ct(C *a, C *b, const FftPlanDev &pl) {
+    static_assert(R0 * R1 * R2 == L, "radices must multiply to the length");
+    const C *__restrict__ tws = static_cast<const C *>(pl.tws);
+    stockham_stage_g<INV, R0>(a, b, CtGeo<L, NB, 1>{}, tws + pl.twoff[0]);
+    __syncthreads();
+    stockham_stage_g<INV, R1>(b, a, CtGeo<L, NB, R0>{}, tws + pl.twoff[1]);
+    __syncthreads();
+    stockham_stage_g<INV, R2>(a, b, CtGeo<L, NB, R0 * R1>{}, tws + pl.twoff[2]);
+    __syncthreads();
+    return b;
 }
 
 }  // namespace ndconv

@@ -27,6 +27,7 @@
 #include <map>
 #include <string>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -335,12 +336,31 @@ __device__ __forceinline__ void mac_group(const RowArgs<T> &A, const typename Ro
 
 // One CTA's share of a row pass: rows [bx * nb, bx * nb + nb) of instance by
 // (ROW_INV_MAC: the group of nb output rows bx, see prep_row).
-template <typename T, int MODE>
+// The row transform: the compile-time geometry for a specialised length FL
+// (FNB rows per CTA), else the run-time one.
+template <bool INV, int FL, int FNB, typename C>
+__device__ __forceinline__ C *row_fft(C *a, C *b, int nb, int lognb, const FftPlanDev &pl, const C *tw) {
+    if constexpr (FL == 2560) return block_fft_ct<INV, 2560, FNB, 16, 16, 10>(a, b, pl);
+    else return block_fft<INV>(a, b, nb, lognb, pl, tw);
+}
+
+// Lengths whose row transforms are specialised at compile time (their plan
+// must be the one make_plan gives them): 2560-point complex transforms, the
+// 5120-sample real rows of the benchmark cases, in CTAs of one or two rows.
+// Same arithmetic as the run-time path; only the index computations fold.
+template <typename T> __device__ __forceinline__ int fixed_rows(const RowArgs<T> &A) {
+    if constexpr (std::is_same<T, float>::value) {
+        if (A.pl.L == 2560 && A.pl.nst == 3 && (A.nb == 1 || A.nb == 2)) return A.nb;
+    }
+    return 0;
+}
+
+template <typename T, int MODE, int FL = 0, int FNB = 0>
 __device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsigned by, unsigned char *smem_raw) {
     using C = typename RowArgs<T>::C;
     using R = typename RowArgs<T>::R;
-    const int nb = A.nb, lognb = A.lognb;
-    const int M = A.pl.L;  // transform length
+    const int nb = FL ? FNB : A.nb, lognb = FL ? (FNB == 2 ? 1 : 0) : A.lognb;
+    const int M = FL ? FL : A.pl.L;  // transform length
     const int cap = (int)padded_slots<C>((int64_t)(A.kind == RK_REAL_EVEN ? M + 1 : M) << lognb);
     RowInfo *rinfo = reinterpret_cast<RowInfo *>(smem_raw);
     C *buf0 = reinterpret_cast<C *>(smem_raw + ((sizeof(RowInfo) * nb + 15) / 16) * 16);
@@ -480,7 +500,7 @@ __device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsi
         }
         if (fastrow) cp_async_wait_all();
         __syncthreads();
-        res = block_fft<false>(buf0, buf1, nb, lognb, A.pl, A.tw);
+        res = row_fft<false, FL, FNB>(buf0, buf1, nb, lognb, A.pl, A.tw);
         C *other = (res == buf0) ? buf1 : buf0;
         const int H = (int)A.H;
         if constexpr (MODE != ROW_FUSED) {
@@ -517,12 +537,12 @@ __device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsi
                 if (k != 0 && km != k) res[s1] = c2r_bin(x1, x0, ldg_c(A.twF + km), false);
             }
             __syncthreads();
-            res = block_fft<true>(res, other, nb, lognb, A.pl, A.tw);
+            res = row_fft<true, FL, FNB>(res, other, nb, lognb, A.pl, A.tw);
         } else {
             const int tot = H << lognb;
             for (int u = threadIdx.x; u < tot; u += blockDim.x) res[sx<C>(u)] = cmul(res[sx<C>(u)], ldcg_c(kspec + (u >> lognb)));
             __syncthreads();
-            res = block_fft<true>(res, other, nb, lognb, A.pl, A.tw);
+            res = row_fft<true, FL, FNB>(res, other, nb, lognb, A.pl, A.tw);
         }
     } else {
         // ---- inverse: spectrum rows (real rows of even length: c2r
@@ -571,7 +591,7 @@ __device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsi
             }
             __syncthreads();
         }
-        res = block_fft<true>(buf0, buf1, nb, lognb, A.pl, A.tw);
+        res = row_fft<true, FL, FNB>(buf0, buf1, nb, lognb, A.pl, A.tw);
     }
     // ---- store time-domain samples (scaled; cropped + strided for INV_OUT / FUSED)
     constexpr bool plain = (MODE == ROW_INV_PLAIN);
@@ -612,6 +632,11 @@ __device__ __forceinline__ void row_block(const RowArgs<T> &A, unsigned bx, unsi
 template <typename T, int MODE, int MAXT>
 __global__ void __launch_bounds__(MAXT, 2) row_kernel(const __grid_constant__ RowArgs<T> A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    if constexpr (std::is_same<T, float>::value && MODE != ROW_FWD_PLAIN && MODE != ROW_INV_PLAIN) {
+        const int f = fixed_rows(A);
+        if (f == 1) return row_block<T, MODE, 2560, 1>(A, blockIdx.x, blockIdx.y, smem_raw);
+        if (f == 2) return row_block<T, MODE, 2560, 2>(A, blockIdx.x, blockIdx.y, smem_raw);
+    }
     row_block<T, MODE>(A, blockIdx.x, blockIdx.y, smem_raw);
 }
 
@@ -875,8 +900,13 @@ template <typename T, int MAXT>
 __global__ void __launch_bounds__(MAXT, 2) row_pair_kernel(const __grid_constant__ RowArgs<T> A,
                                                             const __grid_constant__ RowArgs<T> B, unsigned ga) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    if (blockIdx.x < ga) row_block<T, ROW_FWD_KERNEL>(A, blockIdx.x, blockIdx.y, smem_raw);
-    else row_block<T, ROW_FWD_DATA>(B, blockIdx.x - ga, blockIdx.y, smem_raw);
+    if (blockIdx.x < ga) {
+        if (fixed_rows(A) == 1) row_block<T, ROW_FWD_KERNEL, 2560, 1>(A, blockIdx.x, blockIdx.y, smem_raw);
+        else row_block<T, ROW_FWD_KERNEL>(A, blockIdx.x, blockIdx.y, smem_raw);
+    } else {
+        if (fixed_rows(B) == 1) row_block<T, ROW_FWD_DATA, 2560, 1>(B, blockIdx.x - ga, blockIdx.y, smem_raw);
+        else row_block<T, ROW_FWD_DATA>(B, blockIdx.x - ga, blockIdx.y, smem_raw);
+    }
 }
 
 template <typename T> int launch_row_pair(RowArgs<T> A, RowArgs<T> B, cudaStream_t st, int n_inst) {
