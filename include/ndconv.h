@@ -294,6 +294,29 @@ uint64_t ndconv_kernel_launches(void);
  * reference; used by dispatchers. */
 int ndconv_plan_info(const ndconv_problem *p, double out[8]);
 
+/* Tile and plan parameters inside one algorithm, for the autotuner (no
+ * reference counterpart).  Thread-local; value 0 (the default) lets the
+ * library choose.  The FFT knobs never change results; the direct and
+ * tensor-core ones may change the last bits (another summation chunking),
+ * always within the same error bound.  Knob values that do not apply to a
+ * problem are ignored for it.
+ *   NDCONV_TUNE_SW_TY       output rows per CTA of the sliding-window direct
+ *                           kernel (1, 2, 4, 8; at most 8 / dilation phases)
+ *   NDCONV_TUNE_MAC_ROWS    output rows per CTA of the FFT spectral tap sum
+ *                           (1, 2, 4, 8)
+ *   NDCONV_TUNE_ROW_THREADS threads of FFT row-pass CTAs in launches of many
+ *                           CTAs (a multiple of 32, at most 512)
+ *   NDCONV_TUNE_BF16X3_BN   output rows per tensor-core tile (32 or 64) */
+typedef enum {
+    NDCONV_TUNE_SW_TY = 0,
+    NDCONV_TUNE_MAC_ROWS = 1,
+    NDCONV_TUNE_ROW_THREADS = 2,
+    NDCONV_TUNE_BF16X3_BN = 3,
+    NDCONV_TUNE_COUNT = 4
+} ndconv_tune_knob;
+int ndconv_set_tuning(int32_t knob, int32_t value);
+int32_t ndconv_get_tuning(int32_t knob);
+
 /* Message for the last non-OK status returned on this thread. */
 const char *ndconv_last_error(void);
 

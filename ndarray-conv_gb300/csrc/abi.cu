@@ -24,6 +24,18 @@ void ndconv_count_launch(uint64_t n) { g_launches.fetch_add(n, std::memory_order
 
 extern "C" uint64_t ndconv_kernel_launches(void) { return g_launches.load(); }
 
+namespace {
+thread_local int32_t g_tune[NDCONV_TUNE_COUNT] = {0, 0, 0, 0};
+}
+int ndconv_tune(int knob) { return (knob >= 0 && knob < NDCONV_TUNE_COUNT) ? g_tune[knob] : 0; }
+extern "C" int ndconv_set_tuning(int32_t knob, int32_t value) {
+    if (knob < 0 || knob >= NDCONV_TUNE_COUNT || value < 0)
+        return ndconv_fail(NDCONV_ERR_INVALID, "unknown tuning knob or negative value");
+    g_tune[knob] = value;
+    return NDCONV_OK;
+}
+extern "C" int32_t ndconv_get_tuning(int32_t knob) { return ndconv_tune(knob); }
+
 cudaError_t ndconv_allow_smem(const void *kernel, int bytes) {
     static std::mutex mu;
     static std::set<std::pair<int, std::pair<const void *, int>>> done;

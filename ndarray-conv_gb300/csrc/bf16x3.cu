@@ -411,7 +411,9 @@ extern "C" int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, con
     };
     // 64-row tiles, or 32 when 64 would give fewer than two CTAs per SM
     const int64_t nseg = (A[2].out + BM - 1) / BM;
-    const int BN = (nseg * ((A[1].out + 63) / 64) * A[0].out < 2 * 152) ? 32 : 64;
+    int BN = (nseg * ((A[1].out + 63) / 64) * A[0].out < 2 * 152) ? 32 : 64;
+    const int want_bn = ndconv_tune(NDCONV_TUNE_BF16X3_BN);  // the autotuner's choice
+    if (want_bn == 32 || want_bn == 64) BN = want_bn;
     CUtensorMap mAh, mAl, mBh, mBl;
     {
         const cuuint64_t dA[2] = {(cuuint64_t)Cpad, (cuuint64_t)(L * BM)};

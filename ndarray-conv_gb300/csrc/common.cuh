@@ -190,6 +190,8 @@ __host__ __device__ __forceinline__ int64_t tap_source(int64_t t, int64_t K, int
 
 // Host helpers implemented in abi.cu
 int ndconv_fail(int status, const char *msg);
+// The calling thread's tuning knob (ndconv_set_tuning; 0: automatic).
+int ndconv_tune(int knob);
 void ndconv_count_launch(uint64_t n = 1);
 // Opt a kernel into `bytes` of dynamic shared memory on the current device
 // (once per device and kernel).

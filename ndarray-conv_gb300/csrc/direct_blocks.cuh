@@ -538,6 +538,9 @@ template <typename T> bool plan_sw(DirectParams<T> &P, int RX) {
     const int lines = 8 / D;
     int TY = 1;
     while (TY * 2 <= lines && TY * 2 <= A1.out) TY *= 2;
+    // the autotuner's choice of rows per CTA, where it fits the 8 warp lines
+    const int want_ty = ndconv_tune(NDCONV_TUNE_SW_TY);
+    if (want_ty > 0 && want_ty <= lines && (want_ty & (want_ty - 1)) == 0) TY = want_ty;
     const int SEGW = 32 * RX;
     int NSEG = lines / TY;
     const int64_t segs_needed = (A2.out + (int64_t)D * SEGW - 1) / ((int64_t)D * SEGW);

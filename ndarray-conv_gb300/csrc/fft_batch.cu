@@ -482,7 +482,7 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
             if (A.n_rows <= 0) return NDCONV_OK;
             int64_t grid;
             size_t sm;
-            int s2 = prep_row(A, 1, grid, sm, kBatchSmem);
+            int s2 = prep_row(A, 1, grid, sm, kBatchSmem, false);
             if (s2) return s2;
             if (sm > kBatchSmem) too_big = true;
             inst_smem = std::max(inst_smem, sm);

@@ -788,6 +788,7 @@ int pick_nb(int64_t len, int64_t rows, size_t per_row_bytes, size_t cap) {
 // (kMacSmem): measured on 2560-point rows, two rows per CTA (two CTAs per
 // SM) ran 12 % faster than one, four rows (one CTA per SM) 15 % slower.
 constexpr size_t kMacSmem = 110 * 1024;
+constexpr int64_t kFillCtas = 2 * 152;  // two CTAs per SM of a GB300
 int mac_rows_target() {
     static int v = 0;
     if (!v) {
@@ -806,7 +807,11 @@ int mac_rows_target() {
 // throughput-bound: 256, which keeps more CTAs resident, or 512 when shared
 // memory leaves room for at most two CTAs per SM.
 template <typename T> int row_threads(const RowArgs<T> &A, int64_t ctas, size_t sm) {
-    if (ctas > kFewCtas) return sm > kSmemPerSm / 3 ? 512 : kThreads;
+    if (ctas > kFewCtas) {
+        const int t = ndconv_tune(NDCONV_TUNE_ROW_THREADS);  // the autotuner's choice
+        if (t >= 32 && t <= 512 && t % 32 == 0 && t % A.nb == 0) return t;
+        return sm > kSmemPerSm / 3 ? 512 : kThreads;
+    }
     int maxw = 0;
     for (int i = 0; i < A.pl.nst; i++) maxw = std::max(maxw, (A.pl.L / A.pl.rad[i]) << A.lognb);
     if (maxw < 128 || maxw > kFewThreads) return kThreads;
@@ -842,7 +847,8 @@ template <typename T, int MODE> int launch_row_mode(const RowArgs<T> &A, size_t 
 // output rows: CTA = (axis-0 index and segment, residue class c of o1 mod
 // mac_g, group), rows o1 = c + mac_g (group nb + b); mac_g = d1 / s1 when
 // s1 divides d1 (the rows then share a window of data rows), else 1.
-template <typename T> int prep_row(RowArgs<T> &A, int n_inst, int64_t &grid, size_t &sm, size_t cap = kFftSmemMax) {
+template <typename T>
+int prep_row(RowArgs<T> &A, int n_inst, int64_t &grid, size_t &sm, size_t cap = kFftSmemMax, bool fill = true) {
     using C = typename RowArgs<T>::C;
     const size_t per_row = sizeof(C) * 2 * padded_slots<C>(A.pl.L + 1) + sizeof(RowInfo);
     int64_t rows = A.n_rows;
@@ -856,8 +862,23 @@ template <typename T> int prep_row(RowArgs<T> &A, int n_inst, int64_t &grid, siz
     }
     A.nb = pick_nb(A.pl.L, rows, per_row, std::min(cap, kFftSmemMax));
     if (A.mode == ROW_INV_MAC) {
-        while (A.nb < mac_rows_target() && A.nb * 2 <= rows + 1 && per_row * A.nb * 2 <= std::min(cap, kMacSmem))
-            A.nb *= 2;
+        if (const int t = ndconv_tune(NDCONV_TUNE_MAC_ROWS)) {
+            // the autotuner's rows per CTA, as far as rows and shared memory allow
+            A.nb = 1;
+            while (A.nb < t && A.nb * 2 <= rows + 1 && per_row * A.nb * 2 <= std::min(cap, kFftSmemMax)) A.nb *= 2;
+        } else {
+            while (A.nb < mac_rows_target() && A.nb * 2 <= rows + 1 && per_row * A.nb * 2 <= std::min(cap, kMacSmem))
+                A.nb *= 2;
+            // a launch of its own should still give every SM two CTAs: fewer
+            // rows per CTA for small problems (timed over 3,000 random
+            // problems: one row per CTA is 1.06x the best grouping in the
+            // geometric mean, the shared-kernel-row grouping 1.25x, while
+            // large problems want the grouping)
+            const int64_t sn = A.seg_n > 1 ? A.seg_n : 1;
+            const int64_t outer = A.n_rows / (A.n1 * sn);
+            while (fill && A.nb > 1 && outer * sn * A.mac_g * ((rows + A.nb - 1) / A.nb) * n_inst < kFillCtas)
+                A.nb /= 2;
+        }
         A.mac_gc = (rows + A.nb - 1) / A.nb;
     }
     A.lognb = ilog2(A.nb);

@@ -28,6 +28,9 @@ ERR_INVALID = 6
 ERR_CUDA = 7
 ERR_TIMEOUT = 8
 ERR_NO_MEMORY = 9
+
+# ndconv_tune_knob
+TUNE_SW_TY, TUNE_MAC_ROWS, TUNE_ROW_THREADS, TUNE_BF16X3_BN = 0, 1, 2, 3
 STATUS_NAMES = {
     0: "OK", 1: "DATA_SHAPE", 2: "KERNEL_SHAPE", 3: "MISMATCH_SHAPE",
     4: "PAD_OUT_OF_RANGE", 5: "UNSUPPORTED", 6: "INVALID", 7: "CUDA",
@@ -106,6 +109,8 @@ def lib():
         "ndconv_batch_set_wait_limit": (ctypes.c_int, [vp, ctypes.c_int64]),
         "ndconv_batch_stall_one_wait": (ctypes.c_int, [vp, i32]),
         "ndconv_bf16x3_status": (ctypes.c_int, [vp]),
+        "ndconv_set_tuning": (ctypes.c_int, [i32, i32]),
+        "ndconv_get_tuning": (ctypes.c_int32, [i32]),
         "ndconv_batch_info": (ctypes.c_int, [vp, i64p]),
         "ndconv_batch_destroy": (ctypes.c_int, [vp]),
         "ndconv_plan_info": (ctypes.c_int, [pp, ctypes.POINTER(ctypes.c_double)]),

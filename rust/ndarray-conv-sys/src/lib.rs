@@ -58,6 +58,12 @@ pub const NDCONV_ALGO_FFT_RS: i32 = 4;
 pub const NDCONV_ALGO_FFT_ND_POW2: i32 = 5;
 pub const NDCONV_ALGO_FFT_RS_POW2: i32 = 6;
 
+// ---- ndconv_tune_knob
+pub const NDCONV_TUNE_SW_TY: i32 = 0;
+pub const NDCONV_TUNE_MAC_ROWS: i32 = 1;
+pub const NDCONV_TUNE_ROW_THREADS: i32 = 2;
+pub const NDCONV_TUNE_BF16X3_BN: i32 = 3;
+
 pub const NDCONV_MAX_RANK: usize = 3;
 
 /// `struct ndconv_problem` of include/ndconv.h (same field order and types).
@@ -139,6 +145,10 @@ extern "C" {
     /// Kernels this library launched in the process so far.
     pub fn ndconv_kernel_launches() -> u64;
     pub fn ndconv_plan_info(p: *const ndconv_problem, out: *mut f64) -> i32;
+    /// Thread-local tile / plan knob for the autotuner (0: the library chooses).
+    pub fn ndconv_set_tuning(knob: i32, value: i32) -> i32;
+    /// The knob's current value (not a status).
+    pub fn ndconv_get_tuning(knob: i32) -> i32;
     /// The calling thread's last error message (never null).
     pub fn ndconv_last_error() -> *const c_char;
     pub fn ndconv_version() -> *const c_char;
