@@ -141,6 +141,7 @@ __device__ __forceinline__ void direct_sw_block(const T *__restrict__ x0, const 
     int64_t *mcol = mrow + P.max_rows;
     int64_t *rowoff = mcol + P.max_cols;
     int *zrow = reinterpret_cast<int *>(rowoff + P.max_rows);
+    int *dcol = zrow + P.cky;  // per staged column: its slot in a staged row
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int nlines = TY * NSEG * D;
     const int ty = warp / (NSEG * D);
@@ -187,6 +188,9 @@ __device__ __forceinline__ void direct_sw_block(const T *__restrict__ x0, const 
                     const int rem = i - m * SD;
                     const int rho = rem / D, ph = rem - rho * D;
                     mcol[i] = axis_map(A2, col0 + rho * d2 + s2 * (ph + (int64_t)D * m));
+                    // swizzled slot (rho * D + phi) * PH + (m mod RX) * Q + m / RX, worked
+                    // out once per column instead of once per staged element
+                    dcol[i] = rem * PH + (m & (RX - 1)) * Q + m / RX;
                 }
                 for (int i = tid; i < cky; i += blockDim.x) zrow[i] = 0;
                 __syncthreads();
@@ -211,9 +215,7 @@ __device__ __forceinline__ void direct_sw_block(const T *__restrict__ x0, const 
                         const int64_t mc = mcol[cc];
                         const T v = (ro >= 0 && mc >= 0) ? x[ro + mc * xs2]
                                                          : resolve_padded<T>(x, P.g, mz, mrow[rr], mc);
-                        const int m = (SD == 1) ? cc : cc / SD;
-                        const int rp = cc - m * SD;  // rho * D + phi
-                        trow[rp * PH + (m & (RX - 1)) * Q + m / RX] = v;
+                        trow[dcol[cc]] = v;
                     }
                 }
                 __syncthreads();
@@ -231,11 +233,15 @@ __device__ __forceinline__ void direct_sw_block(const T *__restrict__ x0, const 
                             for (int t0 = 0; t0 < ckr; t0 += CKX) {
                                 T win[RX + CKX - 1];
                                 const T *pw = prow + t0 / RX;
-#pragma unroll
-                                for (int q = 0; q < RX + CKX - 1; q++)
-                                    win[q] = (t0 + q < ckr + RX - 1) ? pw[(q % RX) * Q + q / RX] : E::zero();
                                 if (t0 + CKX <= ckr && !zrow[a]) {
-                                    // full chunk without zero taps: no per-tap branches
+                                    // full chunk without zero taps: every window element
+                                    // exists, no per-tap branches; one base pointer per
+                                    // window residue, the rest immediate offsets
+                                    const T *pr[RX];
+#pragma unroll
+                                    for (int r = 0; r < RX; r++) pr[r] = pw + r * Q;
+#pragma unroll
+                                    for (int q = 0; q < RX + CKX - 1; q++) win[q] = pr[q % RX][q / RX];
 #pragma unroll
                                     for (int t = 0; t < CKX; t++) {
                                         const T w = wrow[t0 + t];
@@ -243,6 +249,9 @@ __device__ __forceinline__ void direct_sw_block(const T *__restrict__ x0, const 
                                         for (int r = 0; r < RX; r++) E::mac(acc[r], win[r + t], w);
                                     }
                                 } else {
+#pragma unroll
+                                    for (int q = 0; q < RX + CKX - 1; q++)
+                                        win[q] = (t0 + q < ckr + RX - 1) ? pw[(q % RX) * Q + q / RX] : E::zero();
 #pragma unroll
                                     for (int t = 0; t < CKX; t++) {
                                         if (t0 + t < ckr) {
@@ -462,9 +471,9 @@ constexpr int kMaxCols = 2048;
 constexpr size_t kSmemBudget = 96 * 1024;
 
 template <typename T> size_t smem_bytes(const DirectParams<T> &P) {
-    // row maps, column maps, row data offsets and per-row zero-tap flags
-    // (the last two used by the sliding-window kernel)
-    return (size_t)P.maps_off + sizeof(int64_t) * (2 * P.max_rows + P.max_cols) + sizeof(int) * P.cky;
+    // row maps, column maps, row data offsets, per-row zero-tap flags and
+    // per-column staging slots (the last three used by the sliding-window kernel)
+    return (size_t)P.maps_off + sizeof(int64_t) * (2 * P.max_rows + P.max_cols) + sizeof(int) * (P.cky + P.max_cols);
 }
 
 // Pick block shape and tap chunks so the staged window fits in shared
@@ -552,7 +561,7 @@ template <typename T> bool plan_sw(DirectParams<T> &P, int RX) {
         rows = (TY - 1) * A1.s + (cky - 1) * A1.d + 1;
         cols = (int64_t)S * D * (NSEG * SEGW + tr - 1);
         return sizeof(T) * (rows * rowe + cky * S * tr) + 16 + sizeof(int64_t) * (2 * rows + cols) +
-               sizeof(int) * cky;
+               sizeof(int) * (cky + cols);
     };
     int Q;
     int64_t rows, cols, rowe;
