@@ -300,19 +300,24 @@ int ndconv_plan_info(const ndconv_problem *p, double out[8]);
  * tensor-core ones may change the last bits (another summation chunking),
  * always within the same error bound.  Knob values that do not apply to a
  * problem are ignored for it.
- *   NDCONV_TUNE_SW_TY       output rows per CTA of the sliding-window direct
- *                           kernel (1, 2, 4, 8; at most 8 / dilation phases)
+ *   NDCONV_TUNE_SW_TY       warp row sets per CTA of the sliding-window
+ *                           direct kernel (1, 2, 4, 8; at most 8 / dilation
+ *                           phases)
  *   NDCONV_TUNE_MAC_ROWS    output rows per CTA of the FFT spectral tap sum
  *                           (1, 2, 4, 8)
  *   NDCONV_TUNE_ROW_THREADS threads of FFT row-pass CTAs in launches of many
  *                           CTAs (a multiple of 32, at most 512)
- *   NDCONV_TUNE_BF16X3_BN   output rows per tensor-core tile (32 or 64) */
+ *   NDCONV_TUNE_BF16X3_BN   output rows per tensor-core tile (32 or 64)
+ *   NDCONV_TUNE_SW_RY       output rows per warp of the sliding-window
+ *                           direct kernel (1, 2 or 4; f64 / c32 at most 2,
+ *                           c64 1) */
 typedef enum {
     NDCONV_TUNE_SW_TY = 0,
     NDCONV_TUNE_MAC_ROWS = 1,
     NDCONV_TUNE_ROW_THREADS = 2,
     NDCONV_TUNE_BF16X3_BN = 3,
-    NDCONV_TUNE_COUNT = 4
+    NDCONV_TUNE_SW_RY = 4,
+    NDCONV_TUNE_COUNT = 5
 } ndconv_tune_knob;
 int ndconv_set_tuning(int32_t knob, int32_t value);
 int32_t ndconv_get_tuning(int32_t knob);

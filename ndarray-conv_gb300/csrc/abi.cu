@@ -25,7 +25,7 @@ void ndconv_count_launch(uint64_t n) { g_launches.fetch_add(n, std::memory_order
 extern "C" uint64_t ndconv_kernel_launches(void) { return g_launches.load(); }
 
 namespace {
-thread_local int32_t g_tune[NDCONV_TUNE_COUNT] = {0, 0, 0, 0};
+thread_local int32_t g_tune[NDCONV_TUNE_COUNT] = {};
 }
 int ndconv_tune(int knob) { return (knob >= 0 && knob < NDCONV_TUNE_COUNT) ? g_tune[knob] : 0; }
 extern "C" int ndconv_set_tuning(int32_t knob, int32_t value) {

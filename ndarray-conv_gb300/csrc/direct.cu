@@ -47,7 +47,7 @@ cudaError_t launch_main(const T *x, const T *k, T *y, DirectParams<T> &P, cudaSt
     if (!force_naive && grid_ok && A1.out < 65536 && !sw_disabled()) {
         // unit x-stride: sliding register windows
         constexpr int SRX = (sizeof(T) <= 4) ? 8 : 4;
-        if (plan_sw(P, SRX)) return launch_sw<T, SRX, 2 * SRX>(x, k, y, P, st, n_inst);
+        if (plan_sw(P, SRX, n_inst)) return launch_sw<T, SRX, 2 * SRX>(x, k, y, P, st, n_inst);
     }
     if (!force_naive && grid_ok) {
         if (plan_tile(P, 4, BX, BY)) return launch_tile<T, 4>(x, k, y, P, BX, BY, st, n_inst);

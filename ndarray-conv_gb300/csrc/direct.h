@@ -14,6 +14,7 @@ template <typename T> struct DirectParams {
     int64_t maps_off;        // byte offset of the int64 border maps in shared memory
     int sw_ty, sw_nseg, sw_q;  // sliding-window tiling (rows, segments, swizzle pitch)
     int sw_ph, sw_res, sw_tr;  // x phases d/g, tap residues s/g (g = gcd(s, d)), tap slots per residue
+    int sw_ry, sw_h;           // output rows per warp line; staged-row step (in d1) between them
     int tile_bx, tile_by;      // tiled kernel block shape
     // batch: device arrays of per-instance pointers (null for one instance)
     const T *const *xs;

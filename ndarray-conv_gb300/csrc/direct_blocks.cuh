@@ -1,6 +1,7 @@
 // Direct-convolution CTA bodies and their tile planners, shared by the
 // standalone kernels (direct.cu) and the persistent batch kernel.
 #pragma once
+#include <cstring>
 #include <type_traits>
 #include <vector>
 
@@ -102,6 +103,33 @@ __global__ void __launch_bounds__(256) direct_tile_kernel(const T *__restrict__ 
     direct_tile_block<T, RX>(x0, k0, y0, P, blockIdx.x, blockIdx.y, blockIdx.z, smem_raw);
 }
 
+// CKX consecutive tap weights from shared memory as 16-byte vectors (the
+// weight slots are 16-byte aligned and padded to whole chunks).
+template <typename T, int N> __device__ __forceinline__ void load_taps(T (&w)[N], const T *p) {
+    static_assert(sizeof(T) <= 16 && 16 % sizeof(T) == 0, "tap vectors hold whole elements");
+    constexpr int PER = 16 / sizeof(T);
+    static_assert(N % PER == 0, "tap chunks are whole vectors");
+#pragma unroll
+    for (int v = 0; v < N / PER; v++) {
+        const uint4 u = reinterpret_cast<const uint4 *>(p)[v];
+        memcpy(&w[v * PER], &u, 16);
+    }
+}
+
+// One element global -> shared without passing through registers
+// (cp.async, completed by cp.async.wait_all); 4-byte pieces, so only the
+// element types' natural 4-byte alignment is assumed.
+template <typename T> __device__ __forceinline__ void stage_async(T *smem, const T *gmem) {
+    static_assert(sizeof(T) % 4 == 0, "elements of whole 4-byte words");
+#pragma unroll
+    for (int b = 0; b < (int)sizeof(T); b += 4) {
+        const unsigned sa = (unsigned)__cvta_generic_to_shared(reinterpret_cast<char *>(smem) + b);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa),
+                     "l"(reinterpret_cast<const char *>(gmem) + b)
+                     : "memory");
+    }
+}
+
 // Sliding-window variant along the contiguous axis, any stride s and
 // dilation d (g = gcd(s, d), D = d / g phases, S = s / g tap residues).
 // Output ox = X0 + phi + D j, tap u = rho + S t of a chunk starting at kx0
@@ -110,12 +138,17 @@ __global__ void __launch_bounds__(256) direct_tile_kernel(const T *__restrict__ 
 // 1-D correlation over the decimated sequence
 //   G[rho][phi][m] = row[X0 s + kx0 d + rho d + s (phi + D m)]
 // with the taps rho, rho + S, ...  (s = 1: one residue, D = d phases).  A
-// warp owns one (output row, phase, segment) line of 32 * RX outputs; lane
-// l owns RX consecutive phase outputs j = l*RX + r and slides a register
-// window over G, so each shared-memory load feeds up to CKX FMAs.  G is
+// warp owns one (row set, phase, segment) line: RY output rows
+// oy0 + ty + i TY (i < RY), 32 * RX outputs of each; lane l owns RX
+// consecutive phase outputs j = l*RX + r of every row and slides a register
+// window over G, so each shared-memory load feeds up to CKX FMAs per row.
+// When TY s1 = H d1 the rows' input rows coincide: row i under kernel row a
+// reads staged row ty s1 + (i H + a) d1, so one window serves every (i, a)
+// with i H + a = j, and each staged row feeds up to RY kernel rows.  G is
 // stored swizzled (element m at (m % RX) * Q + m / RX) so the lanes' window
-// loads hit consecutive banks.
-template <typename T, int RX, int CKX>
+// loads hit consecutive banks.  Every output accumulates its taps in the
+// same order whatever TY and RY are: kz, then ky, then (residue, kx).
+template <typename T, int RX, int CKX, int RYM>
 __device__ __forceinline__ void direct_sw_block(const T *__restrict__ x0, const T *__restrict__ k0,
                                                 T *__restrict__ y0, const DirectParams<T> &P, unsigned bx,
                                                 unsigned by, unsigned bz, unsigned char *smem_raw) {
@@ -128,9 +161,10 @@ __device__ __forceinline__ void direct_sw_block(const T *__restrict__ x0, const 
     T *__restrict__ y = P.ys ? P.ys[P.inst_base + inst] : (P.y1 ? P.y1 : y0);
     const int D = P.sw_ph;              // phases
     const int S = P.sw_res;             // tap residues
-    const int TR = P.sw_tr;             // weight slots per residue
+    const int TR = P.sw_tr;             // weight slots per residue (whole CKX chunks)
     const int SD = S * D;
     const int TY = P.sw_ty, NSEG = P.sw_nseg;
+    const int RY = P.sw_ry, H = P.sw_h;  // rows per line, staged-row step between them
     const int SEGW = 32 * RX;           // phase outputs per line
     const int Q = P.sw_q;               // swizzle pitch
     const int PH = RX * Q;              // smem elements per (residue, phase) of one row
@@ -148,15 +182,17 @@ __device__ __forceinline__ void direct_sw_block(const T *__restrict__ x0, const 
     const int sg = (warp / D) % NSEG;
     const int phi = warp % D;
     const int64_t oz = bz - inst * A0.out;
-    const int64_t oy0 = (int64_t)by * TY;
+    const int64_t oy0 = (int64_t)by * TY * RY;
     const int64_t TXo = (int64_t)NSEG * D * SEGW;
     const int64_t X0 = (int64_t)bx * TXo;
     const int s1 = (int)A1.s, d1 = (int)A1.d;
     const int64_t s2 = A2.s, d2 = A2.d;
 
-    Acc acc[RX];
+    Acc acc[RYM][RX];
 #pragma unroll
-    for (int r = 0; r < RX; r++) acc[r] = E::zero();
+    for (int i = 0; i < RYM; i++)
+#pragma unroll
+        for (int r = 0; r < RX; r++) acc[i][r] = E::zero();
 
     // live taps only (taps outside [t_lo, t_lo + t_n) read padding zeros for every output)
     const int64_t kz_end = P.t_lo[0] + P.t_n[0], ky_end = P.t_lo[1] + P.t_n[1], kx_end = P.t_lo[2] + P.t_n[2];
@@ -166,7 +202,7 @@ __device__ __forceinline__ void direct_sw_block(const T *__restrict__ x0, const 
         for (int64_t ky0 = P.t_lo[1]; ky0 < ky_end; ky0 += P.cky) {
             const int cky = (int)(P.cky < ky_end - ky0 ? P.cky : ky_end - ky0);
             const int64_t row0 = oy0 * s1 + ky0 * d1;
-            const int nrows = (TY - 1) * s1 + (cky - 1) * d1 + 1;
+            const int nrows = (TY * RY - 1) * s1 + (cky - 1) * d1 + 1;
             for (int64_t kx0 = P.t_lo[2]; kx0 < kx_end; kx0 += P.ckx) {
                 const int ckx = (int)(P.ckx < kx_end - kx0 ? P.ckx : kx_end - kx0);
                 const int tr0 = (ckx + S - 1) / S;          // taps of residue 0 (the most)
@@ -207,58 +243,69 @@ __device__ __forceinline__ void direct_sw_block(const T *__restrict__ x0, const 
                     wsm[i] = w;
                 }
                 __syncthreads();
+                // every interior sample is copied asynchronously (all of a
+                // thread's copies in flight at once); border samples are
+                // resolved and stored
                 const int64_t xs2 = A2.xs;
-                for (int rr = 0; rr < nrows; rr++) {
-                    const int64_t ro = rowoff[rr];
-                    T *trow = tile + rr * ROWE;
-                    for (int cc = tid; cc < ncols; cc += blockDim.x) {
-                        const int64_t mc = mcol[cc];
-                        const T v = (ro >= 0 && mc >= 0) ? x[ro + mc * xs2]
-                                                         : resolve_padded<T>(x, P.g, mz, mrow[rr], mc);
-                        trow[dcol[cc]] = v;
+                for (int cc = tid; cc < ncols; cc += blockDim.x) {
+                    const int64_t mc = mcol[cc];
+                    T *dst = tile + dcol[cc];
+                    const T *src = x + mc * xs2;
+                    for (int rr = 0; rr < nrows; rr++) {
+                        const int64_t ro = rowoff[rr];
+                        if (ro >= 0 && mc >= 0) stage_async(dst + rr * ROWE, src + ro);
+                        else dst[rr * ROWE] = resolve_padded<T>(x, P.g, mz, mrow[rr], mc);
                     }
                 }
+                asm volatile("cp.async.wait_all;\n" ::: "memory");
                 __syncthreads();
                 if (warp < nlines) {
                     // lane's first decimated element is a multiple of RX, and so is
                     // every chunk start t0, so element jbase + t0 + q sits at
                     // (q % RX) * Q + (jbase + t0) / RX + q / RX
                     const int lbase = sg * (SEGW / RX) + lane;
-                    for (int a = 0; a < cky; a++) {
-                        const T *prow_a = tile + (ty * s1 + a * d1) * ROWE + phi * PH + lbase;
+                    const int nj = (RY - 1) * H + cky;  // staged rows this line reads
+                    for (int j = 0; j < nj; j++) {
+                        const T *prow_j = tile + (ty * s1 + j * d1) * ROWE + phi * PH + lbase;
                         for (int rho = 0; rho < S; rho++) {
-                            const T *prow = prow_a + rho * D * PH;
-                            const T *wrow = wsm + (a * S + rho) * TR;
+                            const T *prow = prow_j + rho * D * PH;
                             const int ckr = (ckx - rho + S - 1) / S;  // taps of this residue
                             for (int t0 = 0; t0 < ckr; t0 += CKX) {
                                 T win[RX + CKX - 1];
                                 const T *pw = prow + t0 / RX;
-                                if (t0 + CKX <= ckr && !zrow[a]) {
-                                    // full chunk without zero taps: every window element
-                                    // exists, no per-tap branches; one base pointer per
+                                const bool full = t0 + CKX <= ckr;
+                                if (full) {
+                                    // every window element exists: one base pointer per
                                     // window residue, the rest immediate offsets
                                     const T *pr[RX];
 #pragma unroll
                                     for (int r = 0; r < RX; r++) pr[r] = pw + r * Q;
 #pragma unroll
                                     for (int q = 0; q < RX + CKX - 1; q++) win[q] = pr[q % RX][q / RX];
-#pragma unroll
-                                    for (int t = 0; t < CKX; t++) {
-                                        const T w = wrow[t0 + t];
-#pragma unroll
-                                        for (int r = 0; r < RX; r++) E::mac(acc[r], win[r + t], w);
-                                    }
                                 } else {
 #pragma unroll
                                     for (int q = 0; q < RX + CKX - 1; q++)
                                         win[q] = (t0 + q < ckr + RX - 1) ? pw[(q % RX) * Q + q / RX] : E::zero();
+                                }
 #pragma unroll
-                                    for (int t = 0; t < CKX; t++) {
-                                        if (t0 + t < ckr) {
-                                            const T w = wrow[t0 + t];
-                                            if (!E::is_zero(w)) {
+                                for (int i = 0; i < RYM; i++) {
+                                    const int a = j - i * H;  // kernel row of output row i here
+                                    if (i < RY && a >= 0 && a < cky) {
+                                        T w[CKX];
+                                        load_taps<T, CKX>(w, wsm + (a * S + rho) * TR + t0);
+                                        if (full && !zrow[a]) {
+                                            // no zero taps: no per-tap branches
 #pragma unroll
-                                                for (int r = 0; r < RX; r++) E::mac(acc[r], win[r + t], w);
+                                            for (int t = 0; t < CKX; t++)
+#pragma unroll
+                                                for (int r = 0; r < RX; r++) E::mac(acc[i][r], win[r + t], w[t]);
+                                        } else {
+#pragma unroll
+                                            for (int t = 0; t < CKX; t++) {
+                                                if (t0 + t < ckr && !E::is_zero(w[t])) {
+#pragma unroll
+                                                    for (int r = 0; r < RX; r++) E::mac(acc[i][r], win[r + t], w[t]);
+                                                }
                                             }
                                         }
                                     }
@@ -271,23 +318,33 @@ __device__ __forceinline__ void direct_sw_block(const T *__restrict__ x0, const 
         }
     }
     if (warp < nlines) {
-        const int64_t oy = oy0 + ty;
-        if (oy < A1.out) {
-            T *yrow = y + oz * P.ys_[0] + oy * P.ys_[1];
 #pragma unroll
-            for (int r = 0; r < RX; r++) {
-                const int64_t ox = X0 + phi + (int64_t)(sg * SEGW + lane * RX + r) * D;
-                if (ox < A2.out) yrow[ox * P.ys_[2]] = E::out(acc[r]);
+        for (int i = 0; i < RYM; i++) {
+            const int64_t oy = oy0 + ty + (int64_t)i * TY;
+            if (i < RY && oy < A1.out) {
+                T *yrow = y + oz * P.ys_[0] + oy * P.ys_[1];
+#pragma unroll
+                for (int r = 0; r < RX; r++) {
+                    const int64_t ox = X0 + phi + (int64_t)(sg * SEGW + lane * RX + r) * D;
+                    if (ox < A2.out) yrow[ox * P.ys_[2]] = E::out(acc[i][r]);
+                }
             }
         }
     }
 }
 
-template <typename T, int RX, int CKX>
-__global__ void __launch_bounds__(256) direct_sw_kernel(const T *__restrict__ x0, const T *__restrict__ k0,
-                                                        T *__restrict__ y0, const __grid_constant__ DirectParams<T> P) {
+// Output rows a sliding-window line holds at most, per element type (the
+// accumulators of RY rows stay in registers).
+template <typename T> constexpr int sw_ry_max() { return sizeof(T) <= 4 ? 4 : (sizeof(T) == 8 ? 2 : 1); }
+
+// RYM: rows per line the launch's plan uses (at one row of elements up to
+// 8 bytes the accumulators' registers allow three CTAs per SM).
+template <typename T, int RX, int CKX, int RYM>
+__global__ void __launch_bounds__(256, (RYM == 1 && sizeof(T) <= 8) ? 3 : 2)
+    direct_sw_kernel(const T *__restrict__ x0, const T *__restrict__ k0, T *__restrict__ y0,
+                     const __grid_constant__ DirectParams<T> P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    direct_sw_block<T, RX, CKX>(x0, k0, y0, P, blockIdx.x, blockIdx.y, blockIdx.z, smem_raw);
+    direct_sw_block<T, RX, CKX, RYM>(x0, k0, y0, P, blockIdx.x, blockIdx.y, blockIdx.z, smem_raw);
 }
 
 // Output o (flat, row-major) of one instance, read through the border map
@@ -539,70 +596,179 @@ inline bool sw_axis_ok(const AxisGeom &A2, int &D, int &S) {
     return true;
 }
 
-// Sliding-window tiling: warps = TY rows x NSEG segments x D phases (<= 8).
-template <typename T> bool plan_sw(DirectParams<T> &P, int RX) {
-    const AxisGeom &A1 = P.g.ax[1], &A2 = P.g.ax[2];
-    int D, S;
-    if (!sw_axis_ok(A2, D, S)) return false;
-    const int lines = 8 / D;
-    int TY = 1;
-    while (TY * 2 <= lines && TY * 2 <= A1.out) TY *= 2;
-    // the autotuner's choice of rows per CTA, where it fits the 8 warp lines
-    const int want_ty = ndconv_tune(NDCONV_TUNE_SW_TY);
-    if (want_ty > 0 && want_ty <= lines && (want_ty & (want_ty - 1)) == 0) TY = want_ty;
-    const int SEGW = 32 * RX;
-    int NSEG = lines / TY;
-    const int64_t segs_needed = (A2.out + (int64_t)D * SEGW - 1) / ((int64_t)D * SEGW);
-    if (NSEG > segs_needed) NSEG = (int)(segs_needed < 1 ? 1 : segs_needed);
-    auto geom = [&](int64_t ckx, int64_t cky, int &Q, int64_t &rows, int64_t &cols, int64_t &rowe) {
+// Output columns / rows one sliding-window CTA covers.
+template <typename T> inline int64_t sw_cols_per_cta(const DirectParams<T> &P, int RX) {
+    return (int64_t)P.sw_nseg * P.sw_ph * 32 * RX;
+}
+template <typename T> inline int64_t sw_rows_per_cta(const DirectParams<T> &P) {
+    return (int64_t)P.sw_ty * P.sw_ry;
+}
+
+// Estimated duration (microseconds) of a sliding-window launch over n_inst
+// instances, without the per-call overhead (~8.5 us timed from the host:
+// planning, launch).  A model whose constants were fitted to GB300 timings
+// of every (TY, RY) plan of 620 problems (f32; 1-3-D, 2^8..2^24 elements,
+// kernels 3..127 per axis; rms error 14 % of the time):
+//  * one warp line: 0.0874 us per window (RX + CKX - 1 shared loads) and
+//    0.141 us per (row, kernel row) tap chunk (the FMAs);
+//  * the lines of a CTA run concurrently; the SM's issue rate is 0.382 per
+//    resident warp line (CTAs per SM: 2, 3 at one row per line, fewer when
+//    shared memory is short), at most 4; a CTA holds its slot 4.2 us per
+//    staged chunk (global latency, barriers);
+//  * one CTA alone takes at least 1.42 x (6.9e-4 us per staged element,
+//    its line, 0.037 us per staged chunk).
+template <typename T> double sw_time(const DirectParams<T> &P, int RX, int CKX, int64_t n_inst) {
+    const AxisGeom &A0 = P.g.ax[0], &A1 = P.g.ax[1], &A2 = P.g.ax[2];
+    const int64_t TXo = sw_cols_per_cta(P, RX), TYo = sw_rows_per_cta(P);
+    const double ctas = (double)((A2.out + TXo - 1) / TXo) * (double)((A1.out + TYo - 1) / TYo) * (double)A0.out;
+    const int S = P.sw_res, D = P.sw_ph, TY = P.sw_ty, RY = P.sw_ry;
+    double windows = 0, pairs = 0, staged = 0, chunks = 0;
+    const int64_t ny = (P.t_n[1] + P.cky - 1) / P.cky, nx = (P.t_n[2] + P.ckx - 1) / P.ckx;
+    for (int64_t iy = 0; iy < ny; iy++) {
+        const int64_t cky = iy + 1 < ny ? P.cky : P.t_n[1] - iy * P.cky;
+        const double rows = (double)(((int64_t)TY * RY - 1) * A1.s + (cky - 1) * A1.d + 1);
+        const double nj = (double)(RY - 1) * P.sw_h + (double)cky;
+        for (int64_t ix = 0; ix < nx; ix++) {
+            const int64_t ckx = ix + 1 < nx ? P.ckx : P.t_n[2] - ix * P.ckx;
+            const int64_t tr0 = (ckx + S - 1) / S;
+            staged += rows * (double)S * D * (P.sw_nseg * 32.0 * RX + tr0 - 1);
+            chunks += 1;
+            for (int r = 0; r < S; r++) {
+                const double nch = (double)(((ckx - r + S - 1) / S + CKX - 1) / CKX);  // tap chunks of residue r
+                windows += nj * nch;
+                pairs += (double)RY * cky * nch;
+            }
+        }
+    }
+    const double kz = (double)P.t_n[0];
+    const double line = kz * (0.0874 * windows + 0.141 * pairs);
+    const double nlines = (double)TY * P.sw_nseg * D;
+    const double smem = (double)smem_bytes(P) + 1024.0;
+    double resident = (RY == 1 && sizeof(T) <= 8) ? 3.0 : 2.0;
+    if (resident * smem > 228.0 * 1024) resident = smem * 2 > 228.0 * 1024 ? 1.0 : 2.0;
+    double ipc = 0.382 * resident * nlines;
+    if (ipc > 4.0) ipc = 4.0;
+    const double spread = ctas * (double)n_inst * (nlines * line / ipc + 4.2 * kz * chunks / resident) / 152.0;
+    const double alone = 1.42 * (6.9e-4 * kz * staged + line + 0.037 * kz * chunks);
+    return spread > alone ? spread : alone;
+}
+
+// Shared-memory layout of a sliding-window plan of TY x RY rows and NSEG
+// segments: kernel columns per chunk (all of them when one kernel row fits),
+// then kernel rows per chunk.  False when not one tap fits.
+template <typename T>
+bool sw_layout(DirectParams<T> &P, int RX, int TY, int RY, int H, int NSEG, int D, int S) {
+    const AxisGeom &A1 = P.g.ax[1];
+    const int SEGW = 32 * RX, CKX = 2 * RX;
+    auto geom = [&](int64_t ckx, int64_t cky, int &Q, int64_t &trp, int64_t &rows, int64_t &cols, int64_t &rowe) {
         const int64_t tr = (ckx + S - 1) / S;
+        trp = (tr + CKX - 1) / CKX * CKX;  // weight slots: whole tap chunks
         Q = (int)((NSEG * SEGW + tr - 1 + RX - 1) / RX);
         rowe = (int64_t)S * D * RX * Q;
-        rows = (TY - 1) * A1.s + (cky - 1) * A1.d + 1;
+        rows = ((int64_t)TY * RY - 1) * A1.s + (cky - 1) * A1.d + 1;
         cols = (int64_t)S * D * (NSEG * SEGW + tr - 1);
-        return sizeof(T) * (rows * rowe + cky * S * tr) + 16 + sizeof(int64_t) * (2 * rows + cols) +
+        return sizeof(T) * (rows * rowe + cky * S * trp) + 16 + sizeof(int64_t) * (2 * rows + cols) +
                sizeof(int) * (cky + cols);
     };
     int Q;
-    int64_t rows, cols, rowe;
-    // taps per staged chunk along x: all of them if a single kernel row fits
+    int64_t trp, rows, cols, rowe;
     int64_t ckx = P.t_n[2];
-    while (ckx > 1 && geom(ckx, 1, Q, rows, cols, rowe) > kSmemBudget) ckx = (ckx + 1) / 2;
-    if (geom(ckx, 1, Q, rows, cols, rowe) > kSmemBudget) return false;
+    while (ckx > 1 && geom(ckx, 1, Q, trp, rows, cols, rowe) > kSmemBudget) ckx = (ckx + 1) / 2;
+    if (geom(ckx, 1, Q, trp, rows, cols, rowe) > kSmemBudget) return false;
     int64_t cky = P.t_n[1];
-    while (cky > 1 && geom(ckx, cky, Q, rows, cols, rowe) > kSmemBudget) cky = (cky + 1) / 2;
-    geom(ckx, cky, Q, rows, cols, rowe);
+    while (cky > 1 && geom(ckx, cky, Q, trp, rows, cols, rowe) > kSmemBudget) cky = (cky + 1) / 2;
+    geom(ckx, cky, Q, trp, rows, cols, rowe);
     P.sw_ty = TY;
+    P.sw_ry = RY;
+    P.sw_h = H;
     P.sw_nseg = NSEG;
     P.sw_q = Q;
     P.sw_ph = D;
     P.sw_res = S;
-    P.sw_tr = (int)((ckx + S - 1) / S);
+    P.sw_tr = (int)trp;
     P.cky = cky;
     P.ckx = ckx;
     P.max_rows = rows;
     P.max_cols = cols;
     P.tile_elems = rows * rowe;
-    P.w_elems = cky * S * P.sw_tr;
+    P.w_elems = cky * S * trp;
     P.maps_off = ((int64_t)sizeof(T) * (P.tile_elems + P.w_elems) + 15) / 16 * 16;
     return true;
 }
 
-// Output columns one sliding-window CTA covers.
-template <typename T> inline int64_t sw_cols_per_cta(const DirectParams<T> &P, int RX) {
-    return (int64_t)P.sw_nseg * P.sw_ph * 32 * RX;
+// Sliding-window tiling: warps = TY row sets x NSEG segments x D phases
+// (<= 8), RY rows per set.  The first plan is the largest power-of-two TY
+// within the warp lines and the output rows (or the autotuner's TY), one row
+// per line.  When a kernel row's taps need several chunks, the tap order of
+// an output depends on the row chunking, so that plan stays (every launch of
+// the problem then sums in one order).  Otherwise all plans give the same
+// sums, and the one with the lowest estimated duration for n_inst instances
+// is taken among that TY and its half (the best plans of the timed set all
+// were) with RY = 1, 2, 4 (RY > 1 where the rows' input rows coincide, i.e.
+// TY s1 is a multiple of d1), or with the autotuner's RY.  knobs = false
+// ignores the autotuner's settings.
+template <typename T> bool plan_sw(DirectParams<T> &P, int RX, int64_t n_inst = 1, bool knobs = true) {
+    const AxisGeom &A1 = P.g.ax[1], &A2 = P.g.ax[2];
+    int D, S;
+    if (!sw_axis_ok(A2, D, S)) return false;
+    const int lines = 8 / D;
+    const int SEGW = 32 * RX;
+    const int64_t segs_needed = (A2.out + (int64_t)D * SEGW - 1) / ((int64_t)D * SEGW);
+    auto nseg_for = [&](int ty) {
+        int n = lines / ty;
+        if (n > segs_needed) n = (int)(segs_needed < 1 ? 1 : segs_needed);
+        return n;
+    };
+    int TY = 1;
+    while (TY * 2 <= lines && TY * 2 <= A1.out) TY *= 2;
+    // the autotuner's choice of rows per CTA, where it fits the 8 warp lines
+    const int want_ty = knobs ? ndconv_tune(NDCONV_TUNE_SW_TY) : 0;
+    const bool forced = want_ty > 0 && want_ty <= lines && (want_ty & (want_ty - 1)) == 0;
+    if (forced) TY = want_ty;
+    if (!sw_layout(P, RX, TY, 1, 0, nseg_for(TY), D, S)) return false;
+    if (P.ckx < P.t_n[2]) return true;
+    // the autotuner's rows per line (the first plan stays when none fits)
+    const int want_ry = knobs ? ndconv_tune(NDCONV_TUNE_SW_RY) : 0;
+    const bool ry_forced = want_ry == 1 || want_ry == 2 || want_ry == 4;
+    double best = (ry_forced && want_ry != 1) ? 1e300 : sw_time(P, RX, 2 * RX, n_inst);
+    DirectParams<T> pick = P;
+    const int tys[2] = {TY, (!forced && TY > 1) ? TY / 2 : TY};
+    for (int c = 0; c < 2; c++) {
+        const int ty = tys[c];
+        if (c == 1 && ty == tys[0]) break;
+        const bool coincide = ((int64_t)ty * A1.s) % A1.d == 0;
+        for (int ry = 1; ry <= sw_ry_max<T>(); ry *= 2) {
+            if (ry > 1 && (!coincide || (int64_t)ty * (ry / 2) >= A1.out)) break;
+            if ((ty == TY && ry == 1) || (ry_forced && ry != want_ry)) continue;
+            DirectParams<T> Q = P;
+            const int h = ry > 1 ? (int)((int64_t)ty * A1.s / A1.d) : 0;
+            if (!sw_layout(Q, RX, ty, ry, h, nseg_for(ty), D, S) || Q.ckx < Q.t_n[2]) continue;
+            const double t = sw_time(Q, RX, 2 * RX, n_inst);
+            if (t < best * 0.97) {
+                best = t;
+                pick = Q;
+            }
+        }
+    }
+    P = pick;
+    return true;
 }
 
 template <typename T, int RX, int CKX>
 cudaError_t launch_sw(const T *x, const T *k, T *y, const DirectParams<T> &P, cudaStream_t st, int64_t n_inst) {
     static_assert(CKX % RX == 0, "tap chunks must start on window blocks");
     const size_t sm = smem_bytes(P);
-    auto fn = direct_sw_kernel<T, RX, CKX>;
+    auto fn = direct_sw_kernel<T, RX, CKX, 1>;
+    if constexpr (sw_ry_max<T>() >= 2)
+        if (P.sw_ry == 2) fn = direct_sw_kernel<T, RX, CKX, 2>;
+    if constexpr (sw_ry_max<T>() >= 4)
+        if (P.sw_ry == 4) fn = direct_sw_kernel<T, RX, CKX, 4>;
     cudaError_t e = ndconv_allow_smem((const void *)fn, (int)kSmemBudget + 4096);
     if (e != cudaSuccess) return e;
     const AxisGeom &A0 = P.g.ax[0], &A1 = P.g.ax[1], &A2 = P.g.ax[2];
     const int64_t TXo = sw_cols_per_cta(P, RX);
-    dim3 grid((unsigned)((A2.out + TXo - 1) / TXo), (unsigned)((A1.out + P.sw_ty - 1) / P.sw_ty),
+    const int64_t TYo = sw_rows_per_cta(P);
+    dim3 grid((unsigned)((A2.out + TXo - 1) / TXo), (unsigned)((A1.out + TYo - 1) / TYo),
               (unsigned)(A0.out * n_inst));
     fn<<<grid, 256, sm, st>>>(x, k, y, P);
     ndconv_count_launch();
@@ -626,44 +792,17 @@ template <typename T, int RX> cudaError_t launch_tile(const T *x, const T *k, T 
 }  // namespace direct_detail
 using namespace direct_detail;
 
-// Estimated issue slots (warp instructions) of a sliding-window launch of
-// RX outputs per lane and CKX-tap windows, after plan_sw: staging of the
-// padded window (a global load, border map and swizzled store per element;
-// a strided x axis costs whole sectors), and the window loads + FMAs.
+// Estimated duration (seconds) of a sliding-window launch of one instance, after plan_sw.
 template <typename T> double sw_cost(const DirectParams<T> &P, int RX, int CKX) {
-    const AxisGeom &A0 = P.g.ax[0], &A1 = P.g.ax[1], &A2 = P.g.ax[2];
-    const int64_t TXo = sw_cols_per_cta(P, RX);
-    const double ctas = (double)((A2.out + TXo - 1) / TXo) * (double)((A1.out + P.sw_ty - 1) / P.sw_ty) *
-                        (double)A0.out;
-    const int S = P.sw_res, D = P.sw_ph, TY = P.sw_ty;
-    const double nlines = (double)TY * P.sw_nseg * D;
-    double per_cta = 0;
-    const int64_t ny = (P.t_n[1] + P.cky - 1) / P.cky, nx = (P.t_n[2] + P.ckx - 1) / P.ckx;
-    for (int64_t iy = 0; iy < ny; iy++) {
-        const int64_t cky = iy + 1 < ny ? P.cky : P.t_n[1] - iy * P.cky;
-        const int64_t rows = (TY - 1) * A1.s + (cky - 1) * A1.d + 1;
-        for (int64_t ix = 0; ix < nx; ix++) {
-            const int64_t ckx = ix + 1 < nx ? P.ckx : P.t_n[2] - ix * P.ckx;
-            const int64_t tr0 = (ckx + S - 1) / S;
-            const double cols = (double)S * D * (P.sw_nseg * 32.0 * RX + tr0 - 1);
-            const double stage = rows * cols / 32.0 * ((A2.xs == 1 || A2.xs == -1) ? 10.0 : 24.0) +
-                                 (rows + cols) / 32.0 * 30.0 + 200.0;
-            double comp = 0;
-            for (int r = 0; r < S; r++) {
-                const int64_t ckr = (ckx - r + S - 1) / S;
-                comp += (double)((ckr + CKX - 1) / CKX) * (2.0 * (RX + CKX - 1) + (double)CKX * RX);
-            }
-            per_cta += stage + nlines * cky * comp;
-        }
-    }
-    return ctas * per_cta * (double)P.t_n[0];
+    return sw_time(P, RX, CKX, 1) * 1e-6;
 }
 
 // With every border constant zero the padded values do not depend on the
 // order in which axes are resolved, so the problem may be computed with its
 // axes permuted (the output written through permuted strides).  Of the six
 // orders, take the one whose sliding-window launch has the lowest estimated
-// cost; when no order fits that kernel, put the longest output axis last
+// cost (with the library's own plans, so the tuning knobs never change the
+// order, and with it the summation order); when no order fits that kernel, put the longest output axis last
 // (the tiled one) and the next longest in the middle.
 template <typename T> void permute_axes_for_tiles(DirectParams<T> &P) {
     for (int a = 0; a < 3; a++)
@@ -688,7 +827,7 @@ template <typename T> void permute_axes_for_tiles(DirectParams<T> &P) {
         DirectParams<T> Q = permuted(perms[i]);
         // the grid's y and z extents are limited to 65535
         if (Q.g.ax[0].out >= 65536 || Q.g.ax[1].out >= 65536) continue;
-        if (!plan_sw(Q, RX)) continue;
+        if (!plan_sw(Q, RX, 1, false)) continue;
         const double c = sw_cost(Q, RX, 2 * RX);
         if (pick < 0 || c < best * 0.9) {
             best = c;

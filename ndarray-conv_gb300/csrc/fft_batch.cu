@@ -133,7 +133,8 @@ __global__ void __launch_bounds__(256) persistent_kernel(const Task *__restrict_
         switch (tk.kind) {
         case TK_DIRECT_SW: {
             const DirectParams<float> &P = dargs[tk.arg];
-            direct_sw_block<float, 8, 16>(nullptr, nullptr, nullptr, P, tk.bx, tk.by, tk.bz, smem_raw);
+            direct_sw_block<float, 8, 16, sw_ry_max<float>()>(nullptr, nullptr, nullptr, P, tk.bx, tk.by, tk.bz,
+                                                              smem_raw);
             break;
         }
         case TK_DIRECT_TILE4: {
@@ -265,11 +266,12 @@ size_t direct_tasks(ndconv_batch_plan *B, HostInst &h, std::vector<Task> &out) {
     const AxisGeom &A0 = D.g.ax[0], &A1 = D.g.ax[1], &A2 = D.g.ax[2];
     int kind = 0;
     int64_t gx = 0, gy = 0;
-    if (plan_sw(D, 8) && smem_bytes(D) <= kBatchSmem) {
+    // the queue fills the GPU with other tasks: plan for many instances
+    if (plan_sw(D, 8, 1 << 20) && smem_bytes(D) <= kBatchSmem) {
         kind = TK_DIRECT_SW;
-        const int64_t TXo = sw_cols_per_cta(D, 8);
+        const int64_t TXo = sw_cols_per_cta(D, 8), TYo = sw_rows_per_cta(D);
         gx = (A2.out + TXo - 1) / TXo;
-        gy = (A1.out + D.sw_ty - 1) / D.sw_ty;
+        gy = (A1.out + TYo - 1) / TYo;
     } else {
         int BX, BY;
         if (plan_tile(D, 4, BX, BY) && smem_bytes(D) <= kBatchSmem) {
@@ -902,6 +904,12 @@ extern "C" int ndconv_batch_destroy(ndconv_batch_plan *B) {
 // dispatcher and as features of the learned one.  Rates are round numbers
 // for one GB300 (FP32 FMA ~40 T/s, shared memory ~40 TB/s, HBM ~6.8 TB/s);
 // the autotuner's measurements replace them where available.
+// Calibration of the modelled times against GB300 timings of 22,000
+// problems of the autotuner's distribution (least squares in log time):
+// FFT 3.14 x the traffic model + 34.5 us per call (its several launches),
+// direct 1.03 x its model + 6.4 us.
+constexpr double kFftScale = 3.14, kFftCall = 34.5e-6, kDirectScale = 1.03, kDirectCall = 6.4e-6;
+
 extern "C" int ndconv_plan_info(const ndconv_problem *p, double out[8]) {
     using namespace ndconv;
     if (!out) return ndconv_fail(NDCONV_ERR_INVALID, "null output");
@@ -913,7 +921,7 @@ extern "C" int ndconv_plan_info(const ndconv_problem *p, double out[8]) {
     const double nout = (double)(A[0].out * A[1].out * A[2].out);
     const double nx = (double)(A[0].n * A[1].n * A[2].n);
     double taps = (double)(A[0].K * A[1].K * A[2].K);
-    double sw_slots = -1;  // issue slots of the sliding-window kernel, if it applies
+    double sw_s = -1;  // modelled seconds of the sliding-window kernel (f32), if it applies
     double fold_macs = -1, fold_prep = 0;  // the axis-folding form's GEMM and weight folding, if it applies
     {
         // the direct kernels only loop over taps that can see data
@@ -928,18 +936,20 @@ extern "C" int ndconv_plan_info(const ndconv_problem *p, double out[8]) {
                         (double)F.cout * F.cin * F.km * FA[F.f0].K;
         }
         permute_axes_for_tiles(D);
-        if (plan_sw(D, 8)) sw_slots = sw_cost(D, 8, 16);
+        if (plan_sw(D, 8)) sw_s = sw_cost(D, 8, 16);
     }
     const int es = (P.dtype == NDCONV_F64 || P.dtype == NDCONV_C32) ? 8 : (P.dtype == NDCONV_C64 ? 16 : 4);
     const double bytes = es * (nx + taps + nout);
     const double macs = nout * taps * ((P.dtype == NDCONV_C32 || P.dtype == NDCONV_C64) ? 4 : 1);
-    // direct, seconds: FMA rate, or the sliding-window issue model (152 SMs x
-    // 4 schedulers x ~1.9 GHz) when that kernel applies; other tilings run
-    // at about a third of the FMA rate
-    const double issue = 152.0 * 4 * 1.9e9;
-    const double t_fma = (sw_slots >= 0) ? (sw_slots / issue > macs / 40e12 ? sw_slots / issue : macs / 40e12)
-                                         : 3.0 * macs / 40e12;
-    out[0] = t_fma + bytes / 6.8e12 + 4e-6;
+    // direct, seconds: the sliding-window kernel's fitted f32 time model plus
+    // its per-call overhead when that kernel applies, else a third of a 40 T
+    // multiply-add/s rate; complex taps take four FMAs, and FP64 FMAs issue
+    // at a small fraction of the FP32 rate on this GPU
+    const bool cplx = P.dtype == NDCONV_C32 || P.dtype == NDCONV_C64;
+    const bool dbl = P.dtype == NDCONV_F64 || P.dtype == NDCONV_C64;
+    const double t_fma = ((sw_s >= 0) ? sw_s * (cplx ? 4 : 1) : 3.0 * macs / 40e12) * (dbl ? 32 : 1);
+    out[0] = kDirectScale * ((t_fma > bytes / 6.8e12 ? t_fma : bytes / 6.8e12) + (sw_s >= 0 ? 8.5e-6 : 4e-6)) +
+             kDirectCall;
     out[2] = macs;
     if (fold_macs >= 0) {
         // the direct entry point takes the axis-folding form: a gathered
@@ -1006,7 +1016,7 @@ extern "C" int ndconv_plan_info(const ndconv_problem *p, double out[8]) {
         const double smem_bytes = rows * H * (stages(M) + 1) * 16.0;
         const double mac_bytes = (double)A[0].out * A[1].out * sn * H * (double)(A[0].K * A[1].K) * 2.0 * csz;
         const double dram = dram_base + 2.0 * (double)A[0].L * A[1].L * sn * H * csz;
-        out[1] = smem_bytes / 40e12 + mac_bytes / 20e12 + dram / 6.8e12 + 12e-6;
+        out[1] = kFftScale * (smem_bytes / 40e12 + mac_bytes / 20e12 + dram / 6.8e12) + kFftCall;
         out[7] = 1;
         return NDCONV_OK;
     }
@@ -1015,7 +1025,7 @@ extern "C" int ndconv_plan_info(const ndconv_problem *p, double out[8]) {
     const double st = stages(M) + stages(F[1]) + stages(F[0]) + 1;
     const double smem_bytes = 3.0 * vol * st * 16.0;
     const double dram = dram_base + 4.0 * vol * csz;
-    out[1] = smem_bytes / 40e12 + dram / 6.8e12 + 12e-6;
+    out[1] = kFftScale * (smem_bytes / 40e12 + dram / 6.8e12) + kFftCall;
     out[7] = 1;
     return NDCONV_OK;
 }

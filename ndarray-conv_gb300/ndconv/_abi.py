@@ -30,7 +30,7 @@ ERR_TIMEOUT = 8
 ERR_NO_MEMORY = 9
 
 # ndconv_tune_knob
-TUNE_SW_TY, TUNE_MAC_ROWS, TUNE_ROW_THREADS, TUNE_BF16X3_BN = 0, 1, 2, 3
+TUNE_SW_TY, TUNE_MAC_ROWS, TUNE_ROW_THREADS, TUNE_BF16X3_BN, TUNE_SW_RY = 0, 1, 2, 3, 4
 STATUS_NAMES = {
     0: "OK", 1: "DATA_SHAPE", 2: "KERNEL_SHAPE", 3: "MISMATCH_SHAPE",
     4: "PAD_OUT_OF_RANGE", 5: "UNSUPPORTED", 6: "INVALID", 7: "CUDA",

@@ -200,6 +200,8 @@ def main():
     ap.add_argument("--out", required=True)
     ap.add_argument("--seed", type=int, default=5000)
     ap.add_argument("--timings", default=None, help="reuse a saved timings.npz (train + holdout)")
+    ap.add_argument("--seeds", type=int, default=4, help="networks trained; the best on a validation slice is kept")
+    ap.add_argument("--val", type=int, default=2000, help="validation slice carved from the training set")
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)
     n = args.train + args.holdout
@@ -214,9 +216,22 @@ def main():
     for i, (s, t) in enumerate(zip(db.specs, db.times)):
         (train if i < args.train else hold).add(s, t)
     t1 = time.time()
-    net, loss = train_network(train, epochs=args.epochs)
+    # model selection: networks of several seeds fitted on the training set
+    # minus a validation slice; the one whose picks cost least on that slice
+    # is refitted on the whole training set (same seed).  The held-out set
+    # plays no part in the choice.
+    fit, val = TimingDB(), TimingDB()
+    for i, (s, t) in enumerate(zip(train.specs, train.times)):
+        (fit if i < len(train.specs) - args.val else val).add(s, t)
+    scores = []
+    for seed in range(args.seeds):
+        cand_net, _ = train_network(fit, epochs=args.epochs, seed=seed)
+        scores.append(evaluate(cand_net, val)["mlp"]["total_ratio"])
+    seed = int(np.argmin(scores))
+    net, loss = train_network(train, epochs=args.epochs, seed=seed)
     t_train = time.time() - t1
     rep = {"train": len(train.specs), "holdout": len(hold.specs), "final_train_loss": loss,
+           "seed_validation_total_ratio": scores, "seed": seed,
            "tune_s": t_tune, "train_s": t_train, "holdout_eval": evaluate(net, hold),
            "train_eval": evaluate(net, train)}
     net.save(os.path.join(args.out, "dispatcher_mlp.json"), extra={"report": rep["holdout_eval"]})

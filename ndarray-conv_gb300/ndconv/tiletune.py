@@ -3,7 +3,8 @@ dispatcher.
 
 The first stage (ndconv.mlp) picks the algorithm variant of an instance.
 Inside a variant the library exposes tile / plan knobs (ndconv_set_tuning):
-rows per CTA of the sliding-window direct kernel, output rows per CTA of the
+row sets per CTA and rows per warp line of the sliding-window direct kernel,
+output rows per CTA of the
 FFT spectral tap sum and threads of the FFT row passes, and the tensor-core
 tile width.  This module times every knob combination of every variant on a
 set of configurations (CUDA events, warm-up, best of `reps`), keeps the
@@ -29,7 +30,7 @@ from .api import build_problem, with_dilation
 
 # (variant, [knob settings]) -- settings are {knob: value}; {} is the library's choice
 KNOB_SPACE = [
-    (_abi.ALGO_DIRECT, [{}] + [{_abi.TUNE_SW_TY: t} for t in (1, 2, 4, 8)]),
+    (_abi.ALGO_DIRECT, [{}] + [{_abi.TUNE_SW_TY: t, _abi.TUNE_SW_RY: r} for t in (1, 2, 4, 8) for r in (1, 2, 4)]),
     (_abi.ALGO_DIRECT_BF16X3, [{}] + [{_abi.TUNE_BF16X3_BN: b} for b in (32, 64)]),
     (_abi.ALGO_FFT_ND, [{}] + [{_abi.TUNE_ROW_THREADS: t} for t in (128, 256, 512)]),
     (_abi.ALGO_FFT_RS, [{_abi.TUNE_MAC_ROWS: m, _abi.TUNE_ROW_THREADS: t} if (m or t) else {}

@@ -63,6 +63,7 @@ pub const NDCONV_TUNE_SW_TY: i32 = 0;
 pub const NDCONV_TUNE_MAC_ROWS: i32 = 1;
 pub const NDCONV_TUNE_ROW_THREADS: i32 = 2;
 pub const NDCONV_TUNE_BF16X3_BN: i32 = 3;
+pub const NDCONV_TUNE_SW_RY: i32 = 4;
 
 pub const NDCONV_MAX_RANK: usize = 3;
 
