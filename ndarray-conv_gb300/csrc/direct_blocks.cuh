@@ -130,6 +130,30 @@ template <typename T> __device__ __forceinline__ void stage_async(T *smem, const
     }
 }
 
+// acc[r] += win[r + t] w[t] over taps t of [O, O + B), r < RX.
+template <typename E, int RX, int O, int B, typename Acc, typename T, int NW, int NT>
+__device__ __forceinline__ void fma_taps(Acc (&acc)[RX], const T (&win)[NW], const T (&w)[NT]) {
+#pragma unroll
+    for (int t = O; t < O + B; t++)
+#pragma unroll
+        for (int r = 0; r < RX; r++) E::mac(acc[r], win[r + t], w[t]);
+}
+
+// The first m taps (0 < m < 2B) of a chunk whose first O are done, without a
+// branch per tap: the binary digits of m from B down, each a compile-time
+// block of taps, in ascending tap order.
+template <typename E, int RX, int B, int O, typename Acc, typename T, int NW, int NT>
+__device__ __forceinline__ void fma_tail(Acc (&acc)[RX], const T (&win)[NW], const T (&w)[NT], int m) {
+    if constexpr (B >= 1) {
+        if (m & B) {
+            fma_taps<E, RX, O, B>(acc, win, w);
+            fma_tail<E, RX, B / 2, O + B>(acc, win, w, m);
+        } else {
+            fma_tail<E, RX, B / 2, O>(acc, win, w, m);
+        }
+    }
+}
+
 // Sliding-window variant along the contiguous axis, any stride s and
 // dilation d (g = gcd(s, d), D = d / g phases, S = s / g tap residues).
 // Output ox = X0 + phi + D j, tap u = rho + S t of a chunk starting at kx0
@@ -293,12 +317,11 @@ __device__ __forceinline__ void direct_sw_block(const T *__restrict__ x0, const 
                                     if (i < RY && a >= 0 && a < cky) {
                                         T w[CKX];
                                         load_taps<T, CKX>(w, wsm + (a * S + rho) * TR + t0);
-                                        if (full && !zrow[a]) {
-                                            // no zero taps: no per-tap branches
-#pragma unroll
-                                            for (int t = 0; t < CKX; t++)
-#pragma unroll
-                                                for (int r = 0; r < RX; r++) E::mac(acc[i][r], win[r + t], w[t]);
+                                        if (!zrow[a]) {
+                                            // no zero taps: no per-tap branches (a partial
+                                            // chunk in blocks of 8, 4, 2, 1 taps)
+                                            if (full) fma_taps<E, RX, 0, CKX>(acc[i], win, w);
+                                            else fma_tail<E, RX, CKX / 2, 0>(acc[i], win, w, ckr - t0);
                                         } else {
 #pragma unroll
                                             for (int t = 0; t < CKX; t++) {
