@@ -29,16 +29,33 @@ extern "C" {
 /* element type (InElem / T of the reference traits).  The crate's ConvExt
  * is generic over any T: NumAssign + Copy and any rank N
  * (src/conv/mod.rs:78-83,118-124); its own tests pad u8 arrays
- * (src/padding/mod.rs:621-624).  This library runs f32, f64, i32, c32 and
- * c64 at ranks 1..NDCONV_MAX_RANK; any other element type code (i8, i16,
- * i64, u8, u32, ...) and any rank above 3 get NDCONV_ERR_UNSUPPORTED from
- * every entry point (there is no CPU fallback). */
+ * (src/padding/mod.rs:621-624).  This library runs ranks 1..NDCONV_MAX_RANK
+ * and the element types below; any other code and any rank above 3 get
+ * NDCONV_ERR_UNSUPPORTED (there is no CPU fallback).  Integers use wrapping
+ * arithmetic, as release-mode Rust does (the sum of products modulo 2^bits),
+ * and take the direct path only (integer FFT convolution is documented
+ * broken upstream, src/conv_fft/processor/mod.rs:46-59).  i32 runs every
+ * direct entry point (single, batch, host batch, batch plans); the other
+ * integer types run ndconv_conv and ndconv_conv_algo(NDCONV_ALGO_DIRECT)
+ * (and ndconv_output_shape) and are refused by the rest.  8- and 16-bit
+ * data are widened to 32 bits on the device (stream-ordered scratch), summed
+ * by the 32-bit kernels and truncated: the low bits of a wrapping sum depend
+ * only on the low bits of its terms, so results are the element type's own
+ * wrapping sums.  Unsigned types share their signed twin's kernels bit for
+ * bit. */
 typedef enum {
     NDCONV_F32 = 0,
     NDCONV_F64 = 1,
     NDCONV_I32 = 2, /* direct conv only, wrapping arithmetic (release-mode Rust) */
     NDCONV_C32 = 3, /* num_complex::Complex<f32> */
-    NDCONV_C64 = 4
+    NDCONV_C64 = 4,
+    NDCONV_I64 = 5, /* the integer types from here on: ndconv_conv only */
+    NDCONV_U8 = 6,
+    NDCONV_I8 = 7,
+    NDCONV_I16 = 8,
+    NDCONV_U16 = 9,
+    NDCONV_U32 = 10,
+    NDCONV_U64 = 11
 } ndconv_dtype;
 
 typedef enum {

@@ -136,11 +136,12 @@ int plan_problem(const ndconv_problem *p, int algo, Plan3 *out) {
     if (p->rank < 1) return ndconv_fail(NDCONV_ERR_INVALID, "rank must be at least 1");
     // the crate is generic over any const N and any NumAssign element type
     // (src/conv/mod.rs:78-83,118-124); this library's kernels take ranks 1..3
-    // and f32 / f64 / i32 / c32 / c64: everything else is refused, never run
-    // on a fallback
+    // and the element types of ndconv_dtype: everything else is refused,
+    // never run on a fallback
     if (p->rank > 3) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "rank above 3 is not supported (ranks 1..3)");
-    if (p->dtype < NDCONV_F32 || p->dtype > NDCONV_C64)
-        return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "element type not supported (f32, f64, i32, c32, c64)");
+    if (p->dtype < NDCONV_F32 || p->dtype > NDCONV_U64)
+        return ndconv_fail(NDCONV_ERR_UNSUPPORTED,
+                           "element type not supported (f32, f64, c32, c64, i8, u8, i16, u16, i32, u32, i64, u64)");
     const int r = p->rank;
     for (int i = 0; i < r; i++) {
         if (p->data_shape[i] < 0 || p->kernel_shape[i] < 0)
@@ -286,6 +287,11 @@ extern "C" int ndconv_conv(const ndconv_problem *p, const void *data, const void
     case NDCONV_I32: e = direct_conv_launch<int32_t>((const int32_t *)data, (const int32_t *)kernel, (int32_t *)out, P.direct<int32_t>(), st, 0); break;
     case NDCONV_C32: e = direct_conv_launch<c32>((const c32 *)data, (const c32 *)kernel, (c32 *)out, P.direct<c32>(), st, 0); break;
     case NDCONV_C64: e = direct_conv_launch<c64>((const c64 *)data, (const c64 *)kernel, (c64 *)out, P.direct<c64>(), st, 0); break;
+    // u32 and u64 share i32 and i64 bit for bit (wrapping sums)
+    case NDCONV_U32: e = direct_conv_launch<int32_t>((const int32_t *)data, (const int32_t *)kernel, (int32_t *)out, P.direct<int32_t>(), st, 0); break;
+    case NDCONV_I64:
+    case NDCONV_U64: e = direct_conv_launch<int64_t>((const int64_t *)data, (const int64_t *)kernel, (int64_t *)out, P.direct<int64_t>(), st, 0); break;
+    default: return conv_narrow_int(P, data, kernel, out, st);
     }
     if (e != cudaSuccess) return ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e));
     return NDCONV_OK;
@@ -386,6 +392,7 @@ extern "C" int ndconv_conv_batch(const ndconv_problem *p, int64_t n, const void 
     case NDCONV_I32: e = direct_conv_batch_launch<int32_t>(n, (const int32_t *const *)data, (const int32_t *const *)kernel, (int32_t *const *)out, P.direct<int32_t>(), st); break;
     case NDCONV_C32: e = direct_conv_batch_launch<c32>(n, (const c32 *const *)data, (const c32 *const *)kernel, (c32 *const *)out, P.direct<c32>(), st); break;
     case NDCONV_C64: e = direct_conv_batch_launch<c64>(n, (const c64 *const *)data, (const c64 *const *)kernel, (c64 *const *)out, P.direct<c64>(), st); break;
+    default: return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "this integer element type runs ndconv_conv only");
     }
     if (e != cudaSuccess) return ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e));
     return NDCONV_OK;

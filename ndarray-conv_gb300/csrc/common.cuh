@@ -22,6 +22,7 @@ template <> struct Elem<float> {
     using Acc = float;
     using Real = float;
     static constexpr bool kComplex = false;
+    static constexpr bool kInteger = false;
     __host__ __device__ static float zero() { return 0.0f; }
     __host__ __device__ static float from(double re, double) { return (float)re; }
     __device__ static bool is_zero(float v) { return v == 0.0f; }
@@ -33,6 +34,7 @@ template <> struct Elem<double> {
     using Acc = double;
     using Real = double;
     static constexpr bool kComplex = false;
+    static constexpr bool kInteger = false;
     __host__ __device__ static double zero() { return 0.0; }
     __host__ __device__ static double from(double re, double) { return re; }
     __device__ static bool is_zero(double v) { return v == 0.0; }
@@ -45,17 +47,36 @@ template <> struct Elem<int32_t> {
     using Acc = uint32_t;
     using Real = int32_t;
     static constexpr bool kComplex = false;
+    static constexpr bool kInteger = true;
     __host__ __device__ static int32_t zero() { return 0; }
-    __host__ __device__ static int32_t from(double re, double) { return (int32_t)re; }
+    __host__ __device__ static int32_t from(double re, double) {
+        return re >= 2147483648.0 ? (int32_t)(uint32_t)re : (int32_t)re;  // u32 constants above 2^31
+    }
     __device__ static bool is_zero(int32_t v) { return v == 0; }
     __device__ static void mac(uint32_t &a, int32_t x, int32_t w) { a += (uint32_t)x * (uint32_t)w; }
     __device__ static void add(uint32_t &a, int32_t x) { a += (uint32_t)x; }
     __device__ static int32_t out(uint32_t a) { return (int32_t)a; }
 };
+// i64: wrapping two's-complement arithmetic (u64 runs as i64: the same bits)
+template <> struct Elem<int64_t> {
+    using Acc = uint64_t;
+    using Real = int64_t;
+    static constexpr bool kComplex = false;
+    static constexpr bool kInteger = true;
+    __host__ __device__ static int64_t zero() { return 0; }
+    __host__ __device__ static int64_t from(double re, double) {
+        return re >= 9223372036854775808.0 ? (int64_t)(uint64_t)re : (int64_t)re;
+    }
+    __device__ static bool is_zero(int64_t v) { return v == 0; }
+    __device__ static void mac(uint64_t &a, int64_t x, int64_t w) { a += (uint64_t)x * (uint64_t)w; }
+    __device__ static void add(uint64_t &a, int64_t x) { a += (uint64_t)x; }
+    __device__ static int64_t out(uint64_t a) { return (int64_t)a; }
+};
 template <> struct Elem<c32> {
     using Acc = c32;
     using Real = float;
     static constexpr bool kComplex = true;
+    static constexpr bool kInteger = false;
     __host__ __device__ static c32 zero() { return c32{0.0f, 0.0f}; }
     __host__ __device__ static c32 from(double re, double im) { return c32{(float)re, (float)im}; }
     __device__ static bool is_zero(c32 v) { return v.re == 0.0f && v.im == 0.0f; }
@@ -75,6 +96,7 @@ template <> struct Elem<c64> {
     using Acc = c64;
     using Real = double;
     static constexpr bool kComplex = true;
+    static constexpr bool kInteger = false;
     __host__ __device__ static c64 zero() { return c64{0.0, 0.0}; }
     __host__ __device__ static c64 from(double re, double im) { return c64{re, im}; }
     __device__ static bool is_zero(c64 v) { return v.re == 0.0 && v.im == 0.0; }

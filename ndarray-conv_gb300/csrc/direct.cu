@@ -76,7 +76,7 @@ cudaError_t launch_any(const T *x, const T *k, T *y, DirectParams<T> P, cudaStre
         permute_axes_for_tiles(P);
     }
     cudaError_t e = launch_main<T>(x, k, y, P, st, force_naive, n_inst);
-    if (e != cudaSuccess || !taps_restricted(P) || std::is_same<T, int32_t>::value) return e;
+    if (e != cudaSuccess || !taps_restricted(P) || Elem<T>::kInteger) return e;
     // skipped taps with a non-finite weight: every output is NaN, as in the reference
     const int64_t nk = A0.K * A1.K;  // kernel rows
     int64_t parts = (nk + 255) / 256;
@@ -127,6 +127,7 @@ cudaError_t direct_conv_batch_launch(int64_t n, const T *const *xs, const T *con
 NDCONV_INST_DIRECT_BATCH(float)
 NDCONV_INST_DIRECT_BATCH(double)
 NDCONV_INST_DIRECT_BATCH(int32_t)
+NDCONV_INST_DIRECT_BATCH(int64_t)
 NDCONV_INST_DIRECT_BATCH(c32)
 NDCONV_INST_DIRECT_BATCH(c64)
 #define NDCONV_INST_DIRECT(T)                                                                             \
@@ -136,6 +137,7 @@ NDCONV_INST_DIRECT_BATCH(c64)
 NDCONV_INST_DIRECT(float)
 NDCONV_INST_DIRECT(double)
 NDCONV_INST_DIRECT(int32_t)
+NDCONV_INST_DIRECT(int64_t)
 NDCONV_INST_DIRECT(c32)
 NDCONV_INST_DIRECT(c64)
 

@@ -497,12 +497,13 @@ template <typename T> inline bool taps_restricted(const DirectParams<T> &P) {
 }
 
 template <typename T> __device__ __forceinline__ bool non_finite(T v) {
-    if constexpr (std::is_same<T, int32_t>::value) return false;  // integers are always finite
+    if constexpr (Elem<T>::kInteger) return false;  // integers are always finite
     else if constexpr (Elem<T>::kComplex) return !isfinite(v.re) || !isfinite(v.im);
     else return !isfinite(v);
 }
 template <typename T> __device__ __forceinline__ T nan_elem() {
     if constexpr (Elem<T>::kComplex) return T{(decltype(T{}.re))NAN, (decltype(T{}.re))NAN};
+    else if constexpr (Elem<T>::kInteger) return T(0);  // not used: integer taps are never non-finite
     else return (T)NAN;
 }
 

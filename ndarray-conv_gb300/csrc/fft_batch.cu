@@ -377,6 +377,10 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
             std::string m = "instance " + std::to_string(i) + ": " + ndconv_last_error();
             return fail(ndconv_fail(s, m.c_str()));
         }
+        if (single_call_int(h.P.dtype)) {
+            std::string m = "instance " + std::to_string(i) + ": this integer element type runs ndconv_conv only";
+            return fail(ndconv_fail(NDCONV_ERR_UNSUPPORTED, m.c_str()));
+        }
         if (h.algo == 1 && (h.P.dtype == NDCONV_I32))
             return fail(ndconv_fail(NDCONV_ERR_UNSUPPORTED, "integer FFT convolution is not supported"));
         h.x = data[i];
@@ -938,7 +942,9 @@ extern "C" int ndconv_plan_info(const ndconv_problem *p, double out[8]) {
         permute_axes_for_tiles(D);
         if (plan_sw(D, 8)) sw_s = sw_cost(D, 8, 16);
     }
-    const int es = (P.dtype == NDCONV_F64 || P.dtype == NDCONV_C32) ? 8 : (P.dtype == NDCONV_C64 ? 16 : 4);
+    const int es = (P.dtype == NDCONV_F64 || P.dtype == NDCONV_C32 || P.dtype == NDCONV_I64 || P.dtype == NDCONV_U64)
+                       ? 8
+                       : (P.dtype == NDCONV_C64 ? 16 : 4);
     const double bytes = es * (nx + taps + nout);
     const double macs = nout * taps * ((P.dtype == NDCONV_C32 || P.dtype == NDCONV_C64) ? 4 : 1);
     // direct, seconds: the sliding-window kernel's fitted f32 time model plus
@@ -968,7 +974,7 @@ extern "C" int ndconv_plan_info(const ndconv_problem *p, double out[8]) {
     out[6] = (double)F[2];
     const int csz = (P.dtype == NDCONV_F64 || P.dtype == NDCONV_C64) ? 16 : 8;
     const double budget = 100.0 * 1024;  // persistent kernel share
-    if (P.dtype == NDCONV_I32) {
+    if (integer_dtype(P.dtype)) {
         out[1] = 1e30;
         out[7] = 0;
         return NDCONV_OK;

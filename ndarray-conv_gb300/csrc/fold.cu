@@ -152,7 +152,7 @@ cudaError_t fold_launch(const T *x, const T *k, T *y, const FoldParams &F, const
                                                                           tabs + fold_table_entries(F.ax[F.f0]));
         ndconv_count_launch();
     }
-    if (!std::is_same<T, int32_t>::value) {
+    if (!Elem<T>::kInteger) {
         fold_scan_kernel<T><<<152 * 4, 256, 0, st>>>(x, k, F, flag);
         ndconv_count_launch();
     }
@@ -174,6 +174,7 @@ cudaError_t fold_launch(const T *x, const T *k, T *y, const FoldParams &F, const
 NDCONV_INST_FOLD(float)
 NDCONV_INST_FOLD(double)
 NDCONV_INST_FOLD(int32_t)
+NDCONV_INST_FOLD(int64_t)
 NDCONV_INST_FOLD(c32)
 NDCONV_INST_FOLD(c64)
 

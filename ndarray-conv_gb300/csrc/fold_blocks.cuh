@@ -87,7 +87,7 @@ __device__ __forceinline__ void f0_elem(const T *__restrict__ T1, const FoldPara
 }
 
 template <typename T> __device__ __forceinline__ bool finite_elem(T v) {
-    if constexpr (std::is_same<T, int32_t>::value) return true;
+    if constexpr (Elem<T>::kInteger) return true;
     else if constexpr (Elem<T>::kComplex) return isfinite(v.re) && isfinite(v.im);
     else return isfinite(v);
 }

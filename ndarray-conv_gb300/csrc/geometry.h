@@ -39,4 +39,12 @@ struct Plan3 {
 
 int plan_problem(const ndconv_problem *p, int algo, Plan3 *out);
 
+// Element types other than f32 / f64 / i32 / c32 / c64 (the 64-bit and
+// narrow integers, u32): they run the single direct entry point only.
+inline bool single_call_int(int dtype) { return dtype >= NDCONV_I64; }
+inline bool integer_dtype(int dtype) { return dtype == NDCONV_I32 || dtype >= NDCONV_I64; }
+
+// ConvExt::conv for u8 / i8 / u16 / i16 (narrow_int.cu).
+int conv_narrow_int(const Plan3 &P, const void *data, const void *kernel, void *out, cudaStream_t st);
+
 }  // namespace ndconv

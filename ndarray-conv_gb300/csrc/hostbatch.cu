@@ -54,6 +54,8 @@ extern "C" int ndconv_conv_batch_host(const ndconv_problem *p, int32_t algo, int
     Plan3 P;
     int s = plan_problem(p, algo, &P);
     if (s) return s;
+    if (single_call_int(P.dtype))
+        return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "this integer element type runs ndconv_conv only");
     if (n < 0) return ndconv_fail(NDCONV_ERR_INVALID, "negative batch size");
     if (n == 0) return NDCONV_OK;
     if (!data || !kernel || !out) return ndconv_fail(NDCONV_ERR_INVALID, "null pointer array");

@@ -11,6 +11,7 @@ LIB_PATH = os.path.join(os.path.dirname(_HERE), "_build", "libndconv.so")
 
 # ndconv_dtype
 F32, F64, I32, C32, C64 = 0, 1, 2, 3, 4
+I64, U8, I8, I16, U16, U32, U64 = 5, 6, 7, 8, 9, 10, 11  # integer types beyond i32: ndconv_conv only
 # ndconv_status
 # ndconv_algo: algorithm variants (autotuner candidates)
 ALGO_DIRECT, ALGO_FFT, ALGO_DIRECT_BF16X3 = 0, 1, 2

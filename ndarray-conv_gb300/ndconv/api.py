@@ -180,16 +180,18 @@ class CudaError(RuntimeError):
 
 
 _NP_DTYPES = {"float32": _abi.F32, "float64": _abi.F64, "int32": _abi.I32,
-              "complex64": _abi.C32, "complex128": _abi.C64}
+              "complex64": _abi.C32, "complex128": _abi.C64, "int64": _abi.I64, "uint8": _abi.U8,
+              "int8": _abi.I8, "int16": _abi.I16, "uint16": _abi.U16, "uint32": _abi.U32, "uint64": _abi.U64}
 
 
 def dtype_code(dtype):
     """The ABI element type of a numpy / torch dtype.  Like the C ABI, element
-    types other than f32, f64, i32, c32 and c64 (the crate's generic conv
-    also takes i8, i16, i64, u8, u32, ...) raise Unsupported."""
+    types outside f32, f64, c32, c64 and the 8- to 64-bit integers (e.g.
+    float16, bool) raise Unsupported."""
     name = str(dtype).replace("torch.", "")
     if name not in _NP_DTYPES:
-        raise Unsupported(None, f"element type {dtype} is not supported (f32, f64, i32, c32, c64)")
+        raise Unsupported(None, f"element type {dtype} is not supported "
+                                f"(f32, f64, c32, c64, i8, u8, i16, u16, i32, u32, i64, u64)")
     return _NP_DTYPES[name]
 
 

@@ -19,12 +19,25 @@ _TORCH_OF = {_abi.F32: torch.float32, _abi.F64: torch.float64, _abi.I32: torch.i
              _abi.C32: torch.complex64, _abi.C64: torch.complex128}
 
 
+# unsigned numpy types that travel to the device as their signed twin (the
+# same bits; the ABI still gets the unsigned element type)
+_SIGNED_TWIN = {np.dtype(np.uint16): np.int16, np.dtype(np.uint32): np.int32, np.dtype(np.uint64): np.int64}
+
+
 def _to_device(a):
     if isinstance(a, torch.Tensor):
         if not a.is_cuda:
             return a.cuda(), True
         return a, False
-    return torch.from_numpy(np.ascontiguousarray(a)).cuda(), True
+    a = np.ascontiguousarray(a)
+    if a.dtype in _SIGNED_TWIN:
+        a = a.view(_SIGNED_TWIN[a.dtype])
+    return torch.from_numpy(a).cuda(), True
+
+
+def _np_dtype(a):
+    """numpy dtype of a host array argument (None for tensors)."""
+    return None if isinstance(a, torch.Tensor) else np.asarray(a).dtype
 
 
 def _stream_ptr(stream):
@@ -38,7 +51,8 @@ def _prepare(data, kernel, conv_mode, padding_mode):
     k, _ = _to_device(kwd.kernel)
     if x.dtype != k.dtype:
         raise TypeError(f"data {x.dtype} and kernel {k.dtype} element types differ")
-    dt = dtype_code(x.dtype)
+    nd = _np_dtype(data)
+    dt = dtype_code(nd if nd is not None and nd in _SIGNED_TWIN else x.dtype)
     from .api import KernelWithDilation
     kwd = KernelWithDilation(k, kwd.dilation, kwd.reverse_flag)
     p = build_problem(dt, tuple(x.shape), kwd, conv_mode, padding_mode,
@@ -65,7 +79,9 @@ def _run(algo, data, kernel, conv_mode, padding_mode, processor=None, stream=Non
                                ctypes.c_void_p(k.data_ptr()), ctypes.c_void_p(y.data_ptr()), h, sp)
     raise_for_status(st, p, algo)
     if x_host:
-        return y.cpu().numpy()
+        out = y.cpu().numpy()
+        nd = _np_dtype(data)
+        return out.view(nd) if nd in _SIGNED_TWIN else out
     return y
 
 

@@ -47,7 +47,8 @@ enum {
     ORC_UNSUPPORTED = 5,
     ORC_INVALID = 6,
 };
-enum { DT_F32 = 0, DT_F64 = 1, DT_I32 = 2, DT_C32 = 3, DT_C64 = 4 };
+enum { DT_F32 = 0, DT_F64 = 1, DT_I32 = 2, DT_C32 = 3, DT_C64 = 4, DT_I64 = 5, DT_U8 = 6, DT_I8 = 7,
+       DT_I16 = 8, DT_U16 = 9, DT_U32 = 10, DT_U64 = 11 };
 enum { BT_ZEROS = 0, BT_CONST = 1, BT_REFLECT = 2, BT_REPLICATE = 3, BT_CIRCULAR = 4 };
 enum { PM_ZEROS = 0, PM_CONST = 1, PM_REFLECT = 2, PM_REPLICATE = 3, PM_CIRCULAR = 4,
        PM_CUSTOM = 5, PM_EXPLICIT = 6 };
@@ -348,8 +349,20 @@ static void to_double(int dt, const void *src, long n, double *dst) {
     case DT_F32: case DT_C32: for (long i = 0; i < m; i++) dst[i] = ((const float *)src)[i]; break;
     case DT_F64: case DT_C64: memcpy(dst, src, sizeof(double) * m); break;
     case DT_I32: for (long i = 0; i < m; i++) dst[i] = ((const int32_t *)src)[i]; break;
+    /* 64-bit values are exact while |v| <= 2^53 */
+    case DT_I64: for (long i = 0; i < m; i++) dst[i] = (double)((const int64_t *)src)[i]; break;
+    case DT_U64: for (long i = 0; i < m; i++) dst[i] = (double)((const uint64_t *)src)[i]; break;
+    case DT_U8: for (long i = 0; i < m; i++) dst[i] = ((const uint8_t *)src)[i]; break;
+    case DT_I8: for (long i = 0; i < m; i++) dst[i] = ((const int8_t *)src)[i]; break;
+    case DT_I16: for (long i = 0; i < m; i++) dst[i] = ((const int16_t *)src)[i]; break;
+    case DT_U16: for (long i = 0; i < m; i++) dst[i] = ((const uint16_t *)src)[i]; break;
+    case DT_U32: for (long i = 0; i < m; i++) dst[i] = ((const uint32_t *)src)[i]; break;
     }
 }
+
+/* An integral double (|v| < 2^64) as the two's-complement bits of the
+ * element: negative values through int64, the rest through uint64. */
+static uint64_t int_bits(double v) { return v < 0 ? (uint64_t)(int64_t)v : (uint64_t)v; }
 
 /* ------------------------------------------------------- direct conv --- */
 static int shape_checks(const orc_problem *p, int kernel_code) {
@@ -361,7 +374,9 @@ static int shape_checks(const orc_problem *p, int kernel_code) {
 }
 
 /* ConvExt::conv, src/conv/mod.rs:128-200.  Accumulates in the element type
- * from zero, tap-list order (f32 in float, f64 in double, i32 wrapping,
+ * from zero, tap-list order (f32 in float, f64 in double, integers
+ * wrapping as release-mode Rust: the sum of products modulo 2^64, then its
+ * low 8 / 16 / 32 / 64 bits, which is the element type's own wrapping sum;
  * complex with the componentwise product of num-complex). ys receives the
  * output shape; y may be NULL to query it. */
 int orc_conv(const orc_problem *p, const void *x, const void *k, int64_t *ys, void *y) {
@@ -413,11 +428,15 @@ int orc_conv(const orc_problem *p, const void *x, const void *k, int64_t *ys, vo
                 ((double *)y)[f] = acc;
                 break;
             }
-            case DT_I32: {
-                uint32_t acc = 0;
-                for (long t = 0; t < nt; t++)
-                    acc += (uint32_t)(int32_t)pd[anchor + offs[t]] * (uint32_t)(int32_t)tv[t];
-                ((int32_t *)y)[f] = (int32_t)acc;
+            case DT_I32: case DT_I64: case DT_U8: case DT_I8: case DT_I16: case DT_U16: case DT_U32: case DT_U64: {
+                uint64_t acc = 0;
+                for (long t = 0; t < nt; t++) acc += int_bits(pd[anchor + offs[t]]) * int_bits(tv[t]);
+                switch (dt) {
+                case DT_U8: case DT_I8: ((uint8_t *)y)[f] = (uint8_t)acc; break;
+                case DT_I16: case DT_U16: ((uint16_t *)y)[f] = (uint16_t)acc; break;
+                case DT_I32: case DT_U32: ((uint32_t *)y)[f] = (uint32_t)acc; break;
+                default: ((uint64_t *)y)[f] = acc; break;
+                }
                 break;
             }
             case DT_C32: {

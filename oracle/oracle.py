@@ -18,8 +18,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "libndconv_oracle.so")
 
 DT_F32, DT_F64, DT_I32, DT_C32, DT_C64 = 0, 1, 2, 3, 4
+DT_I64, DT_U8, DT_I8, DT_I16, DT_U16, DT_U32, DT_U64 = 5, 6, 7, 8, 9, 10, 11
 NP_OF = {DT_F32: np.float32, DT_F64: np.float64, DT_I32: np.int32,
-         DT_C32: np.complex64, DT_C64: np.complex128}
+         DT_C32: np.complex64, DT_C64: np.complex128, DT_I64: np.int64, DT_U8: np.uint8, DT_I8: np.int8,
+         DT_I16: np.int16, DT_U16: np.uint16, DT_U32: np.uint32, DT_U64: np.uint64}
 
 _lib = None
 

@@ -13,6 +13,13 @@ pub const NDCONV_F64: i32 = 1;
 pub const NDCONV_I32: i32 = 2;
 pub const NDCONV_C32: i32 = 3;
 pub const NDCONV_C64: i32 = 4;
+pub const NDCONV_I64: i32 = 5;
+pub const NDCONV_U8: i32 = 6;
+pub const NDCONV_I8: i32 = 7;
+pub const NDCONV_I16: i32 = 8;
+pub const NDCONV_U16: i32 = 9;
+pub const NDCONV_U32: i32 = 10;
+pub const NDCONV_U64: i32 = 11;
 
 // ---- ndconv_status
 pub const NDCONV_OK: i32 = 0;

@@ -11,8 +11,11 @@ use num::Complex;
 
 use crate::{BorderType, ConvMode, Error, KernelWithDilation, PaddingMode};
 
-/// Element types with a device implementation (f32, f64, i32, Complex<f32>,
-/// Complex<f64>); the original accepts any `NumAssign + Copy` type.
+/// Element types with a device implementation: f32, f64, Complex<f32>,
+/// Complex<f64> and the 8- to 64-bit integers (wrapping sums; integers other
+/// than i32 run `conv` one call at a time, and integer FFT convolution is
+/// refused as upstream documents it broken).  The original accepts any
+/// `NumAssign + Copy` type.
 pub trait DeviceElem: num::traits::NumAssign + Copy + 'static {
     /// `ndconv_dtype`
     const DTYPE: i32;
@@ -38,6 +41,19 @@ impl DeviceElem for i32 {
         [self as f64, 0.0]
     }
 }
+macro_rules! device_int {
+    ($($t:ty => $code:ident),*) => {$(
+        impl DeviceElem for $t {
+            const DTYPE: i32 = sys::$code;
+            fn parts(self) -> [f64; 2] {
+                [self as f64, 0.0]
+            }
+        }
+    )*};
+}
+device_int!(i8 => NDCONV_I8, u8 => NDCONV_U8, i16 => NDCONV_I16, u16 => NDCONV_U16, u32 => NDCONV_U32,
+            i64 => NDCONV_I64, u64 => NDCONV_U64);
+
 impl DeviceElem for Complex<f32> {
     const DTYPE: i32 = sys::NDCONV_C32;
     fn parts(self) -> [f64; 2] {

@@ -85,7 +85,8 @@ def test_last_error_message():
 
 def test_unsupported_ranks_and_element_types_are_refused():
     """The crate is generic over rank and element type; the library takes
-    ranks 1..3 and f32/f64/i32/c32/c64 and refuses the rest (no fallback)."""
+    ranks 1..3, f32/f64/c32/c64 and the 8- to 64-bit integers, and refuses
+    the rest (no fallback)."""
     from helpers import with_dilation
     p = problem(F32, np.ones((4, 5)), np.ones((3, 3)), ConvMode.Same, PaddingMode.Zeros)
     sh = (ctypes.c_int64 * 3)()
@@ -93,7 +94,7 @@ def test_unsupported_ranks_and_element_types_are_refused():
     q.rank = 4
     assert _abi.lib().ndconv_output_shape(ctypes.byref(q), 0, sh) == _abi.ERR_UNSUPPORTED
     assert "rank" in _abi.last_error()
-    for code in (5, 9, 100):  # no such element type in the ABI
+    for code in (12, 13, 100, -1):  # no such element type in the ABI
         q = _abi.Problem.from_buffer_copy(p)
         q.dtype = code
         assert _abi.lib().ndconv_output_shape(ctypes.byref(q), 0, sh) == _abi.ERR_UNSUPPORTED
@@ -101,9 +102,12 @@ def test_unsupported_ranks_and_element_types_are_refused():
     q = _abi.Problem.from_buffer_copy(p)
     q.rank = 0
     assert _abi.lib().ndconv_output_shape(ctypes.byref(q), 0, sh) == _abi.ERR_INVALID
-    for dt in (np.int8, np.int16, np.int64, np.uint8, np.uint32):
+    for dt in (np.float16, np.bool_):
         with pytest.raises(ndconv.Unsupported):
             ndconv.api.dtype_code(np.dtype(dt))
+    for dt, code in ((np.int8, _abi.I8), (np.uint8, _abi.U8), (np.int16, _abi.I16), (np.uint16, _abi.U16),
+                     (np.uint32, _abi.U32), (np.int64, _abi.I64), (np.uint64, _abi.U64)):
+        assert ndconv.api.dtype_code(np.dtype(dt)) == code
     with pytest.raises(ndconv.Unsupported):
         ndconv.build_problem(F32, (2, 2, 2, 2), with_dilation(np.ones((1, 1, 1, 1)), 1), ConvMode.Same,
                              PaddingMode.Zeros)
