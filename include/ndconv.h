@@ -193,8 +193,11 @@ int ndconv_conv_batch_host(const ndconv_problem *p, int32_t algo, int64_t n, con
 
 /* ConvExt::conv for f32 on the tensor cores: 3xBF16 split products
  * (x k ~ xh kh + xh kl + xl kh) accumulated in f32, normwise error ~1e-6 vs
- * f64.  Unit stride along the middle canonical axis only (else
- * NDCONV_ERR_UNSUPPORTED); non-finite inputs fall back to the FP32 loop so
+ * f64: row correlations of the padded data with groups of kernel rows on
+ * the tensor cores, summed over each group's rows in the epilogue.  Any
+ * strides, dilations, modes and borders (index ranges beyond the TMA
+ * coordinate range: NDCONV_ERR_UNSUPPORTED); non-finite inputs fall back to
+ * the FP32 loop so
  * NaN / Inf propagate as in the reference.  Same as
  * ndconv_conv_algo(p, NDCONV_ALGO_DIRECT_BF16X3, ...).  Asynchronous on
  * stream; a tensor-core pipeline wait that runs out (bounded at ~1 s, not
@@ -324,7 +327,9 @@ int ndconv_plan_info(const ndconv_problem *p, double out[8]);
  *                           (1, 2, 4, 8)
  *   NDCONV_TUNE_ROW_THREADS threads of FFT row-pass CTAs in launches of many
  *                           CTAs (a multiple of 32, at most 512)
- *   NDCONV_TUNE_BF16X3_BN   output rows per tensor-core tile (32 or 64)
+ *   NDCONV_TUNE_BF16X3_BN   output columns per tensor-core tile (16, 32 or
+ *                           64; taken when it times the group's kernel rows
+ *                           fits 256 MMA columns)
  *   NDCONV_TUNE_SW_RY       output rows per warp of the sliding-window
  *                           direct kernel (1, 2 or 4; f64 / c32 at most 2,
  *                           c64 1) */

@@ -12,6 +12,7 @@
 
 #include <atomic>
 #include <mutex>
+#include <map>
 #include <set>
 #include <utility>
 
@@ -36,17 +37,21 @@ extern "C" int ndconv_set_tuning(int32_t knob, int32_t value) {
 }
 extern "C" int32_t ndconv_get_tuning(int32_t knob) { return ndconv_tune(knob); }
 
+// The attribute is a per-(device, kernel) maximum: it is only ever raised, so
+// a launch with less shared memory never lowers it below what another launch
+// of the same kernel with more shared memory was granted.
 cudaError_t ndconv_allow_smem(const void *kernel, int bytes) {
     static std::mutex mu;
-    static std::set<std::pair<int, std::pair<const void *, int>>> done;
+    static std::map<std::pair<int, const void *>, int> granted;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     std::lock_guard<std::mutex> lk(mu);
-    auto key = std::make_pair(dev, std::make_pair(kernel, bytes));
-    if (done.count(key)) return cudaSuccess;
+    auto key = std::make_pair(dev, kernel);
+    auto it = granted.find(key);
+    if (it != granted.end() && it->second >= bytes) return cudaSuccess;
     e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e == cudaSuccess) done.insert(key);
+    if (e == cudaSuccess) granted[key] = bytes;
     return e;
 }
 

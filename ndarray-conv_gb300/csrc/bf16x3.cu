@@ -4,14 +4,27 @@
 // Each f32 value v is split as hi = bf16(v), lo = bf16(v - hi), and a
 // product x k is formed as xh kh + xh kl + xl kh (the dropped xl kl term and
 // the splits' rounding leave ~2^-16 relative error per product, below the
-// 1e-5 normwise bar).  The convolution becomes one GEMM per output tile:
-//   D[m][n] = sum over leading taps t = (kz, ky) and input offsets c of
-//             T_t[m][c] * X_t[n][c]
-// with m = 128 consecutive outputs along the contiguous axis (TMEM lanes),
-// n = BN consecutive output rows (TMEM columns), T_t the Toeplitz band of
-// kernel row t (T_t[m][c] = k[t][tx] when c = m s2 + tx d2), and X_t the
-// padded data rows (oz s0 + kz d0, oy + ky d1) over the tile's input window.
-// Both operands are K-major bf16 tiles of 64 elements (one 128-byte
+// 1e-5 normwise bar).
+//
+// Lowering: row correlations on the tensor cores, shifted sums in the
+// epilogue.  For an output plane oz and a tile of BN output columns starting
+// at ox0, correlating padded data row r with kernel row ky gives
+//   P[r][ky][b] = sum over kz, tx of kf[kz][ky][tx] X[oz s0 + kz d0][r][(ox0 + b) s2 + tx d2]
+// and output row oy is sum over ky of P[oy s1 + ky d1][ky][b].  The first sum
+// is one GEMM per 64-wide K chunk:
+//   D[m][n] = sum_c X[r0 + m][ox0 s2 + c] T[n][c],    n = (ky, b)
+// with M = 128 consecutive padded rows (TMEM lanes), N = G BN (G kernel rows
+// of a group times BN output columns: TMEM columns), K = the tile's input
+// window (BN - 1) s2 + (K2 - 1) d2 + 1 rounded up to 16, and T the Toeplitz
+// bands of the group's kernel rows: T[(ky, b)][c] = kf[kz][ky][tx] where
+// c = b s2 + tx d2.  The data operand (a 128-row x 64-column TMA box of the
+// padded plane) is shared by the G kernel rows, so one MMA covers a whole
+// group; the plane taps kz accumulate in TMEM.  The epilogue moves D through
+// shared memory and sums each output over the group's kernel rows; kernels
+// with more than G rows run as several groups whose sums add in registers.
+// A tile keeps the output rows whose G input rows lie inside its 128 rows.
+//
+// Operands are K-major bf16 tiles of 64 elements per row (one 128-byte
 // swizzled row) staged by TMA from two pre-built planes in global memory:
 // the padded data (border map applied once, split into hi / lo) and the
 // Toeplitz bands.  One thread issues TMA, one issues tcgen05.mma, all four
@@ -27,6 +40,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "common.cuh"
@@ -38,19 +52,16 @@
 namespace ndconv {
 namespace bf16x3 {
 
-constexpr int BM = 128;  // outputs along the contiguous axis per tile (TMEM lanes)
-constexpr int KC = 64;   // bf16 per K chunk: one 128-byte swizzled row
-constexpr int A_BYTES = BM * KC * 2;
-// BN output rows per tile (TMEM columns): 64, or 32 for problems whose
-// 64-row tiles would leave SMs idle
-template <int BN> struct Tile {
-    static constexpr int B_BYTES = BN * KC * 2;
-    static constexpr int STAGES = BN >= 64 ? 4 : 5;
-    static constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
-    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
-};
+constexpr int BM = 128;                 // padded rows per tile (TMEM lanes)
+constexpr int KC = 64;                  // bf16 per K chunk: one 128-byte swizzled row
+constexpr int A_BYTES = BM * KC * 2;    // one data box (hi or lo)
+constexpr int RP = 20;                  // floats per row of the epilogue's row block (16 + 4: no bank conflicts)
+constexpr int kRowBlockBytes = 3 * BM * RP * 4;  // the epilogue's exchange / row blocks
+constexpr int kMaxStages = 4;
+constexpr int kSmemLimit = 227 * 1024;
+constexpr int kSmemExtra = 1024 + 256 + kRowBlockBytes;  // alignment slack, barriers, row block
 constexpr long long kWaitCycles = 2000000000LL;  // ~1 s of polling before a wait gives up
-constexpr int kThreads = 128;
+constexpr int kThreads = 320;  // warps 0-7 epilogue (two groups), 8 TMA producer, 9 MMA issuer
 
 // Timeouts of any launch on this device since the last ndconv_bf16x3_status
 // call (a file-scope device variable: one per device that loads the library).
@@ -58,11 +69,19 @@ __device__ int g_timeouts;
 
 struct Params {
     int64_t out0, out1, out2;
-    int64_t s0, d0, d1;
-    int K0, K1;
-    int nchunk;  // K chunks per leading tap
-    int nseg;    // tiles along the contiguous axis
-    int64_t s2;
+    int64_t s0, d0, s1, d1, s2;
+    int K0;
+    int G, ngroups;      // kernel rows per group (zero rows pad the last), groups
+    int N;               // G * BN: MMA N and Toeplitz rows per (kz, group)
+    int mvalid;          // output rows per tile
+    int64_t nrt, nct;    // tiles along the middle and contiguous axes
+    int64_t ntiles;      // out0 * nrt * nct
+    int nchunk, klast;   // 64-wide K chunks per (group, kz); 16-wide steps in the last one
+    int stages, stage_bytes, ring_bytes;  // ring_bytes includes the resident Toeplitz tiles
+    int bres, b_off;     // Toeplitz tiles resident per group (at byte b_off), or in each stage
+    int tmem_cols;
+    int shfl_epi;        // epilogue by warp shuffles (unit middle stride, (G - 1) d1 < 32)
+    uint32_t idesc;
     float *y;
     int64_t ys0, ys1;
     int *status;  // bit 0: non-finite input seen; bit 1: a wait ran out
@@ -147,43 +166,84 @@ __device__ __forceinline__ void tmem_ld16(uint32_t addr, float *v) {
     for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// tcgen05.ld without the wait, and the wait tied to the loaded registers (so
+// that no use of them is scheduled before it)
+__device__ __forceinline__ void tmem_ld16_issue(uint32_t addr, uint32_t *r) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(addr));
+}
+__device__ __forceinline__ void tmem_ld_wait(uint32_t *r) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                   "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                   "+r"(r[15])
+                 :
+                 : "memory");
+}
+
 // ---- pre-passes -----------------------------------------------------------
 // Padded data planes [P0][P1][W] (hi, lo); zero beyond the padded extent.
-__global__ void split_data_kernel(const float *__restrict__ x, Geom3<float> g, int64_t W,
-                                  __nv_bfloat16 *__restrict__ hi, __nv_bfloat16 *__restrict__ lo, int *status) {
-    const int64_t P1 = g.ax[1].L, P2 = g.ax[2].L;
-    const int64_t total = g.ax[0].L * P1 * W;
+// A thread converts 8 consecutive samples of a row and stores them as
+// 16-byte vectors (W is a multiple of 8).
+__global__ void __launch_bounds__(256) split_data_kernel(const float *__restrict__ x, Geom3<float> g, int64_t W,
+                                                         __nv_bfloat16 *__restrict__ hi,
+                                                         __nv_bfloat16 *__restrict__ lo, int *status) {
+    const AxisGeom &A2 = g.ax[2];
+    const int64_t cw = W / 8, total = g.ax[0].L * g.ax[1].L * cw;
     bool bad = false;
     for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total;
          u += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i2 = u % W, r = u / W;
-        const int64_t i1 = r % P1, i0 = r / P1;
-        float v = 0.f;
-        if (i2 < P2)
-            v = resolve_padded<float>(x, g, axis_map(g.ax[0], i0), axis_map(g.ax[1], i1), axis_map(g.ax[2], i2));
-        if (!isfinite(v)) bad = true;
-        const __nv_bfloat16 h = __float2bfloat16_rn(v);
-        hi[u] = h;
-        lo[u] = __float2bfloat16_rn(v - __bfloat162float(h));
+        const int64_t row = u / cw, c0 = (u - row * cw) * 8;
+        const int64_t i1 = row % g.ax[1].L, i0 = row / g.ax[1].L;
+        const int64_t m0 = axis_map(g.ax[0], i0), m1 = axis_map(g.ax[1], i1);
+        uint32_t h[4], l[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            float v[2];
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                const int64_t i2 = c0 + 2 * e + q;
+                v[q] = i2 < A2.L ? resolve_padded<float>(x, g, m0, m1, axis_map(A2, i2)) : 0.f;
+                if (!isfinite(v[q])) bad = true;
+            }
+            const __nv_bfloat162 hh = __floats2bfloat162_rn(v[0], v[1]);
+            const float2 hf = __bfloat1622float2(hh);
+            const __nv_bfloat162 ll = __floats2bfloat162_rn(v[0] - hf.x, v[1] - hf.y);
+            h[e] = *reinterpret_cast<const uint32_t *>(&hh);
+            l[e] = *reinterpret_cast<const uint32_t *>(&ll);
+        }
+        *reinterpret_cast<uint4 *>(hi + row * W + c0) = make_uint4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<uint4 *>(lo + row * W + c0) = make_uint4(l[0], l[1], l[2], l[3]);
     }
     if (bad) atomicOr(status, 1);
 }
 
-// Toeplitz bands [K0 K1][BM][Cpad] (hi, lo): T_t[m][c] = kf[t][tx] where
-// c = m s2 + tx d2 (kf: the kernel in tap order, reversed for convolution).
-__global__ void toeplitz_kernel(const float *__restrict__ k, Geom3<float> g, int reverse, int64_t Cpad,
-                                __nv_bfloat16 *__restrict__ hi, __nv_bfloat16 *__restrict__ lo, int *status) {
+// Toeplitz bands [K0][ngroups][G][BN][Cp] (hi, lo): row (kz, group, kl, b),
+// column c holds kf[kz][ky][tx] when ky = group G + kl < K1 and
+// c = b s2 + tx d2 (kf: the kernel in tap order, reversed for convolution);
+// zero elsewhere (the padding rows of the last group included).
+__global__ void toeplitz_kernel(const float *__restrict__ k, Geom3<float> g, int reverse, int G, int BN,
+                                int ngroups, int64_t Cp, __nv_bfloat16 *__restrict__ hi,
+                                __nv_bfloat16 *__restrict__ lo, int *status) {
     const AxisGeom &A0 = g.ax[0], &A1 = g.ax[1], &A2 = g.ax[2];
-    const int64_t total = A0.K * A1.K * BM * Cpad;
+    const int64_t total = A0.K * ngroups * G * BN * Cp;
     bool bad = false;
     for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total;
          u += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t c = u % Cpad, r = u / Cpad;
-        const int64_t m = r % BM, t = r / BM;
-        const int64_t kz = t / A1.K, ky = t % A1.K;
+        const int64_t c = u % Cp;
+        int64_t r = u / Cp;
+        const int64_t b = r % BN;
+        r /= BN;
+        const int64_t kl = r % G;
+        r /= G;
+        const int64_t ky = (r % ngroups) * G + kl, kz = r / ngroups;
         float w = 0.f;
-        const int64_t off = c - m * A2.s;
-        if (off >= 0 && off % A2.d == 0 && off / A2.d < A2.K) {
+        const int64_t off = c - b * A2.s;
+        if (ky < A1.K && off >= 0 && off % A2.d == 0 && off / A2.d < A2.K) {
             const int64_t tx = off / A2.d;
             w = k[tap_source(kz, A0.K, reverse) * A0.ks + tap_source(ky, A1.K, reverse) * A1.ks +
                   tap_source(tx, A2.K, reverse) * A2.ks];
@@ -197,47 +257,97 @@ __global__ void toeplitz_kernel(const float *__restrict__ k, Geom3<float> g, int
 }
 
 // ---- main kernel ----------------------------------------------------------
+__device__ __forceinline__ void mbar_arrive(uint64_t *b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+// Named barriers of the epilogue warps: 1 (vote) and 2 over both groups
+// (256 threads), 3 over group 0 (128 threads).
+__device__ __forceinline__ bool epi_vote(bool pred) {
+    uint32_t r;
+    asm volatile(
+        "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n barrier.cta.red.or.pred q, 1, 256, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+        : "=r"(r)
+        : "r"((uint32_t)pred)
+        : "memory");
+    return r != 0;
+}
+__device__ __forceinline__ void epi_sync() { asm volatile("barrier.cta.sync 2, 256;" ::: "memory"); }
+__device__ __forceinline__ void grp0_sync() { asm volatile("barrier.cta.sync 3, 128;" ::: "memory"); }
+
+struct TileCoord {
+    int64_t oz, oy0, ox0;
+};
+// (32-bit division: the host keeps the tile count below 2^31)
+template <int BN> __device__ __forceinline__ TileCoord tile_of(const Params &P, int64_t t) {
+    const uint32_t tt = (uint32_t)t, nct = (uint32_t)P.nct, nrt = (uint32_t)P.nrt;
+    const uint32_t r = tt / nct;
+    TileCoord c;
+    c.ox0 = (int64_t)(tt - r * nct) * BN;
+    c.oy0 = (int64_t)(r % nrt) * P.mvalid;
+    c.oz = r / nrt;
+    return c;
+}
+
+// Persistent and warp-specialised: CTA b takes tiles b, b + grid, ...; per
+// tile the kernel-row groups are work items.  Warp 8 (one lane) streams the
+// items' stages through the TMA ring, warp 9 (one lane) issues the MMAs of
+// item j into TMEM buffer j % 2, warps 0-7 drain buffer j % 2 (the shifted
+// sums: warp shuffles, or a row block in shared memory) while the MMAs of
+// item j + 1 run in the other buffer.
 template <int BN>
 __global__ void __launch_bounds__(kThreads, 1)
-    conv_kernel(const __grid_constant__ CUtensorMap tA_hi, const __grid_constant__ CUtensorMap tA_lo,
-                const __grid_constant__ CUtensorMap tB_hi, const __grid_constant__ CUtensorMap tB_lo,
+    conv_kernel(const __grid_constant__ CUtensorMap tX_hi, const __grid_constant__ CUtensorMap tX_lo,
+                const __grid_constant__ CUtensorMap tT_hi, const __grid_constant__ CUtensorMap tT_lo,
                 const __grid_constant__ Params P) {
-    constexpr int STAGES = Tile<BN>::STAGES, STAGE_BYTES = Tile<BN>::STAGE_BYTES, B_BYTES = Tile<BN>::B_BYTES;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *base = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-    uint64_t *full = reinterpret_cast<uint64_t *>(base + STAGES * STAGE_BYTES);
-    uint64_t *empty = full + STAGES;
-    uint64_t *done = empty + STAGES;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
-    int *bad = reinterpret_cast<int *>(tmem_slot + 1);  // a role's wait ran out
+    float *R = reinterpret_cast<float *>(base + P.ring_bytes);  // [2][BM][RP]
+    uint64_t *full = reinterpret_cast<uint64_t *>(base + P.ring_bytes + kRowBlockBytes);
+    uint64_t *empty = full + kMaxStages;
+    uint64_t *tfull = empty + kMaxStages;
+    uint64_t *tempty = tfull + 2;
+    uint64_t *mdone = tempty + 2;
+    uint64_t *bfull = mdone + 1;  // resident Toeplitz tiles loaded
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bfull + 1);
+    int *bad = reinterpret_cast<int *>(tmem_slot + 1);     // some wait ran out
+    int *issued_out = bad + 1;                              // the producer's stage count
+    int *b_issued = issued_out + 1;                         // the producer's resident loads
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int q = blockIdx.x % P.nseg;          // tile along the contiguous axis
-    const int64_t oy0 = (int64_t)(blockIdx.x / P.nseg) * BN;
-    const int64_t oz = blockIdx.y;
+    const int64_t t0 = blockIdx.x, tstep = gridDim.x;
 
     if (*reinterpret_cast<volatile int *>(P.status) & 1) {
-        // non-finite input somewhere: the FP32 direct loop for this tile
-        for (int u = tid; u < BM * BN; u += kThreads) {
-            const int64_t ox = (int64_t)q * BM + (u % BM), oy = oy0 + u / BM;
-            if (ox < P.out2 && oy < P.out1)
-                direct_naive_one<float>(P.x, P.k, P.y, P.dp, (oz * P.out1 + oy) * P.out2 + ox);
+        // non-finite input somewhere: the FP32 direct loop for this CTA's tiles
+        for (int64_t t = t0; t < P.ntiles; t += tstep) {
+            const TileCoord c = tile_of<BN>(P, t);
+            for (int u = tid; u < P.mvalid * BN; u += kThreads) {
+                const int64_t oy = c.oy0 + u / BN, ox = c.ox0 + u % BN;
+                if (ox < P.out2 && oy < P.out1)
+                    direct_naive_one<float>(P.x, P.k, P.y, P.dp, (c.oz * P.out1 + oy) * P.out2 + ox);
+            }
         }
         return;
     }
 
     if (tid == 0) {
-        for (int s = 0; s < STAGES; s++) {
+        for (int s = 0; s < P.stages; s++) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(done, 1);
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&tfull[b], 1);
+            mbar_init(&tempty[b], 8);  // one arrival per epilogue warp
+        }
+        mbar_init(mdone, 1);
+        mbar_init(bfull, 1);
         *bad = 0;
+        *issued_out = 0;
+        *b_issued = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 0) {
+    if (warp == 9) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(BN)
+                     "r"(2 * P.tmem_cols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -245,95 +355,286 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
-    const int niter = P.K0 * P.K1 * P.nchunk;
+    volatile int *vbad = bad;
+    const int per_group = P.K0 * P.nchunk;
 
-    int issued = 0;  // producer: K steps whose TMA loads were issued
-    if (tid == 0) {
-        // producer: Toeplitz band tiles and data row tiles
-        const int x0 = (int)((int64_t)q * BM * P.s2);
-        for (int i = 0; i < niter; i++) {
-            const int s = i % STAGES;
-            if (i >= STAGES && !mbar_wait(&empty[s], ((i / STAGES) - 1) & 1)) {
-                atomicOr(bad, 1);
-                break;
+    if (warp == 8) {
+        if (lane == 0) {
+            // producer: data boxes (shared by a group's kernel rows) and the
+            // Toeplitz tiles -- in each stage, or loaded once and kept resident
+            // when the kernel is a single row group whose tiles fit
+            const int b_bytes = P.N * KC * 2;
+            int it = 0;
+            bool ok = true;
+            if (P.bres) {
+                mbar_expect_tx(bfull, per_group * 2 * b_bytes);
+                for (int i = 0; i < per_group; i++) {
+                    const int kz = i / P.nchunk, ch = i % P.nchunk;
+                    unsigned char *bs = base + P.b_off + i * 2 * b_bytes;
+                    tma_2d(bs, &tT_hi, ch * KC, kz * P.N, bfull);
+                    tma_2d(bs + b_bytes, &tT_lo, ch * KC, kz * P.N, bfull);
+                }
+                *b_issued = 1;
             }
-            const int t = i / P.nchunk, c = i % P.nchunk;
-            const int kz = t / P.K1, ky = t % P.K1;
-            unsigned char *st = base + s * STAGE_BYTES;
-            mbar_expect_tx(&full[s], STAGE_BYTES);
-            tma_2d(st, &tA_hi, c * KC, t * BM, &full[s]);
-            tma_2d(st + A_BYTES, &tA_lo, c * KC, t * BM, &full[s]);
-            const int by = (int)(oy0 + (int64_t)ky * P.d1), bz = (int)(oz * P.s0 + (int64_t)kz * P.d0);
-            tma_3d(st + 2 * A_BYTES, &tB_hi, x0 + c * KC, by, bz, &full[s]);
-            tma_3d(st + 2 * A_BYTES + B_BYTES, &tB_lo, x0 + c * KC, by, bz, &full[s]);
-            issued = i + 1;
+            for (int64_t t = t0; t < P.ntiles && ok && !*vbad; t += tstep) {
+                const TileCoord c = tile_of<BN>(P, t);
+                const int xb = (int)(c.ox0 * P.s2);
+                for (int g = 0; g < P.ngroups && ok; g++) {
+                    const int rb = (int)(c.oy0 * P.s1 + (int64_t)g * P.G * P.d1);
+                    for (int i = 0; i < per_group; i++, it++) {
+                        const int s = it % P.stages;
+                        if (it >= P.stages && !mbar_wait(&empty[s], ((it / P.stages) - 1) & 1)) {
+                            atomicOr(bad, 1);
+                            ok = false;
+                            break;
+                        }
+                        const int kz = i / P.nchunk, ch = i % P.nchunk;
+                        unsigned char *st = base + s * P.stage_bytes;
+                        mbar_expect_tx(&full[s], P.stage_bytes);
+                        const int z = (int)(c.oz * P.s0 + (int64_t)kz * P.d0);
+                        tma_3d(st, &tX_hi, xb + ch * KC, rb, z, &full[s]);
+                        tma_3d(st + A_BYTES, &tX_lo, xb + ch * KC, rb, z, &full[s]);
+                        if (!P.bres) {
+                            const int trow = (kz * P.ngroups + g) * P.N;
+                            tma_2d(st + 2 * A_BYTES, &tT_hi, ch * KC, trow, &full[s]);
+                            tma_2d(st + 2 * A_BYTES + b_bytes, &tT_lo, ch * KC, trow, &full[s]);
+                        }
+                    }
+                }
+            }
+            *issued_out = it;
         }
-    } else if (tid == 32) {
-        // MMA issuer: three split products per 16-wide K step
-        constexpr uint32_t idesc = idesc_bf16(BM, BN);
-        for (int i = 0; i < niter; i++) {
-            const int s = i % STAGES;
-            if (!mbar_wait(&full[s], (i / STAGES) & 1)) {
-                atomicOr(bad, 1);
-                break;
+    } else if (warp == 9) {
+        if (lane == 0) {
+            // MMA issuer: three split products per 16-wide K step, item j into buffer j % 2
+            const int b_bytes = P.N * KC * 2;
+            int it = 0, j = 0;
+            bool ok = !P.bres || mbar_wait(bfull, 0);
+            if (!ok) atomicOr(bad, 1);
+            for (int64_t t = t0; t < P.ntiles && ok && !*vbad; t += tstep) {
+                for (int g = 0; g < P.ngroups && ok; g++, j++) {
+                    const int buf = j & 1;
+                    if (j >= 2 && !mbar_wait(&tempty[buf], ((j >> 1) - 1) & 1)) {
+                        atomicOr(bad, 1);
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t d = tmem + (uint32_t)(buf * P.tmem_cols);
+                    for (int i = 0; i < per_group; i++, it++) {
+                        const int s = it % P.stages;
+                        if (!mbar_wait(&full[s], (it / P.stages) & 1)) {
+                            atomicOr(bad, 1);
+                            ok = false;
+                            break;
+                        }
+                        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                        const uint32_t sa = smem_u32(base + s * P.stage_bytes);
+                        const uint32_t a_hi = sa, a_lo = sa + A_BYTES;
+                        const uint32_t b_hi =
+                            P.bres ? smem_u32(base + P.b_off + i * 2 * b_bytes) : sa + 2 * A_BYTES;
+                        const uint32_t b_lo = b_hi + b_bytes;
+                        const int nk = (i % P.nchunk == P.nchunk - 1) ? P.klast : KC / 16;
+                        for (int kk = 0; kk < nk; kk++) {
+                            const uint32_t o = kk * 32;  // 16 bf16 along the swizzled 128-byte row
+                            mma_bf16(d, sw128_desc(a_hi + o), sw128_desc(b_hi + o), P.idesc, (i | kk) != 0);
+                            mma_bf16(d, sw128_desc(a_hi + o), sw128_desc(b_lo + o), P.idesc, 1);
+                            mma_bf16(d, sw128_desc(a_lo + o), sw128_desc(b_hi + o), P.idesc, 1);
+                        }
+                        mma_commit(&empty[s]);  // stage reusable once these MMAs have read it
+                    }
+                    if (!ok) break;
+                    mma_commit(&tfull[buf]);  // buffer ready once the item's MMAs finish
+                }
             }
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t sa = smem_u32(base + s * STAGE_BYTES);
-            const uint32_t a_hi = sa, a_lo = sa + A_BYTES, b_hi = sa + 2 * A_BYTES, b_lo = b_hi + B_BYTES;
+            // every MMA issued has finished before the CTA moves on
+            mma_commit(mdone);
+            if (!mbar_wait(mdone, 0)) atomicOr(bad, 1);
+        }
+    } else {
+        // epilogue: two groups of four warps (eg = warp / 4); warp w reads
+        // TMEM lanes 32 (w % 4) .. +31 (tile rows).  Output row y of the tile
+        // sums the kernel rows kl of the item at rows y s1 + kl d1; group eg
+        // takes the rows kl = eg, eg + 2, ... and group 0 combines.
+        const int eg = warp >> 2, et = tid & 127, ew = warp & 3;
+        const uint32_t lane_base = (uint32_t)(ew * 32) << 16;
+        float *X0 = R, *X1 = R + BM * RP, *X2 = R + 2 * BM * RP;  // exchange blocks
+        float acc[BN];
+        int j = 0, rbuf = 0;
+        bool stop = false;
+        for (int64_t t = t0; t < P.ntiles && !stop; t += tstep) {
+            const TileCoord c = tile_of<BN>(P, t);
 #pragma unroll
-            for (int kk = 0; kk < KC / 16; kk++) {
-                const uint32_t o = kk * 32;  // 16 bf16 along the swizzled 128-byte row
-                mma_bf16(tmem, sw128_desc(a_hi + o), sw128_desc(b_hi + o), idesc, (i | kk) != 0);
-                mma_bf16(tmem, sw128_desc(a_hi + o), sw128_desc(b_lo + o), idesc, 1);
-                mma_bf16(tmem, sw128_desc(a_lo + o), sw128_desc(b_hi + o), idesc, 1);
+            for (int q = 0; q < BN; q++) acc[q] = 0.f;
+            for (int g = 0; g < P.ngroups; g++, j++) {
+                const int buf = j & 1;
+                const bool late = !mbar_wait(&tfull[buf], (j >> 1) & 1);
+                if (epi_vote(late || *vbad)) {
+                    if (late) atomicOr(bad, 1);
+                    stop = true;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t tb = tmem + lane_base + (uint32_t)(buf * P.tmem_cols);
+                if (P.shfl_epi) {
+                    // unit middle stride, row shifts kl d1 < 32: lane l takes the
+                    // value of lane (l + kl d1) mod 32 of its own warp -- its own
+                    // output's term when l + kl d1 < 32, else a term of output
+                    // row l of the warp below (kept in spill); the partial sums
+                    // meet in shared memory once per 16 columns
+#pragma unroll
+                    for (int bc = 0; bc < BN / 16; bc++) {
+                        float own[16], spill[16];
+#pragma unroll
+                        for (int q = 0; q < 16; q++) own[q] = spill[q] = 0.f;
+                        auto sum_row = [&](const uint32_t *v, int kl) {
+                            const int sh = (int)(kl * P.d1);
+                            if (sh == 0) {
+#pragma unroll
+                                for (int q = 0; q < 16; q++) own[q] += __uint_as_float(v[q]);
+                                return;
+                            }
+                            const int src = (lane + sh) & 31;
+                            const bool mine = lane + sh < 32;
+#pragma unroll
+                            for (int q = 0; q < 16; q++) {
+                                const float a = __shfl_sync(0xffffffffu, __uint_as_float(v[q]), src);
+                                if (mine) own[q] += a;
+                                else spill[q] += a;
+                            }
+                        };
+                        // the next row's TMEM load is in flight while a row is summed
+                        uint32_t va[16], vb[16];
+                        int kl = eg;
+                        if (kl < P.G) {
+                            tmem_ld16_issue(tb + (uint32_t)(kl * BN + bc * 16), va);
+                            tmem_ld_wait(va);
+                        }
+                        for (; kl < P.G; kl += 4) {
+                            const bool more = kl + 2 < P.G;
+                            if (more) tmem_ld16_issue(tb + (uint32_t)((kl + 2) * BN + bc * 16), vb);
+                            sum_row(va, kl);
+                            if (more) {
+                                tmem_ld_wait(vb);
+                                const bool more2 = kl + 4 < P.G;
+                                if (more2) tmem_ld16_issue(tb + (uint32_t)((kl + 4) * BN + bc * 16), va);
+                                sum_row(vb, kl + 2);
+                                if (more2) tmem_ld_wait(va);
+                            }
+                        }
+                        // group 1: own -> X0, spill -> X1; group 0: spill -> X2
+                        float4 *d0 = reinterpret_cast<float4 *>((eg ? X1 : X2) + et * RP);
+#pragma unroll
+                        for (int q = 0; q < 4; q++)
+                            d0[q] = make_float4(spill[4 * q], spill[4 * q + 1], spill[4 * q + 2], spill[4 * q + 3]);
+                        if (eg) {
+                            float4 *d1 = reinterpret_cast<float4 *>(X0 + et * RP);
+#pragma unroll
+                            for (int q = 0; q < 4; q++)
+                                d1[q] = make_float4(own[4 * q], own[4 * q + 1], own[4 * q + 2], own[4 * q + 3]);
+                        }
+                        epi_sync();
+                        if (!eg) {
+                            auto add = [&](const float *blk, int row) {
+                                const float4 *s4 = reinterpret_cast<const float4 *>(blk + row * RP);
+#pragma unroll
+                                for (int q = 0; q < 4; q++) {
+                                    const float4 u = s4[q];
+                                    own[4 * q] += u.x;
+                                    own[4 * q + 1] += u.y;
+                                    own[4 * q + 2] += u.z;
+                                    own[4 * q + 3] += u.w;
+                                }
+                            };
+                            add(X0, et);
+                            if (ew < 3) {
+                                add(X2, et + 32);
+                                add(X1, et + 32);
+                            }
+#pragma unroll
+                            for (int q = 0; q < 16; q++) acc[bc * 16 + q] += own[q];
+                        }
+                        epi_sync();  // the blocks are rewritten for the next 16 columns
+                    }
+                } else if (!eg) {
+                    // any stride: the rows pass through a double-buffered row
+                    // block, one kernel row at a time (group 0 alone)
+#pragma unroll
+                    for (int bc = 0; bc < BN / 16; bc++) {
+                        for (int kl = 0; kl < P.G; kl++, rbuf ^= 1) {
+                            float v[16];
+                            tmem_ld16(tb + (uint32_t)(kl * BN + bc * 16), v);
+                            float *Rb = R + rbuf * (BM * RP);
+                            float4 *dst = reinterpret_cast<float4 *>(Rb + et * RP);
+#pragma unroll
+                            for (int q = 0; q < 4; q++)
+                                dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                            grp0_sync();
+                            if (et < P.mvalid) {
+                                const int r = (int)(et * P.s1 + kl * P.d1);  // < BM by the choice of mvalid
+                                const float4 *src = reinterpret_cast<const float4 *>(Rb + r * RP);
+#pragma unroll
+                                for (int q = 0; q < 4; q++) {
+                                    const float4 u = src[q];
+                                    acc[bc * 16 + 4 * q] += u.x;
+                                    acc[bc * 16 + 4 * q + 1] += u.y;
+                                    acc[bc * 16 + 4 * q + 2] += u.z;
+                                    acc[bc * 16 + 4 * q + 3] += u.w;
+                                }
+                            }
+                        }
+                    }
+                }
+                // buffer free for item j + 2
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&tempty[buf]);
             }
-            mma_commit(&empty[s]);  // stage reusable once these MMAs have read it
+            if (!stop && !eg && et < P.mvalid && c.oy0 + et < P.out1) {
+                float *yr = P.y + c.oz * P.ys0 + (c.oy0 + et) * P.ys1 + c.ox0;
+                if (c.ox0 + BN <= P.out2 && (reinterpret_cast<uintptr_t>(yr) & 15) == 0) {
+#pragma unroll
+                    for (int q = 0; q < BN / 4; q++)
+                        reinterpret_cast<float4 *>(yr)[q] =
+                            make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < BN; q++)
+                        if (c.ox0 + q < P.out2) yr[q] = acc[q];
+                }
+            }
         }
-        mma_commit(done);
     }
-    __syncwarp();
-    // accumulator complete?  (one waiter; the verdict is shared so that the
-    // warp-collective TMEM loads below run uniformly or not at all)
-    if (tid == 0 && !mbar_wait(done, 0)) atomicOr(bad, 1);
+    __syncwarp();  // the producer and MMA warps reconverge after their single-lane roles
     __syncthreads();
-    const bool good = (*reinterpret_cast<volatile int *>(bad) == 0);
-    if (!good) {
-        // a pipeline wait ran out (not expected): the tile's outputs become NaN
+    if (*vbad) {
+        // a pipeline wait ran out (not expected): this CTA's tiles become NaN
         // and the per-device word keeps the event.  Before the shared memory
-        // and TMEM are released, the loads already issued must have landed and
-        // the MMAs already issued must have finished (waits bounded as well).
+        // and TMEM are released, the loads already issued must have landed
+        // (the MMAs issued have finished: mdone); waits bounded as well.
         if (tid == 0) {
-            for (int i = issued > STAGES ? issued - STAGES : 0; i < issued; i++)
-                mbar_wait(&full[i % STAGES], (i / STAGES) & 1);
-            mbar_wait(done, 0);
+            const int issued = *issued_out;
+            for (int i = issued > P.stages ? issued - P.stages : 0; i < issued; i++)
+                mbar_wait(&full[i % P.stages], (i / P.stages) & 1);
+            if (*b_issued) mbar_wait(bfull, 0);
             atomicOr(P.status, 2);
             atomicOr(&g_timeouts, 1);
         }
-        for (int u = tid; u < BM * BN; u += kThreads) {
-            const int64_t ox = (int64_t)q * BM + (u % BM), oy = oy0 + u / BM;
-            if (ox < P.out2 && oy < P.out1) P.y[oz * P.ys0 + oy * P.ys1 + ox] = __int_as_float(0x7fc00000);
-        }
-    }
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (good) {
-        const int m = warp * 32 + lane;  // TMEM lane = output along the contiguous axis
-        const int64_t ox = (int64_t)q * BM + m;
-        float *yrow = P.y + oz * P.ys0 + ox;
-#pragma unroll
-        for (int c0 = 0; c0 < BN; c0 += 16) {
-            float v[16];
-            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c0, v);
-#pragma unroll
-            for (int j = 0; j < 16; j++) {
-                const int64_t oy = oy0 + c0 + j;
-                if (ox < P.out2 && oy < P.out1) yrow[oy * P.ys1] = v[j];
+        for (int64_t t = t0; t < P.ntiles; t += tstep) {
+            const TileCoord c = tile_of<BN>(P, t);
+            for (int u = tid; u < P.mvalid * BN; u += kThreads) {
+                const int64_t oy = c.oy0 + u / BN, ox = c.ox0 + u % BN;
+                if (ox < P.out2 && oy < P.out1) P.y[c.oz * P.ys0 + oy * P.ys1 + ox] = __int_as_float(0x7fc00000);
             }
         }
+        __syncthreads();
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 0) {
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN) : "memory");
+    if (warp == 9) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * P.tmem_cols)
+                     : "memory");
     }
 }
 
@@ -368,15 +669,74 @@ int make_map(CUtensorMap *m, void *base, int rank, const cuuint64_t *dims, const
     return NDCONV_OK;
 }
 
-// Which problems the split path takes (f32; unit stride along the middle
-// axis; all index ranges within the TMA coordinate range).
+// Tile plan of one problem.
+struct TilePlan {
+    int G, ngroups, BN, N;
+    int64_t Kpad;  // K extent of one row correlation (multiple of 16)
+    int nchunk, klast;
+    int mvalid;
+    int stages, stage_bytes, ring_bytes, smem;
+    int bres, b_off;
+};
+
+inline int64_t kpad_of(const AxisGeom &A2, int BN) {
+    return ((BN - 1) * A2.s + (A2.K - 1) * A2.d + 1 + 15) / 16 * 16;
+}
+
+// Kernel rows per group: at most 16, and few enough that (G - 1) d1 leaves
+// at least half of the 128 staged rows as outputs; the groups are evened out.
+// Output columns per tile BN (16, 32 or 64, with G BN <= 256): the
+// autotuner's choice when it fits, else the one with the least modelled MMA
+// time per output -- an MMA of N columns costs max(N / 2, (4096 + 32 N) / 128)
+// cycles (tensor rate, or shared-memory reads of its two operands).
+TilePlan plan_tiles(const Plan3 &P) {
+    const AxisGeom *A = P.ax;
+    TilePlan t{};
+    int G = (int)std::min<int64_t>(A[1].K, 16);
+    while (G > 1 && (G - 1) * A[1].d > 63) G--;
+    t.ngroups = (int)((A[1].K + G - 1) / G);
+    t.G = (int)((A[1].K + t.ngroups - 1) / t.ngroups);
+    double best = 1e300;
+    for (int bn = 16; bn <= 64; bn *= 2) {
+        if (t.G * bn > 256) break;
+        const int n = t.G * bn;
+        const double mma = std::max(n / 2.0, (4096.0 + 32.0 * n) / 128.0);
+        const double cost = (double)(kpad_of(A[2], bn) / 16) * mma / bn;
+        if (cost < best) {
+            best = cost;
+            t.BN = bn;
+        }
+    }
+    const int want = ndconv_tune(NDCONV_TUNE_BF16X3_BN);
+    if ((want == 16 || want == 32 || want == 64) && t.G * want <= 256) t.BN = want;
+    t.N = t.G * t.BN;
+    t.Kpad = kpad_of(A[2], t.BN);
+    t.nchunk = (int)((t.Kpad + KC - 1) / KC);
+    t.klast = (int)((t.Kpad - (int64_t)(t.nchunk - 1) * KC) / 16);
+    t.mvalid = (int)((BM - 1 - (int64_t)(t.G - 1) * A[1].d) / A[1].s + 1);
+    // a kernel of one row group whose Toeplitz tiles (all plane taps and K
+    // chunks) take at most 96 KB keeps them in shared memory for the whole
+    // launch; the ring then streams only the data boxes
+    const int bslot = 2 * t.N * KC * 2;
+    const int64_t bres_bytes = (int64_t)A[0].K * t.nchunk * bslot;
+    t.bres = t.ngroups == 1 && bres_bytes <= 96 * 1024;
+    t.stage_bytes = 2 * A_BYTES + (t.bres ? 0 : bslot);
+    t.stages = std::min<int64_t>(kMaxStages, (kSmemLimit - kSmemExtra - (t.bres ? bres_bytes : 0)) / t.stage_bytes);
+    t.b_off = t.stages * t.stage_bytes;
+    t.ring_bytes = t.b_off + (t.bres ? (int)bres_bytes : 0);
+    t.smem = t.ring_bytes + kSmemExtra;
+    return t;
+}
+
+// Which problems the split path takes (f32; all index ranges within the TMA
+// coordinate range).
 bool applies(const Plan3 &P) {
     const AxisGeom *A = P.ax;
     if (P.dtype != NDCONV_F32) return false;
-    if (A[1].s != 1) return false;
     for (int a = 0; a < 3; a++)
-        if (A[a].L > (1 << 30) || A[a].out < 1) return false;
-    return (int64_t)A[0].K * A[1].K * BM < (1 << 30);
+        if (A[a].L > (1 << 30) || A[a].out < 1 || A[a].s > (1 << 20) || A[a].d > (1 << 20)) return false;
+    return A[0].K * (2 * A[1].K + 16) * 64 < (1 << 30) && A[2].K * A[2].d < (1 << 28) &&
+           A[0].L * A[1].L < 0x7fffffff;
 }
 
 }  // namespace bf16x3
@@ -391,14 +751,22 @@ extern "C" int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, con
     int s = plan_problem(p, 0, &P);
     if (s) return s;
     if (!data || !kernel || !out) return ndconv_fail(NDCONV_ERR_INVALID, "null pointer");
-    if (!applies(P)) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "3xBF16 path: f32 with unit middle-axis stride only");
+    if (!applies(P)) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "3xBF16 path: f32 within the TMA index range only");
     cudaStream_t st = (cudaStream_t)stream;
     const AxisGeom *A = P.ax;
     const Geom3<float> g = P.geom<float>();
-    const int64_t Cpad = ((BM - 1) * A[2].s + (A[2].K - 1) * A[2].d + 1 + KC - 1) / KC * KC;
-    const int64_t W = (A[2].L + 7) / 8 * 8;  // row pitch (16-byte multiple)
-    const int64_t L = A[0].K * A[1].K;
-    const size_t nX = (size_t)(A[0].L * A[1].L * W), nT = (size_t)(L * BM * Cpad);
+    const TilePlan T = plan_tiles(P);
+    const int64_t Cp = (int64_t)T.nchunk * KC;                  // Toeplitz row pitch (elements)
+    const int64_t W = std::max<int64_t>(KC, (A[2].L + 7) / 8 * 8);  // data row pitch (16-byte multiple)
+    const int64_t Rt = A[0].K * T.ngroups * T.N;                // Toeplitz rows
+    const size_t nX = (size_t)(A[0].L * A[1].L * W), nT = (size_t)(Rt * Cp);
+    const int64_t nrt = (A[1].out + T.mvalid - 1) / T.mvalid, nct = (A[2].out + T.BN - 1) / T.BN;
+    const int64_t ntiles = A[0].out * nrt * nct;
+    int dev = 0, nsm = 0;
+    NDCONV_CUDA_OK(cudaGetDevice(&dev));
+    NDCONV_CUDA_OK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    if (ntiles >= 0x7fffffff) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "too many tiles");
+    const int64_t gx = std::min<int64_t>(ntiles, nsm);  // persistent: one CTA per SM
     unsigned char *ws = nullptr;
     const size_t bytes = 2 * sizeof(__nv_bfloat16) * (nX + nT) + 256;
     NDCONV_CUDA_OK(cudaMallocAsync((void **)&ws, bytes, st));
@@ -409,26 +777,26 @@ extern "C" int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, con
         cudaFreeAsync(ws, st);
         return code;
     };
-    // 64-row tiles, or 32 when 64 would give fewer than two CTAs per SM
-    const int64_t nseg = (A[2].out + BM - 1) / BM;
-    int BN = (nseg * ((A[1].out + 63) / 64) * A[0].out < 2 * 152) ? 32 : 64;
-    const int want_bn = ndconv_tune(NDCONV_TUNE_BF16X3_BN);  // the autotuner's choice
-    if (want_bn == 32 || want_bn == 64) BN = want_bn;
-    CUtensorMap mAh, mAl, mBh, mBl;
+    CUtensorMap mXh, mXl, mTh, mTl;
     {
-        const cuuint64_t dA[2] = {(cuuint64_t)Cpad, (cuuint64_t)(L * BM)};
-        const cuuint64_t sA[1] = {(cuuint64_t)Cpad * 2};
-        const cuuint32_t bA[2] = {KC, BM};
-        const cuuint64_t dB[3] = {(cuuint64_t)W, (cuuint64_t)A[1].L, (cuuint64_t)A[0].L};
-        const cuuint64_t sB[2] = {(cuuint64_t)W * 2, (cuuint64_t)(W * A[1].L * 2)};
-        const cuuint32_t bB[3] = {KC, (cuuint32_t)BN, 1};
-        if ((s = make_map(&mAh, th, 2, dA, sA, bA)) || (s = make_map(&mAl, tl, 2, dA, sA, bA)) ||
-            (s = make_map(&mBh, xh, 3, dB, sB, bB)) || (s = make_map(&mBl, xl, 3, dB, sB, bB)))
+        const cuuint64_t dX[3] = {(cuuint64_t)W, (cuuint64_t)A[1].L, (cuuint64_t)A[0].L};
+        const cuuint64_t sX[2] = {(cuuint64_t)W * 2, (cuuint64_t)(W * A[1].L * 2)};
+        const cuuint32_t bX[3] = {KC, BM, 1};
+        const cuuint64_t dT[2] = {(cuuint64_t)Cp, (cuuint64_t)Rt};
+        const cuuint64_t sT[1] = {(cuuint64_t)Cp * 2};
+        const cuuint32_t bT[2] = {KC, (cuuint32_t)T.N};
+        if ((s = make_map(&mXh, xh, 3, dX, sX, bX)) || (s = make_map(&mXl, xl, 3, dX, sX, bX)) ||
+            (s = make_map(&mTh, th, 2, dT, sT, bT)) || (s = make_map(&mTl, tl, 2, dT, sT, bT)))
             return fail(s);
     }
     cudaMemsetAsync(status, 0, sizeof(int), st);
-    split_data_kernel<<<152 * 8, 256, 0, st>>>(static_cast<const float *>(data), g, W, xh, xl, status);
-    toeplitz_kernel<<<152 * 4, 256, 0, st>>>(static_cast<const float *>(kernel), g, P.reverse, Cpad, th, tl, status);
+    {
+        const int64_t items = A[0].L * A[1].L * (W / 8);
+        const unsigned nb = (unsigned)std::max<int64_t>(1, std::min<int64_t>(152 * 16, (items + 255) / 256));
+        split_data_kernel<<<nb, 256, 0, st>>>(static_cast<const float *>(data), g, W, xh, xl, status);
+    }
+    toeplitz_kernel<<<152 * 4, 256, 0, st>>>(static_cast<const float *>(kernel), g, P.reverse, T.G, T.BN,
+                                             T.ngroups, Cp, th, tl, status);
     ndconv_count_launch(2);
     Params Q{};
     Q.out0 = A[0].out;
@@ -436,12 +804,27 @@ extern "C" int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, con
     Q.out2 = A[2].out;
     Q.s0 = A[0].s;
     Q.d0 = A[0].d;
+    Q.s1 = A[1].s;
     Q.d1 = A[1].d;
-    Q.K0 = (int)A[0].K;
-    Q.K1 = (int)A[1].K;
-    Q.nchunk = (int)(Cpad / KC);
-    Q.nseg = (int)((A[2].out + BM - 1) / BM);
     Q.s2 = A[2].s;
+    Q.K0 = (int)A[0].K;
+    Q.G = T.G;
+    Q.ngroups = T.ngroups;
+    Q.N = T.N;
+    Q.mvalid = T.mvalid;
+    Q.nrt = nrt;
+    Q.nct = nct;
+    Q.ntiles = ntiles;
+    Q.nchunk = T.nchunk;
+    Q.klast = T.klast;
+    Q.stages = T.stages;
+    Q.stage_bytes = T.stage_bytes;
+    Q.ring_bytes = T.ring_bytes;
+    Q.bres = T.bres;
+    Q.b_off = T.b_off;
+    Q.shfl_epi = (A[1].s == 1 && (T.G - 1) * A[1].d < 32) ? 1 : 0;
+    Q.tmem_cols = T.N <= 32 ? 32 : T.N <= 64 ? 64 : T.N <= 128 ? 128 : 256;
+    Q.idesc = idesc_bf16(BM, T.N);
     Q.y = static_cast<float *>(out);
     Q.ys0 = A[1].out * A[2].out;
     Q.ys1 = A[2].out;
@@ -449,15 +832,15 @@ extern "C" int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, con
     Q.dp = P.direct<float>();
     Q.x = static_cast<const float *>(data);
     Q.k = static_cast<const float *>(kernel);
-    const int64_t gx = (int64_t)Q.nseg * ((A[1].out + BN - 1) / BN);
-    if (gx > 0x7fffffff || A[0].out > 65535) return fail(ndconv_fail(NDCONV_ERR_UNSUPPORTED, "grid too large"));
-    const void *fn = BN == 32 ? (const void *)conv_kernel<32> : (const void *)conv_kernel<64>;
-    const int smem = BN == 32 ? Tile<32>::SMEM_BYTES : Tile<64>::SMEM_BYTES;
-    cudaError_t e = ndconv_allow_smem(fn, smem);
+    const void *fn = T.BN == 16   ? (const void *)conv_kernel<16>
+                     : T.BN == 32 ? (const void *)conv_kernel<32>
+                                  : (const void *)conv_kernel<64>;
+    cudaError_t e = ndconv_allow_smem(fn, T.smem);
     if (e != cudaSuccess) return fail(ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e)));
-    const dim3 grid((unsigned)gx, (unsigned)A[0].out);
-    if (BN == 32) conv_kernel<32><<<grid, kThreads, smem, st>>>(mAh, mAl, mBh, mBl, Q);
-    else conv_kernel<64><<<grid, kThreads, smem, st>>>(mAh, mAl, mBh, mBl, Q);
+    const dim3 grid((unsigned)gx);
+    if (T.BN == 16) conv_kernel<16><<<grid, kThreads, T.smem, st>>>(mXh, mXl, mTh, mTl, Q);
+    else if (T.BN == 32) conv_kernel<32><<<grid, kThreads, T.smem, st>>>(mXh, mXl, mTh, mTl, Q);
+    else conv_kernel<64><<<grid, kThreads, T.smem, st>>>(mXh, mXl, mTh, mTl, Q);
     ndconv_count_launch();
     e = cudaGetLastError();
     cudaFreeAsync(ws, st);  // stream-ordered: after the launch has finished with it

@@ -31,7 +31,7 @@ from .api import build_problem, with_dilation
 # (variant, [knob settings]) -- settings are {knob: value}; {} is the library's choice
 KNOB_SPACE = [
     (_abi.ALGO_DIRECT, [{}] + [{_abi.TUNE_SW_TY: t, _abi.TUNE_SW_RY: r} for t in (1, 2, 4, 8) for r in (1, 2, 4)]),
-    (_abi.ALGO_DIRECT_BF16X3, [{}] + [{_abi.TUNE_BF16X3_BN: b} for b in (32, 64)]),
+    (_abi.ALGO_DIRECT_BF16X3, [{}] + [{_abi.TUNE_BF16X3_BN: b} for b in (16, 32, 64)]),
     (_abi.ALGO_FFT_ND, [{}] + [{_abi.TUNE_ROW_THREADS: t} for t in (128, 256, 512)]),
     (_abi.ALGO_FFT_RS, [{_abi.TUNE_MAC_ROWS: m, _abi.TUNE_ROW_THREADS: t} if (m or t) else {}
                         for m in (0, 1, 2, 4) for t in (0, 256, 512)]),

@@ -30,6 +30,13 @@ def _lib():
     ((1000,), (31,), 1, ConvMode.Full, PaddingMode.Zeros),
     ((130, 257), (17, 17), 1, ConvMode.Valid, PaddingMode.Zeros),
     ((64, 640), (15, 63), 1, ConvMode.Same, PaddingMode.Circular),
+    # strides along the middle axis, kernels of several row groups, dilation
+    # that shrinks the row groups, rows of one output
+    ((90, 300), (5, 9), [3, 2], ConvMode.Custom([3, 2], [3, 2]), PaddingMode.Reflect),
+    ((300, 200), (40, 21), 1, ConvMode.Same, PaddingMode.Zeros),
+    ((260, 180), (9, 7), [30, 1], ConvMode.Same, PaddingMode.Replicate),
+    ((4, 260, 90), (3, 33, 5), [2, 1, 3], ConvMode.Custom([2, 5, 1], [1, 3, 2]), PaddingMode.Zeros),
+    ((1, 4000), (1, 127), 1, ConvMode.Valid, PaddingMode.Zeros),
 ])
 def test_bf16x3_vs_oracle(shape, kshape, dil, mode, pm):
     rng = np.random.default_rng(sum(shape) + sum(kshape))
@@ -65,9 +72,26 @@ def test_bf16x3_nonfinite_follows_reference():
     assert np.allclose(y[fin], y64[fin], rtol=1e-5, atol=1e-5)
 
 
+@pytest.mark.parametrize("bn", [16, 32, 64])
+def test_bf16x3_tile_widths_agree(bn):
+    """Every tile width the tuner may pick meets the same bound."""
+    rng = np.random.default_rng(bn)
+    x = rng.random((150, 333)).astype(np.float32) - 0.5
+    k = rng.random((3, 19)).astype(np.float32) - 0.5
+    mode, pm = ConvMode.Same, PaddingMode.Custom([BorderType.Circular, BorderType.Reflect])
+    y64 = _oracle64(x, k, mode, pm)
+    L = _abi.lib()
+    old = L.ndconv_get_tuning(_abi.TUNE_BF16X3_BN)
+    try:
+        assert L.ndconv_set_tuning(_abi.TUNE_BF16X3_BN, bn) == 0
+        assert normwise_err(ndconv.conv_algo(x, k, mode, pm, BF), y64) <= TOL32
+    finally:
+        L.ndconv_set_tuning(_abi.TUNE_BF16X3_BN, old)
+
+
 def test_bf16x3_unsupported():
     x = np.ones((30, 40), np.float32)
     with pytest.raises(ndconv.ConvError):
-        ndconv.conv_algo(x, np.ones((3, 3), np.float32), ConvMode.Custom([1, 1], [2, 1]), PaddingMode.Zeros, BF)
+        ndconv.conv_algo(x.astype(np.float64), np.ones((3, 3)), ConvMode.Same, PaddingMode.Zeros, BF)
     with pytest.raises(ndconv.ConvError):
         ndconv.conv_algo(x.astype(np.int32), np.ones((3, 3), np.int32), ConvMode.Same, PaddingMode.Zeros, BF)
