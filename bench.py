@@ -18,6 +18,9 @@ The default line also carries, in `config`:
   uneven_batch  the uneven batch (4096 instances, one persistent launch +
                 CUDA graph, dispatcher-picked variants) against the plain
                 drop-in (per-instance calls with the library's default picks)
+  variants      the 1-D and 3-D cases (and the 3-D complex copy, and a 2-D
+                31 x 31 kernel) through direct FP32, 3xBF16 tensor cores
+                and FFT: device time per call and error against f64
 Reference arm (--impl reference): the oracle port of conv_fft_par (same
 algorithm as the crate, rayon-style threads on all host cores) over the
 same 64 instances per step.  The GPU line's cpu_baseline is that arm run as
@@ -442,6 +445,90 @@ def cpu_baseline_uneven(specs, seconds):
             "sample": f"{n} random instances of the uneven batch (conv_fft_par port, f32) in {el:.1f} s"}
 
 
+# The benchmark's other single-instance cases, each through every variant
+# that applies (device time of one call, CUDA-graph replay), with its
+# normwise error against the f64 oracle: (key, description, x shape, kernel
+# shape, mode, padding, dtype, variants)
+VARIANT_CASES = [
+    ("c1", "1-D f32 x[5000] * k[31], Full, Zeros", (5000,), (31,), "Full", "Zeros", "f32", ["direct", "fft"]),
+    ("c3", "3-D f32 x[10,100,200] * k[5,11,31], Same, Zeros", (10, 100, 200), (5, 11, 31), "Same", "Zeros", "f32",
+     ["direct", "bf16x3", "fft"]),
+    ("c3_complex", "3-D Complex<f32> x[10,100,200] * k[5,11,31] (re, im i.i.d. N(0,1)), Same, Zeros",
+     (10, 100, 200), (5, 11, 31), "Same", "Zeros", "c32", ["direct", "fft"]),
+    ("2d_k31x31", "2-D f32 x[1024,1024] * k[31,31], Same, Zeros (a dense kernel of >= 15 taps per axis)",
+     (1024, 1024), (31, 31), "Same", "Zeros", "f32", ["direct", "bf16x3", "fft"]),
+]
+VARIANT_ALGO = {"direct": 0, "bf16x3": 2, "fft": 1}
+
+
+def measure_variants(reps=20):
+    """Device time of one call of each variant on each VARIANT_CASES case
+    (one call captured in a CUDA graph, replayed `reps` times between CUDA
+    events), the FP32-equivalent rate 2 |y| taps / t, and the normwise error
+    against the f64 oracle's direct loop."""
+    out = {}
+    for key, desc, xs, ksh, mode_n, pad_n, dt, variants in VARIANT_CASES:
+        try:
+            out[key] = _variant_case(desc, xs, ksh, mode_n, pad_n, dt, variants, reps)
+        except Exception as ex:  # the line still prints; the case records why it has no figures
+            out[key] = {"workload": desc, "error": f"{type(ex).__name__}: {ex}"[:200]}
+    return out
+
+
+def _variant_case(desc, xs, ksh, mode_n, pad_n, dt, variants, reps):
+    import torch
+    import ndconv
+    from ndconv import _abi, build_problem, ConvMode, PaddingMode, with_dilation
+    from oracle import oracle as O
+    mode, pm = getattr(ConvMode, mode_n), getattr(PaddingMode, pad_n)
+    rng = np.random.default_rng(3000 + len(xs))
+    if dt == "c32":
+        x = (rng.standard_normal(xs) + 1j * rng.standard_normal(xs)).astype(np.complex64)
+        k = (rng.standard_normal(ksh) + 1j * rng.standard_normal(ksh)).astype(np.complex64)
+        d64 = _abi.C64
+    else:
+        x = rng.random(xs, dtype=np.float32)
+        k = rng.random(ksh, dtype=np.float32)
+        d64 = _abi.F64
+    st, y64 = O.conv(build_problem(d64, xs, with_dilation(k, 1), mode, pm),
+                     x.astype(np.complex128 if dt == "c32" else np.float64),
+                     k.astype(np.complex128 if dt == "c32" else np.float64))
+    xd, kd = torch.from_numpy(x).cuda(), torch.from_numpy(k).cuda()
+    res = {"workload": desc}
+    for v in variants:
+        algo = VARIANT_ALGO[v]
+        for _ in range(3):
+            y = ndconv.conv_algo(xd, kd, mode, pm, algo)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            with torch.cuda.graph(g, stream=side):
+                y = ndconv.conv_algo(xd, kd, mode, pm, algo)
+        torch.cuda.synchronize()
+        g.replay()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            g.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        us = e0.elapsed_time(e1) / reps * 1e3
+        yh = y.cpu().numpy().astype(y64.dtype)
+        err = float(np.linalg.norm(yh - y64) / np.linalg.norm(y64)) if st == 0 else None
+        taps = float(np.prod(ksh))
+        flops = (8.0 if dt == "c32" else 2.0) * float(np.prod(y64.shape)) * taps
+        res[v] = {"us_per_call": us, "normwise_err": err, "fp32_equiv_tflops": flops / (us * 1e-6) / 1e12}
+        del g
+    fastest = min(variants, key=lambda v: res[v]["us_per_call"])
+    res["fastest"] = fastest
+    if "bf16x3" in variants:
+        res["bf16x3_over_direct_speedup"] = res["direct"]["us_per_call"] / res["bf16x3"]["us_per_call"]
+    return res
+
+
 def measure_c2(args, algo, form, world, rank, local_rank, dist):
     """The 2-D case over B instances: conv_fft (algo 1) or conv (algo 0),
     batched or one call per instance; device-resident, plain per-instance
@@ -627,10 +714,12 @@ def main():
             return bench_uneven(args, world, rank, local_rank, dist)
         algo = 1 if args.algo == "fft" else 0
         r = measure_c2(args, algo, args.form, world, rank, local_rank, dist)
-        extra_direct = extra_uneven = None
+        extra_direct = extra_uneven = extra_variants = None
         if not args.no_extra and algo == 1 and args.form == "batched":
             extra_direct = measure_c2(args, 0, "batched", world, rank, local_rank, dist)
             extra_uneven = measure_uneven(args, world, rank, local_rank, dist)
+            if rank == 0:
+                extra_variants = measure_variants()
         if rank != 0:
             return
         B = args.batch
@@ -664,6 +753,8 @@ def main():
                                 "clocks": d["clocks"]}
         if extra_uneven:
             config["uneven_batch"] = uneven_summary(extra_uneven, world)
+        if extra_variants:
+            config["variants"] = extra_variants
         line = {
             "metric": METRIC,
             "value": gbs(r["ms"]), "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
