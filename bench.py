@@ -260,8 +260,11 @@ def measure_uneven(args, world, rank, local_rank, dist):
     kbuf.uniform_(-1, 1, generator=gen)
     if args.dispatch == "mlp":
         from ndconv.mlp import MLPDispatcher, default_available
+        # the tensor-core variant runs beside the queue as ordinary launches
+        # that want every SM's shared memory; measured on this batch it only
+        # costs (71 ms per step without it, 112 ms with its 87 largest picks)
         avail = default_available()
-        avail[1] = 0.0  # the tensor-core variant is not a persistent-queue task
+        avail[1] = 0.0
         algos = MLPDispatcher(available=avail).choose(specs)
     else:
         algos = ModelDispatcher().choose(specs)

@@ -223,11 +223,15 @@ int ndconv_conv_fft_batch(const ndconv_problem *p, int64_t n, const void *const 
 
 /* Heterogeneous batch: n independent problems (any shapes, kernels, modes,
  * element types), each run by the algorithm variant algo[i] (ndconv_algo:
- * 0 direct, 1 FFT, 3..6 the FFT plan variants).  No counterpart in the reference (its calls are one instance
- * at a time).  data / kernel / out are HOST arrays of n device pointers,
- * bound at creation.  f32 instances become tasks of one persistent kernel
- * driven by a device-side work queue; others run as ordinary launches in
- * the same submission.  The plan owns all spectra (allocated once). */
+ * 0 direct, 1 FFT, 2 direct on the tensor cores (3xBF16; other element
+ * types run the FP32-family direct kernels), 3..6 the FFT plan variants).
+ * No counterpart in the reference (its calls are one instance at a time).
+ * data / kernel / out are HOST arrays of n device pointers, bound at
+ * creation.  f32 instances become tasks of one persistent kernel driven by a
+ * device-side work queue; others, and the tensor-core instances, run as
+ * ordinary launches on a side stream in the same submission.  The plan owns
+ * all spectra (allocated once); a tensor-core instance allocates its bf16
+ * planes stream-ordered on each run. */
 int ndconv_batch_create(const ndconv_problem *problems, int64_t n, const int32_t *algo,
                         const void *const *data, const void *const *kernel, void *const *out,
                         ndconv_batch_plan **plan);

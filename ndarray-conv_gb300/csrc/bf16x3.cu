@@ -740,6 +740,9 @@ bool applies(const Plan3 &P) {
 }
 
 }  // namespace bf16x3
+
+bool bf16x3_applies(const Plan3 &P) { return bf16x3::applies(P); }
+
 }  // namespace ndconv
 
 using namespace ndconv;

@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(256) persistent_kernel(const Task *__restrict_
 
 // work estimate of one instance (for ordering direct tiles, longest first)
 struct HostInst {
-    int algo;        // 0 direct, 1 FFT
+    int algo;        // 0 direct, 1 FFT, 2 direct on the tensor cores (3xBF16, an ordinary launch)
     int fv;          // FFT plan variant (FftVariant)
     int standalone;  // runs as ordinary launches before the persistent kernel
     int fold;        // f32 direct instance in the axis-folding form, inside the queue
@@ -206,6 +206,7 @@ struct HostInst {
     size_t ws_off;   // workspace offset: spectra (FFT) or folded weights (direct)
     size_t ws_bytes; // direct: folded-form scratch (0: none)
     FftConvPlan<float> cp;
+    ndconv_problem prob;  // the instance's descriptor (tensor-core instances)
 };
 
 }  // namespace batch
@@ -367,9 +368,9 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
     for (int64_t i = 0; i < n; i++) {
         HostInst &h = B->inst[(size_t)i];
         const int32_t a = algo ? algo[i] : NDCONV_ALGO_FFT;
-        if (a < 0 || a >= NDCONV_ALGO_COUNT || a == NDCONV_ALGO_DIRECT_BF16X3)
-            return fail(ndconv_fail(NDCONV_ERR_INVALID, "algo must be 0 (direct), 1 (FFT) or 3..6 (FFT variants)"));
-        h.algo = (a == NDCONV_ALGO_DIRECT) ? 0 : 1;
+        if (a < 0 || a >= NDCONV_ALGO_COUNT)
+            return fail(ndconv_fail(NDCONV_ERR_INVALID, "algo must be 0 (direct), 1 (FFT), 2 (direct, 3xBF16) or 3..6 (FFT variants)"));
+        h.algo = (a == NDCONV_ALGO_DIRECT || a == NDCONV_ALGO_DIRECT_BF16X3) ? 0 : 1;
         h.fv = (a == NDCONV_ALGO_FFT_ND) ? FFTV_ND : (a == NDCONV_ALGO_FFT_RS) ? FFTV_RS
              : (a == NDCONV_ALGO_FFT_ND_POW2) ? FFTV_ND_POW2 : (a == NDCONV_ALGO_FFT_RS_POW2) ? FFTV_RS_POW2 : FFTV_AUTO;
         int s = plan_problem(&probs[i], h.algo, &h.P);
@@ -390,6 +391,14 @@ int create(const ndconv_problem *probs, int64_t n, const int32_t *algo, const vo
         h.fold = 0;
         h.ws_off = 0;
         h.ws_bytes = 0;
+        h.prob = probs[i];
+        if (a == NDCONV_ALGO_DIRECT_BF16X3 && bf16x3_applies(h.P)) {
+            // the tensor-core kernel is persistent over all SMs itself: an
+            // ordinary launch beside the queue (it allocates its own planes)
+            h.algo = 2;
+            h.standalone = 1;
+            continue;
+        }
         if (h.algo == 1) {
             // transforms that do not fit one CTA's shared memory: the same
             // convolution by the direct kernels (as ndconv_conv_fft does)
@@ -707,6 +716,10 @@ int run_standalone(ndconv_batch_plan *B, cudaStream_t st) {
         if (!h.standalone) continue;
         unsigned char *scr = static_cast<unsigned char *>(B->ws) + h.ws_off;
         int s = NDCONV_OK;
+        if (h.algo == 2) {
+            if ((s = ndconv_conv_bf16x3(&h.prob, h.x, h.k, h.y, st))) return s;
+            continue;
+        }
         if (h.algo == 0) {
             cudaError_t e = cudaSuccess;
             void *ds = h.ws_bytes ? scr : nullptr;
@@ -823,6 +836,11 @@ extern "C" int ndconv_batch_run_plain(ndconv_batch_plan *B, void *stream) {
     cudaStream_t st = (cudaStream_t)stream;
     for (auto &h : B->inst) {
         unsigned char *scr = static_cast<unsigned char *>(B->ws) + h.ws_off;
+        if (h.algo == 2) {
+            const int s = ndconv_conv_bf16x3(&h.prob, h.x, h.k, h.y, st);
+            if (s) return s;
+            continue;
+        }
         if (h.algo == 0) {
             cudaError_t e = cudaSuccess;
             switch (h.P.dtype) {

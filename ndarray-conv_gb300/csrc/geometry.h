@@ -44,6 +44,9 @@ int plan_problem(const ndconv_problem *p, int algo, Plan3 *out);
 inline bool single_call_int(int dtype) { return dtype >= NDCONV_I64; }
 inline bool integer_dtype(int dtype) { return dtype == NDCONV_I32 || dtype >= NDCONV_I64; }
 
+// Whether the 3xBF16 tensor-core path takes the problem (bf16x3.cu).
+bool bf16x3_applies(const Plan3 &P);
+
 // ConvExt::conv for u8 / i8 / u16 / i16 (narrow_int.cu).
 int conv_narrow_int(const Plan3 &P, const void *data, const void *kernel, void *out, cudaStream_t st);
 

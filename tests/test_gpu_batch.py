@@ -108,3 +108,52 @@ def test_host_batch_equals_device_calls(algo, dt):
     for i in range(n):
         ref = f(xs[i].cuda(), with_dilation(ks[i].cuda(), 2), mode, pm).cpu()
         assert torch.equal(ys[i], ref), i
+
+
+def test_batch_tensor_core_instances():
+    """Instances sent to the tensor cores (algo 2) run beside the queue and
+    give exactly what ndconv_conv_algo(NDCONV_ALGO_DIRECT_BF16X3) gives; an
+    f64 instance given algo 2 runs the direct kernels."""
+    import torch
+    from ndconv import _abi, BorderType, ConvMode, PaddingMode
+    from ndconv.batch import BatchPlan
+    specs, xs, ks, kws, modes = _batch(24, 5, max_log2=14, kmax=31)
+    algos = [2 if (s.rank >= 2 and i % 2 == 0) else (i % 2) for i, s in enumerate(specs)]
+    g = torch.Generator(device="cuda").manual_seed(5)
+    xs = list(xs) + [torch.rand((40, 60), generator=g, device="cuda", dtype=torch.float64),
+                     torch.rand((70, 90), generator=g, device="cuda")]
+    k64, k32 = (torch.rand((5, 7), generator=g, device="cuda", dtype=torch.float64),
+                torch.rand((15, 17), generator=g, device="cuda"))
+    kws = list(kws) + [with_dilation(k64, 1), with_dilation(k32, [1, 2])]
+    ks = list(ks) + [k64, k32]
+    modes = list(modes) + [(ConvMode.Same, PaddingMode.Reflect),
+                           (ConvMode.Same, PaddingMode.Custom([BorderType.Circular, BorderType.Replicate]))]
+    algos += [2, 2]
+    assert sum(a == 2 for a in algos) >= 3
+    plan = BatchPlan(modes, xs, kws, algos=algos)
+    refs = []
+    for i in range(len(xs)):
+        if algos[i] == 2 and xs[i].dtype == torch.float32:
+            refs.append(ndconv.conv_algo(xs[i], kws[i], *modes[i], _abi.ALGO_DIRECT_BF16X3))
+        elif algos[i] in (0, 2):
+            refs.append(ndconv.conv(xs[i], kws[i], *modes[i]))
+        else:
+            refs.append(ndconv.conv_fft(xs[i], kws[i], *modes[i]))
+    for form in ("queue", "graph", "graph2", "plain"):
+        for y in plan.outs:
+            y.fill_(float("nan"))
+        if form == "plain":
+            plan.run_plain()
+        else:
+            plan.run(graph=form != "queue")
+        plan.check()
+        torch.cuda.synchronize()
+        for i in range(len(xs)):
+            assert torch.equal(plan.outs[i], refs[i]), (form, i, algos[i])
+    # the last instance (tensor cores, dilation, mixed borders) against the f64 oracle
+    x, k = xs[-1].cpu().numpy(), ks[-1].cpu().numpy()
+    p = problem(F64, x, with_dilation(k, [1, 2]), *modes[-1])
+    st, y64 = O.conv(p, x.astype(np.float64), k.astype(np.float64))
+    assert st == 0
+    assert normwise_err(plan.outs[-1].cpu().numpy(), y64) <= 1e-5
+    plan.close()
