@@ -18,6 +18,8 @@ The default line also carries, in `config`:
   uneven_batch  the uneven batch (4096 instances, one persistent launch +
                 CUDA graph, dispatcher-picked variants) against the plain
                 drop-in (per-instance calls with the library's default picks)
+  direct_tensor_cores  the same 64 instances through the batched 3xBF16
+                tensor-core direct path (one persistent launch)
   variants      the 1-D and 3-D cases (and the 3-D complex copy, and a 2-D
                 31 x 31 kernel) through direct FP32, 3xBF16 tensor cores
                 and FFT: device time per call and error against f64
@@ -532,6 +534,69 @@ def _variant_case(desc, xs, ksh, mode_n, pad_n, dt, variants, reps):
     return res
 
 
+def measure_c2_tensor(args, world, rank, local_rank, dist):
+    """The headline's B instances through the batched 3xBF16 tensor-core
+    direct path (ndconv_conv_bf16x3_batch, one persistent launch):
+    device-resident time per step, the FP32-equivalent rate 2 |y| taps / t
+    and the split-product bf16 rate (three products per tap) against the
+    measured bf16 peak, and the f64-oracle error of instance 0."""
+    import torch
+    mode, pm, ndconv = problem_args()
+    from ndconv import _abi, build_problem, with_dilation
+    L = _abi.lib()
+    B = args.batch
+    xs_np, ks_np = c2_inputs(B, SEED_C2 + rank)
+    xs = [torch.from_numpy(a).cuda() for a in xs_np]
+    ks = [torch.from_numpy(a).cuda() for a in ks_np]
+    p = build_problem(_abi.F32, SHAPE_X, with_dilation(ks[0], DIL), mode, pm)
+    osh = (ctypes.c_int64 * 3)()
+    assert L.ndconv_output_shape(ctypes.byref(p), 0, osh) == 0, _abi.last_error()
+    out_shape = (osh[0], osh[1])
+    ys = [torch.empty(out_shape, device="cuda") for _ in range(B)]
+    P_X, P_K, P_Y = [torch.tensor([t.data_ptr() for t in ts], dtype=torch.int64, device="cuda") for ts in (xs, ks, ys)]
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def step():
+        s = L.ndconv_conv_bf16x3_batch(ctypes.byref(p), B, ctypes.c_void_p(P_X.data_ptr()),
+                                       ctypes.c_void_p(P_K.data_ptr()), ctypes.c_void_p(P_Y.data_ptr()), sp)
+        if s:
+            raise RuntimeError(_abi.last_error())
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        e0.record()
+        for _ in range(args.steps):
+            step()
+        e1.record()
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    from oracle import oracle as O
+    p64 = build_problem(_abi.F64, SHAPE_X, with_dilation(ks_np[0], DIL), mode, pm)
+    stt, y64 = O.conv(p64, xs_np[0].astype(np.float64), ks_np[0].astype(np.float64))
+    err = float(np.linalg.norm(ys[0].cpu().numpy().astype(np.float64) - y64) / np.linalg.norm(y64)) if stt == 0 else None
+    flops = 2.0 * float(np.prod(out_shape)) * float(np.prod(SHAPE_K)) * B
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            bf16_peak = float(json.load(f)["bf16_tflops"])
+        peak_kind = "measured"
+    except Exception:
+        bf16_peak, peak_kind = 1900.0, "fallback"
+    split_tflops = 3.0 * flops / (ms * 1e-3) / 1e12
+    return {"workload": WORKLOAD_C2.format(B=B, what="conv on the tensor cores (3xBF16 split products)",
+                                           form="batched (ndconv_conv_bf16x3_batch)"),
+            "gbs": algorithmic_bytes(out_shape) * B * world / (ms * 1e-3) / 1e9, "ms_per_step": ms,
+            "fp32_equiv_tflops": flops / (ms * 1e-3) / 1e12,
+            "bf16_split_product_tflops": split_tflops,
+            "bf16_peak_tflops": bf16_peak, "bf16_peak_source": f"MEASURED_PEAKS.json bf16_tflops ({peak_kind})",
+            "useful_bf16_frac": split_tflops / bf16_peak,
+            "normwise_err": err, "clocks": clk.summary()}
+
+
 def measure_c2(args, algo, form, world, rank, local_rank, dist):
     """The 2-D case over B instances: conv_fft (algo 1) or conv (algo 0),
     batched or one call per instance; device-resident, plain per-instance
@@ -717,9 +782,13 @@ def main():
             return bench_uneven(args, world, rank, local_rank, dist)
         algo = 1 if args.algo == "fft" else 0
         r = measure_c2(args, algo, args.form, world, rank, local_rank, dist)
-        extra_direct = extra_uneven = extra_variants = None
+        extra_direct = extra_uneven = extra_variants = extra_tensor = None
         if not args.no_extra and algo == 1 and args.form == "batched":
             extra_direct = measure_c2(args, 0, "batched", world, rank, local_rank, dist)
+            try:
+                extra_tensor = measure_c2_tensor(args, world, rank, local_rank, dist)
+            except Exception as ex:  # the line still prints; the block says why it has no figures
+                extra_tensor = {"error": f"{type(ex).__name__}: {ex}"[:200]}
             extra_uneven = measure_uneven(args, world, rank, local_rank, dist)
             if rank == 0:
                 extra_variants = measure_variants()
@@ -758,6 +827,8 @@ def main():
             config["uneven_batch"] = uneven_summary(extra_uneven, world)
         if extra_variants:
             config["variants"] = extra_variants
+        if extra_tensor:
+            config["direct_tensor_cores"] = extra_tensor
         line = {
             "metric": METRIC,
             "value": gbs(r["ms"]), "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,

@@ -204,6 +204,17 @@ int ndconv_conv_batch_host(const ndconv_problem *p, int32_t algo, int64_t n, con
  * expected) leaves NaN in the affected output tile and is recorded in a
  * per-device word that ndconv_bf16x3_status reports. */
 int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, const void *kernel, void *out, void *stream);
+/* ndconv_conv_bf16x3 over n instances of one geometry (shapes, dilation,
+ * modes) in one persistent launch: data / kernel / out are DEVICE arrays of n
+ * device pointers (as ndconv_conv_batch).  The padded bf16 planes of all
+ * instances are built first (stream-ordered workspace of ~4 bytes per
+ * padded sample and instance), then every CTA takes tiles of any instance,
+ * so small instances keep the tensor pipeline full.  Each instance's
+ * result equals its ndconv_conv_bf16x3 call bit for bit.  A non-finite
+ * value in any instance sends every instance through the FP32 loop.  No
+ * reference counterpart (the crate convolves one array per call). */
+int ndconv_conv_bf16x3_batch(const ndconv_problem *p, int64_t n, const void *const *data,
+                             const void *const *kernel, void *const *out, void *stream);
 /* Synchronises stream, then reports (NDCONV_ERR_TIMEOUT) and clears the
  * timeouts of every 3xBF16 launch on the current device since the last
  * call; NDCONV_OK when there were none.  No reference counterpart. */

@@ -84,9 +84,17 @@ struct Params {
     uint32_t idesc;
     float *y;
     int64_t ys0, ys1;
-    int *status;  // bit 0: non-finite input seen; bit 1: a wait ran out
+    int *status;  // bit 0: non-finite input seen (any instance); bit 1: a wait ran out
     DirectParams<float> dp;  // FP32 fallback
     const float *x, *k;
+    // batches of instances sharing the geometry: device arrays of their
+    // pointers (null for one instance: x, k, y above); tiles per instance,
+    // padded planes per instance (plane index of instance i: i P0 + ...),
+    // Toeplitz rows per instance
+    const float *const *xs;
+    const float *const *ks;
+    float *const *ys;
+    int64_t tiles_inst, P0, Rt;
 };
 
 // ---- PTX wrappers --------------------------------------------------------
@@ -186,18 +194,22 @@ __device__ __forceinline__ void tmem_ld_wait(uint32_t *r) {
 }
 
 // ---- pre-passes -----------------------------------------------------------
-// Padded data planes [P0][P1][W] (hi, lo); zero beyond the padded extent.
-// A thread converts 8 consecutive samples of a row and stores them as
-// 16-byte vectors (W is a multiple of 8).
-__global__ void __launch_bounds__(256) split_data_kernel(const float *__restrict__ x, Geom3<float> g, int64_t W,
+// Padded data planes [n][P0][P1][W] (hi, lo) of n instances (xs: device
+// array of their data pointers, or null for the one instance x); zero beyond
+// the padded extent.  A thread converts 8 consecutive samples of a row and
+// stores them as 16-byte vectors (W is a multiple of 8).
+__global__ void __launch_bounds__(256) split_data_kernel(const float *__restrict__ x, const float *const *xs,
+                                                         int64_t n, Geom3<float> g, int64_t W,
                                                          __nv_bfloat16 *__restrict__ hi,
                                                          __nv_bfloat16 *__restrict__ lo, int *status) {
     const AxisGeom &A2 = g.ax[2];
-    const int64_t cw = W / 8, total = g.ax[0].L * g.ax[1].L * cw;
+    const int64_t cw = W / 8, rows = g.ax[0].L * g.ax[1].L, total = n * rows * cw;
     bool bad = false;
     for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total;
          u += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t row = u / cw, c0 = (u - row * cw) * 8;
+        const int64_t grow = u / cw, c0 = (u - grow * cw) * 8;  // row over all instances
+        const int64_t inst = grow / rows, row = grow - inst * rows;
+        const float *xi = xs ? xs[inst] : x;
         const int64_t i1 = row % g.ax[1].L, i0 = row / g.ax[1].L;
         const int64_t m0 = axis_map(g.ax[0], i0), m1 = axis_map(g.ax[1], i1);
         uint32_t h[4], l[4];
@@ -207,7 +219,7 @@ __global__ void __launch_bounds__(256) split_data_kernel(const float *__restrict
 #pragma unroll
             for (int q = 0; q < 2; q++) {
                 const int64_t i2 = c0 + 2 * e + q;
-                v[q] = i2 < A2.L ? resolve_padded<float>(x, g, m0, m1, axis_map(A2, i2)) : 0.f;
+                v[q] = i2 < A2.L ? resolve_padded<float>(xi, g, m0, m1, axis_map(A2, i2)) : 0.f;
                 if (!isfinite(v[q])) bad = true;
             }
             const __nv_bfloat162 hh = __floats2bfloat162_rn(v[0], v[1]);
@@ -216,26 +228,28 @@ __global__ void __launch_bounds__(256) split_data_kernel(const float *__restrict
             h[e] = *reinterpret_cast<const uint32_t *>(&hh);
             l[e] = *reinterpret_cast<const uint32_t *>(&ll);
         }
-        *reinterpret_cast<uint4 *>(hi + row * W + c0) = make_uint4(h[0], h[1], h[2], h[3]);
-        *reinterpret_cast<uint4 *>(lo + row * W + c0) = make_uint4(l[0], l[1], l[2], l[3]);
+        *reinterpret_cast<uint4 *>(hi + grow * W + c0) = make_uint4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<uint4 *>(lo + grow * W + c0) = make_uint4(l[0], l[1], l[2], l[3]);
     }
     if (bad) atomicOr(status, 1);
 }
 
-// Toeplitz bands [K0][ngroups][G][BN][Cp] (hi, lo): row (kz, group, kl, b),
-// column c holds kf[kz][ky][tx] when ky = group G + kl < K1 and
-// c = b s2 + tx d2 (kf: the kernel in tap order, reversed for convolution);
-// zero elsewhere (the padding rows of the last group included).
-__global__ void toeplitz_kernel(const float *__restrict__ k, Geom3<float> g, int reverse, int G, int BN,
-                                int ngroups, int64_t Cp, __nv_bfloat16 *__restrict__ hi,
-                                __nv_bfloat16 *__restrict__ lo, int *status) {
+// Toeplitz bands [n][K0][ngroups][G][BN][Cp] (hi, lo): row (kz, group, kl, b)
+// of an instance, column c holds kf[kz][ky][tx] when ky = group G + kl < K1
+// and c = b s2 + tx d2 (kf: the kernel in tap order, reversed for
+// convolution); zero elsewhere (the padding rows of the last group included).
+__global__ void toeplitz_kernel(const float *__restrict__ k1, const float *const *ks, int64_t n, Geom3<float> g,
+                                int reverse, int G, int BN, int ngroups, int64_t Cp,
+                                __nv_bfloat16 *__restrict__ hi, __nv_bfloat16 *__restrict__ lo, int *status) {
     const AxisGeom &A0 = g.ax[0], &A1 = g.ax[1], &A2 = g.ax[2];
-    const int64_t total = A0.K * ngroups * G * BN * Cp;
+    const int64_t per = A0.K * ngroups * G * BN * Cp, total = n * per;
     bool bad = false;
     for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total;
          u += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t inst = u / per;
+        const float *k = ks ? ks[inst] : k1;
         const int64_t c = u % Cp;
-        int64_t r = u / Cp;
+        int64_t r = (u - inst * per) / Cp;
         const int64_t b = r % BN;
         r /= BN;
         const int64_t kl = r % G;
@@ -275,18 +289,22 @@ __device__ __forceinline__ void epi_sync() { asm volatile("barrier.cta.sync 2, 2
 __device__ __forceinline__ void grp0_sync() { asm volatile("barrier.cta.sync 3, 128;" ::: "memory"); }
 
 struct TileCoord {
-    int64_t oz, oy0, ox0;
+    int64_t inst, oz, oy0, ox0;
 };
 // (32-bit division: the host keeps the tile count below 2^31)
 template <int BN> __device__ __forceinline__ TileCoord tile_of(const Params &P, int64_t t) {
-    const uint32_t tt = (uint32_t)t, nct = (uint32_t)P.nct, nrt = (uint32_t)P.nrt;
+    const uint32_t ti = (uint32_t)P.tiles_inst;
+    const uint32_t inst = (uint32_t)t / ti;
+    const uint32_t tt = (uint32_t)t - inst * ti, nct = (uint32_t)P.nct, nrt = (uint32_t)P.nrt;
     const uint32_t r = tt / nct;
     TileCoord c;
+    c.inst = inst;
     c.ox0 = (int64_t)(tt - r * nct) * BN;
     c.oy0 = (int64_t)(r % nrt) * P.mvalid;
     c.oz = r / nrt;
     return c;
 }
+__device__ __forceinline__ float *out_of(const Params &P, int64_t inst) { return P.ys ? P.ys[inst] : P.y; }
 
 // Persistent and warp-specialised: CTA b takes tiles b, b + grid, ...; per
 // tile the kernel-row groups are work items.  Warp 8 (one lane) streams the
@@ -320,10 +338,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         // non-finite input somewhere: the FP32 direct loop for this CTA's tiles
         for (int64_t t = t0; t < P.ntiles; t += tstep) {
             const TileCoord c = tile_of<BN>(P, t);
+            const float *x = P.xs ? P.xs[c.inst] : P.x, *k = P.ks ? P.ks[c.inst] : P.k;
+            float *y = out_of(P, c.inst);
             for (int u = tid; u < P.mvalid * BN; u += kThreads) {
                 const int64_t oy = c.oy0 + u / BN, ox = c.ox0 + u % BN;
-                if (ox < P.out2 && oy < P.out1)
-                    direct_naive_one<float>(P.x, P.k, P.y, P.dp, (c.oz * P.out1 + oy) * P.out2 + ox);
+                if (ox < P.out2 && oy < P.out1) direct_naive_one<float>(x, k, y, P.dp, (c.oz * P.out1 + oy) * P.out2 + ox);
             }
         }
         return;
@@ -391,11 +410,11 @@ __global__ void __launch_bounds__(kThreads, 1)
                         const int kz = i / P.nchunk, ch = i % P.nchunk;
                         unsigned char *st = base + s * P.stage_bytes;
                         mbar_expect_tx(&full[s], P.stage_bytes);
-                        const int z = (int)(c.oz * P.s0 + (int64_t)kz * P.d0);
+                        const int z = (int)(c.inst * P.P0 + c.oz * P.s0 + (int64_t)kz * P.d0);
                         tma_3d(st, &tX_hi, xb + ch * KC, rb, z, &full[s]);
                         tma_3d(st + A_BYTES, &tX_lo, xb + ch * KC, rb, z, &full[s]);
                         if (!P.bres) {
-                            const int trow = (kz * P.ngroups + g) * P.N;
+                            const int trow = (int)(c.inst * P.Rt) + (kz * P.ngroups + g) * P.N;
                             tma_2d(st + 2 * A_BYTES, &tT_hi, ch * KC, trow, &full[s]);
                             tma_2d(st + 2 * A_BYTES + b_bytes, &tT_lo, ch * KC, trow, &full[s]);
                         }
@@ -591,7 +610,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (lane == 0) mbar_arrive(&tempty[buf]);
             }
             if (!stop && !eg && et < P.mvalid && c.oy0 + et < P.out1) {
-                float *yr = P.y + c.oz * P.ys0 + (c.oy0 + et) * P.ys1 + c.ox0;
+                float *yr = out_of(P, c.inst) + c.oz * P.ys0 + (c.oy0 + et) * P.ys1 + c.ox0;
                 if (c.ox0 + BN <= P.out2 && (reinterpret_cast<uintptr_t>(yr) & 15) == 0) {
 #pragma unroll
                     for (int q = 0; q < BN / 4; q++)
@@ -622,9 +641,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         for (int64_t t = t0; t < P.ntiles; t += tstep) {
             const TileCoord c = tile_of<BN>(P, t);
+            float *y = out_of(P, c.inst);
             for (int u = tid; u < P.mvalid * BN; u += kThreads) {
                 const int64_t oy = c.oy0 + u / BN, ox = c.ox0 + u % BN;
-                if (ox < P.out2 && oy < P.out1) P.y[c.oz * P.ys0 + oy * P.ys1 + ox] = __int_as_float(0x7fc00000);
+                if (ox < P.out2 && oy < P.out1) y[c.oz * P.ys0 + oy * P.ys1 + ox] = __int_as_float(0x7fc00000);
             }
         }
         __syncthreads();
@@ -748,31 +768,45 @@ bool bf16x3_applies(const Plan3 &P) { return bf16x3::applies(P); }
 using namespace ndconv;
 using namespace ndconv::bf16x3;
 
-extern "C" int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, const void *kernel, void *out,
-                                  void *stream) {
+namespace {
+// n instances of one geometry: pointers x / k / y for one instance, or
+// device arrays xs / ks / ys of n pointers each.  The padded planes and
+// Toeplitz bands of all instances live in one workspace; one persistent
+// launch covers every instance's tiles.
+int run_bf16x3(const ndconv_problem *p, int64_t n, const float *x, const float *k, float *y,
+               const float *const *xs, const float *const *ks, float *const *ys, cudaStream_t st) {
     Plan3 P;
     int s = plan_problem(p, 0, &P);
     if (s) return s;
-    if (!data || !kernel || !out) return ndconv_fail(NDCONV_ERR_INVALID, "null pointer");
     if (!applies(P)) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "3xBF16 path: f32 within the TMA index range only");
-    cudaStream_t st = (cudaStream_t)stream;
     const AxisGeom *A = P.ax;
     const Geom3<float> g = P.geom<float>();
-    const TilePlan T = plan_tiles(P);
+    TilePlan T = plan_tiles(P);
+    if (n > 1 && T.bres) {
+        // the resident Toeplitz tiles belong to one instance: stream them
+        T.bres = 0;
+        T.stage_bytes = 2 * A_BYTES + 2 * T.N * KC * 2;
+        T.stages = std::min(kMaxStages, (kSmemLimit - kSmemExtra) / T.stage_bytes);
+        T.b_off = T.stages * T.stage_bytes;
+        T.ring_bytes = T.b_off;
+        T.smem = T.ring_bytes + kSmemExtra;
+    }
     const int64_t Cp = (int64_t)T.nchunk * KC;                  // Toeplitz row pitch (elements)
     const int64_t W = std::max<int64_t>(KC, (A[2].L + 7) / 8 * 8);  // data row pitch (16-byte multiple)
-    const int64_t Rt = A[0].K * T.ngroups * T.N;                // Toeplitz rows
-    const size_t nX = (size_t)(A[0].L * A[1].L * W), nT = (size_t)(Rt * Cp);
+    const int64_t Rt = A[0].K * T.ngroups * T.N;                // Toeplitz rows per instance
+    const size_t nX = (size_t)(n * A[0].L * A[1].L * W), nT = (size_t)(n * Rt * Cp);
     const int64_t nrt = (A[1].out + T.mvalid - 1) / T.mvalid, nct = (A[2].out + T.BN - 1) / T.BN;
-    const int64_t ntiles = A[0].out * nrt * nct;
+    const int64_t tiles_inst = A[0].out * nrt * nct, ntiles = n * tiles_inst;
+    if (ntiles >= 0x7fffffff || n * A[0].L >= 0x7fffffff || n * Rt >= 0x7fffffff)
+        return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "batch beyond the 32-bit tile and TMA coordinate range");
     int dev = 0, nsm = 0;
     NDCONV_CUDA_OK(cudaGetDevice(&dev));
     NDCONV_CUDA_OK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    if (ntiles >= 0x7fffffff) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "too many tiles");
     const int64_t gx = std::min<int64_t>(ntiles, nsm);  // persistent: one CTA per SM
     unsigned char *ws = nullptr;
     const size_t bytes = 2 * sizeof(__nv_bfloat16) * (nX + nT) + 256;
-    NDCONV_CUDA_OK(cudaMallocAsync((void **)&ws, bytes, st));
+    cudaError_t e = cudaMallocAsync((void **)&ws, bytes, st);
+    if (e != cudaSuccess) return ndconv_fail(NDCONV_ERR_NO_MEMORY, cudaGetErrorString(e));
     __nv_bfloat16 *xh = reinterpret_cast<__nv_bfloat16 *>(ws), *xl = xh + nX, *th = xl + nX, *tl = th + nT;
     int *status = reinterpret_cast<int *>(tl + nT);
     status = reinterpret_cast<int *>((reinterpret_cast<uintptr_t>(status) + 15) & ~(uintptr_t)15);
@@ -782,10 +816,10 @@ extern "C" int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, con
     };
     CUtensorMap mXh, mXl, mTh, mTl;
     {
-        const cuuint64_t dX[3] = {(cuuint64_t)W, (cuuint64_t)A[1].L, (cuuint64_t)A[0].L};
+        const cuuint64_t dX[3] = {(cuuint64_t)W, (cuuint64_t)A[1].L, (cuuint64_t)(n * A[0].L)};
         const cuuint64_t sX[2] = {(cuuint64_t)W * 2, (cuuint64_t)(W * A[1].L * 2)};
         const cuuint32_t bX[3] = {KC, BM, 1};
-        const cuuint64_t dT[2] = {(cuuint64_t)Cp, (cuuint64_t)Rt};
+        const cuuint64_t dT[2] = {(cuuint64_t)Cp, (cuuint64_t)(n * Rt)};
         const cuuint64_t sT[1] = {(cuuint64_t)Cp * 2};
         const cuuint32_t bT[2] = {KC, (cuuint32_t)T.N};
         if ((s = make_map(&mXh, xh, 3, dX, sX, bX)) || (s = make_map(&mXl, xl, 3, dX, sX, bX)) ||
@@ -794,12 +828,11 @@ extern "C" int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, con
     }
     cudaMemsetAsync(status, 0, sizeof(int), st);
     {
-        const int64_t items = A[0].L * A[1].L * (W / 8);
+        const int64_t items = n * A[0].L * A[1].L * (W / 8);
         const unsigned nb = (unsigned)std::max<int64_t>(1, std::min<int64_t>(152 * 16, (items + 255) / 256));
-        split_data_kernel<<<nb, 256, 0, st>>>(static_cast<const float *>(data), g, W, xh, xl, status);
+        split_data_kernel<<<nb, 256, 0, st>>>(x, xs, n, g, W, xh, xl, status);
     }
-    toeplitz_kernel<<<152 * 4, 256, 0, st>>>(static_cast<const float *>(kernel), g, P.reverse, T.G, T.BN,
-                                             T.ngroups, Cp, th, tl, status);
+    toeplitz_kernel<<<152 * 4, 256, 0, st>>>(k, ks, n, g, P.reverse, T.G, T.BN, T.ngroups, Cp, th, tl, status);
     ndconv_count_launch(2);
     Params Q{};
     Q.out0 = A[0].out;
@@ -828,17 +861,23 @@ extern "C" int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, con
     Q.shfl_epi = (A[1].s == 1 && (T.G - 1) * A[1].d < 32) ? 1 : 0;
     Q.tmem_cols = T.N <= 32 ? 32 : T.N <= 64 ? 64 : T.N <= 128 ? 128 : 256;
     Q.idesc = idesc_bf16(BM, T.N);
-    Q.y = static_cast<float *>(out);
+    Q.y = y;
     Q.ys0 = A[1].out * A[2].out;
     Q.ys1 = A[2].out;
     Q.status = status;
     Q.dp = P.direct<float>();
-    Q.x = static_cast<const float *>(data);
-    Q.k = static_cast<const float *>(kernel);
+    Q.x = x;
+    Q.k = k;
+    Q.xs = xs;
+    Q.ks = ks;
+    Q.ys = ys;
+    Q.tiles_inst = tiles_inst;
+    Q.P0 = A[0].L;
+    Q.Rt = Rt;
     const void *fn = T.BN == 16   ? (const void *)conv_kernel<16>
                      : T.BN == 32 ? (const void *)conv_kernel<32>
                                   : (const void *)conv_kernel<64>;
-    cudaError_t e = ndconv_allow_smem(fn, T.smem);
+    e = ndconv_allow_smem(fn, T.smem);
     if (e != cudaSuccess) return fail(ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e)));
     const dim3 grid((unsigned)gx);
     if (T.BN == 16) conv_kernel<16><<<grid, kThreads, T.smem, st>>>(mXh, mXl, mTh, mTl, Q);
@@ -849,6 +888,31 @@ extern "C" int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, con
     cudaFreeAsync(ws, st);  // stream-ordered: after the launch has finished with it
     if (e != cudaSuccess) return ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e));
     return NDCONV_OK;
+}
+}  // namespace
+
+extern "C" int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, const void *kernel, void *out,
+                                  void *stream) {
+    if (!data || !kernel || !out) {
+        Plan3 P;
+        if (const int s = plan_problem(p, 0, &P)) return s;
+        return ndconv_fail(NDCONV_ERR_INVALID, "null pointer");
+    }
+    return run_bf16x3(p, 1, static_cast<const float *>(data), static_cast<const float *>(kernel),
+                      static_cast<float *>(out), nullptr, nullptr, nullptr, (cudaStream_t)stream);
+}
+
+// See include/ndconv.h.
+extern "C" int ndconv_conv_bf16x3_batch(const ndconv_problem *p, int64_t n, const void *const *data,
+                                        const void *const *kernel, void *const *out, void *stream) {
+    Plan3 P;
+    if (const int s = plan_problem(p, 0, &P)) return s;
+    if (n < 0) return ndconv_fail(NDCONV_ERR_INVALID, "negative batch size");
+    if (n == 0) return NDCONV_OK;
+    if (!data || !kernel || !out) return ndconv_fail(NDCONV_ERR_INVALID, "null pointer array");
+    return run_bf16x3(p, n, nullptr, nullptr, nullptr, reinterpret_cast<const float *const *>(data),
+                      reinterpret_cast<const float *const *>(kernel), reinterpret_cast<float *const *>(out),
+                      (cudaStream_t)stream);
 }
 
 // See include/ndconv.h.  Waits for the stream, then reads and clears the

@@ -216,7 +216,8 @@ def _run_batch(algo, datas, kernels, conv_mode, padding_mode, processor=None, st
         if tuple(x.shape) != tuple(xs[0].shape) or tuple(k.shape) != tuple(ks[0].shape) or x.dtype != xs[0].dtype:
             raise ValueError("batched instances must share shapes and element type")
     shape = (ctypes.c_int64 * 3)()
-    raise_for_status(L.ndconv_output_shape(ctypes.byref(p), algo, shape), p, algo)
+    base = 1 if algo == 1 else 0
+    raise_for_status(L.ndconv_output_shape(ctypes.byref(p), base, shape), p, base)
     ys = [torch.empty([shape[i] for i in range(p.rank)], dtype=xs[0].dtype, device=xs[0].device)
           for _ in xs]
     px, pk, py = _ptr_array(xs), _ptr_array(ks), _ptr_array(ys)
@@ -225,11 +226,14 @@ def _run_batch(algo, datas, kernels, conv_mode, padding_mode, processor=None, st
     if algo == 0:
         st = L.ndconv_conv_batch(ctypes.byref(p), n, ctypes.c_void_p(px.data_ptr()), ctypes.c_void_p(pk.data_ptr()),
                                  ctypes.c_void_p(py.data_ptr()), sp)
+    elif algo == _abi.ALGO_DIRECT_BF16X3:
+        st = L.ndconv_conv_bf16x3_batch(ctypes.byref(p), n, ctypes.c_void_p(px.data_ptr()),
+                                        ctypes.c_void_p(pk.data_ptr()), ctypes.c_void_p(py.data_ptr()), sp)
     else:
         h = processor._handle if processor is not None else None
         st = L.ndconv_conv_fft_batch(ctypes.byref(p), n, ctypes.c_void_p(px.data_ptr()),
                                      ctypes.c_void_p(pk.data_ptr()), ctypes.c_void_p(py.data_ptr()), h, sp)
-    raise_for_status(st, p, algo)
+    raise_for_status(st, p, base)
     torch.cuda.current_stream().synchronize() if stream is None else stream.synchronize()
     return ys
 
@@ -238,6 +242,12 @@ def conv_batch(datas, kernels, conv_mode, padding_mode, stream=None):
     """conv over many instances with one geometry (kernels may carry the
     same dilation / no_reverse)."""
     return _run_batch(0, datas, kernels, conv_mode, padding_mode, stream=stream)
+
+
+def conv_bf16x3_batch(datas, kernels, conv_mode, padding_mode, stream=None):
+    """conv over many f32 instances with one geometry on the tensor cores
+    (3xBF16 split products), one persistent launch for all of them."""
+    return _run_batch(_abi.ALGO_DIRECT_BF16X3, datas, kernels, conv_mode, padding_mode, stream=stream)
 
 
 def conv_fft_batch(datas, kernels, conv_mode, padding_mode, processor=None, stream=None):

@@ -123,6 +123,9 @@ extern "C" {
                                   proc_: *mut ndconv_fft_processor, stream: *mut c_void) -> i32;
     pub fn ndconv_conv_bf16x3(p: *const ndconv_problem, data: *const c_void, kernel: *const c_void,
                               out: *mut c_void, stream: *mut c_void) -> i32;
+    pub fn ndconv_conv_bf16x3_batch(p: *const ndconv_problem, n: i64, data: *const *const c_void,
+                                    kernel: *const *const c_void, out: *const *mut c_void,
+                                    stream: *mut c_void) -> i32;
     pub fn ndconv_bf16x3_status(stream: *mut c_void) -> i32;
     pub fn ndconv_conv_batch(p: *const ndconv_problem, n: i64, data: *const *const c_void,
                              kernel: *const *const c_void, out: *const *mut c_void, stream: *mut c_void) -> i32;

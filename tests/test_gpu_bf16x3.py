@@ -95,3 +95,44 @@ def test_bf16x3_unsupported():
         ndconv.conv_algo(x.astype(np.float64), np.ones((3, 3)), ConvMode.Same, PaddingMode.Zeros, BF)
     with pytest.raises(ndconv.ConvError):
         ndconv.conv_algo(x.astype(np.int32), np.ones((3, 3), np.int32), ConvMode.Same, PaddingMode.Zeros, BF)
+
+
+@pytest.mark.parametrize("shape,kshape,dil,mode,pm,n", [
+    ((60, 170), (9, 13), [1, 2], ConvMode.Same, PaddingMode.Custom([BorderType.Reflect, BorderType.Circular]), 5),
+    ((3, 40, 90), (2, 7, 11), 1, ConvMode.Same, PaddingMode.Zeros, 4),
+    ((150, 130), (21, 5), 1, ConvMode.Valid, PaddingMode.Zeros, 3),
+    ((40, 70), (3, 3), 1, ConvMode.Full, PaddingMode.Replicate, 7),
+])
+def test_bf16x3_batch_equals_single_calls(shape, kshape, dil, mode, pm, n):
+    """ndconv_conv_bf16x3_batch: each instance bit for bit its single call,
+    and within 1e-5 of the f64 oracle."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(sum(shape) + n)
+    xs = [torch.rand(shape, generator=g, device="cuda") - 0.5 for _ in range(n)]
+    ks = [torch.rand(kshape, generator=g, device="cuda") - 0.5 for _ in range(n)]
+    ys = ndconv.conv_bf16x3_batch(xs, [with_dilation(k, dil) for k in ks], mode, pm)
+    for i in range(n):
+        y1 = ndconv.conv_algo(xs[i], with_dilation(ks[i], dil), mode, pm, BF)
+        assert torch.equal(ys[i], y1), i
+    i = n - 1
+    y64 = _oracle64(xs[i].cpu().numpy(), with_dilation(ks[i].cpu().numpy(), dil), mode, pm)
+    assert normwise_err(ys[i].cpu().numpy(), y64) <= TOL32
+
+
+def test_bf16x3_batch_nonfinite_instance():
+    """A non-finite value in one instance: every instance through the FP32
+    loop, with the reference's NaN pattern where the values are not finite."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(11)
+    xs = [torch.rand((20, 100), generator=g, device="cuda") for _ in range(3)]
+    ks = [torch.rand((5, 9), generator=g, device="cuda") for _ in range(3)]
+    xs[1][4, 17] = float("nan")
+    mode, pm = ConvMode.Same, PaddingMode.Zeros
+    ys = ndconv.conv_bf16x3_batch(xs, ks, mode, pm)
+    for i in range(3):
+        x, k = xs[i].cpu().numpy(), ks[i].cpu().numpy()
+        st, y64 = O.conv(problem(F64, x, k, mode, pm), x.astype(np.float64), k.astype(np.float64))
+        y = ys[i].cpu().numpy()
+        assert np.array_equal(np.isnan(y), np.isnan(y64))
+        fin = np.isfinite(y64)
+        assert np.allclose(y[fin], y64[fin], rtol=1e-5, atol=1e-5)
