@@ -327,16 +327,20 @@ __global__ void __launch_bounds__(kThreads, 1)
     uint64_t *tempty = tfull + 2;
     uint64_t *mdone = tempty + 2;
     uint64_t *bfull = mdone + 1;  // resident Toeplitz tiles loaded
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bfull + 1);
+    uint64_t *bfree = bfull + 1;  // resident Toeplitz tiles no longer read
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bfree + 1);
     int *bad = reinterpret_cast<int *>(tmem_slot + 1);     // some wait ran out
     int *issued_out = bad + 1;                              // the producer's stage count
     int *b_issued = issued_out + 1;                         // the producer's resident loads
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int64_t t0 = blockIdx.x, tstep = gridDim.x;
+    // CTA b takes the contiguous tiles [t0, t1) (tiles are instance-major, so
+    // a CTA meets few instances and reloads resident Toeplitz tiles rarely)
+    const int64_t per_cta = (P.ntiles + gridDim.x - 1) / gridDim.x;
+    const int64_t t0 = (int64_t)blockIdx.x * per_cta, t1 = min(P.ntiles, t0 + per_cta);
 
     if (*reinterpret_cast<volatile int *>(P.status) & 1) {
         // non-finite input somewhere: the FP32 direct loop for this CTA's tiles
-        for (int64_t t = t0; t < P.ntiles; t += tstep) {
+        for (int64_t t = t0; t < t1; t++) {
             const TileCoord c = tile_of<BN>(P, t);
             const float *x = P.xs ? P.xs[c.inst] : P.x, *k = P.ks ? P.ks[c.inst] : P.k;
             float *y = out_of(P, c.inst);
@@ -359,6 +363,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         mbar_init(mdone, 1);
         mbar_init(bfull, 1);
+        mbar_init(bfree, 1);
         *bad = 0;
         *issued_out = 0;
         *b_issued = 0;
@@ -380,24 +385,33 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (warp == 8) {
         if (lane == 0) {
             // producer: data boxes (shared by a group's kernel rows) and the
-            // Toeplitz tiles -- in each stage, or loaded once and kept resident
+            // Toeplitz tiles -- in each stage, or kept resident per instance
             // when the kernel is a single row group whose tiles fit
             const int b_bytes = P.N * KC * 2;
-            int it = 0;
+            int it = 0, bl = 0;
+            int64_t cur = -1;  // instance whose Toeplitz tiles are resident
             bool ok = true;
-            if (P.bres) {
-                mbar_expect_tx(bfull, per_group * 2 * b_bytes);
-                for (int i = 0; i < per_group; i++) {
-                    const int kz = i / P.nchunk, ch = i % P.nchunk;
-                    unsigned char *bs = base + P.b_off + i * 2 * b_bytes;
-                    tma_2d(bs, &tT_hi, ch * KC, kz * P.N, bfull);
-                    tma_2d(bs + b_bytes, &tT_lo, ch * KC, kz * P.N, bfull);
-                }
-                *b_issued = 1;
-            }
-            for (int64_t t = t0; t < P.ntiles && ok && !*vbad; t += tstep) {
+            for (int64_t t = t0; t < t1 && ok && !*vbad; t++) {
                 const TileCoord c = tile_of<BN>(P, t);
                 const int xb = (int)(c.ox0 * P.s2);
+                if (P.bres && c.inst != cur) {
+                    // (re)load the instance's tiles once the MMAs reading the
+                    // previous instance's have finished
+                    if (bl > 0 && !mbar_wait(bfree, (bl - 1) & 1)) {
+                        atomicOr(bad, 1);
+                        break;
+                    }
+                    mbar_expect_tx(bfull, per_group * 2 * b_bytes);
+                    for (int i = 0; i < per_group; i++) {
+                        const int kz = i / P.nchunk, ch = i % P.nchunk;
+                        unsigned char *bs = base + P.b_off + i * 2 * b_bytes;
+                        const int trow = (int)(c.inst * P.Rt) + kz * P.N;
+                        tma_2d(bs, &tT_hi, ch * KC, trow, bfull);
+                        tma_2d(bs + b_bytes, &tT_lo, ch * KC, trow, bfull);
+                    }
+                    cur = c.inst;
+                    *b_issued = ++bl;
+                }
                 for (int g = 0; g < P.ngroups && ok; g++) {
                     const int rb = (int)(c.oy0 * P.s1 + (int64_t)g * P.G * P.d1);
                     for (int i = 0; i < per_group; i++, it++) {
@@ -427,10 +441,23 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (lane == 0) {
             // MMA issuer: three split products per 16-wide K step, item j into buffer j % 2
             const int b_bytes = P.N * KC * 2;
-            int it = 0, j = 0;
-            bool ok = !P.bres || mbar_wait(bfull, 0);
-            if (!ok) atomicOr(bad, 1);
-            for (int64_t t = t0; t < P.ntiles && ok && !*vbad; t += tstep) {
+            int it = 0, j = 0, bl = 0;
+            int64_t cur = -1;
+            bool ok = true;
+            for (int64_t t = t0; t < t1 && ok && !*vbad; t++) {
+                if (P.bres) {
+                    const int64_t inst = (uint32_t)t / (uint32_t)P.tiles_inst;
+                    if (inst != cur) {
+                        // the previous instance's tiles are free once its MMAs finish
+                        if (bl > 0) mma_commit(bfree);
+                        if (!mbar_wait(bfull, bl & 1)) {
+                            atomicOr(bad, 1);
+                            break;
+                        }
+                        cur = inst;
+                        bl++;
+                    }
+                }
                 for (int g = 0; g < P.ngroups && ok; g++, j++) {
                     const int buf = j & 1;
                     if (j >= 2 && !mbar_wait(&tempty[buf], ((j >> 1) - 1) & 1)) {
@@ -481,7 +508,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         float acc[BN];
         int j = 0, rbuf = 0;
         bool stop = false;
-        for (int64_t t = t0; t < P.ntiles && !stop; t += tstep) {
+        for (int64_t t = t0; t < t1 && !stop; t++) {
             const TileCoord c = tile_of<BN>(P, t);
 #pragma unroll
             for (int q = 0; q < BN; q++) acc[q] = 0.f;
@@ -635,11 +662,11 @@ __global__ void __launch_bounds__(kThreads, 1)
             const int issued = *issued_out;
             for (int i = issued > P.stages ? issued - P.stages : 0; i < issued; i++)
                 mbar_wait(&full[i % P.stages], (i / P.stages) & 1);
-            if (*b_issued) mbar_wait(bfull, 0);
+            if (*b_issued > 0) mbar_wait(bfull, (*b_issued - 1) & 1);
             atomicOr(P.status, 2);
             atomicOr(&g_timeouts, 1);
         }
-        for (int64_t t = t0; t < P.ntiles; t += tstep) {
+        for (int64_t t = t0; t < t1; t++) {
             const TileCoord c = tile_of<BN>(P, t);
             float *y = out_of(P, c.inst);
             for (int u = tid; u < P.mvalid * BN; u += kThreads) {
@@ -781,16 +808,7 @@ int run_bf16x3(const ndconv_problem *p, int64_t n, const float *x, const float *
     if (!applies(P)) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "3xBF16 path: f32 within the TMA index range only");
     const AxisGeom *A = P.ax;
     const Geom3<float> g = P.geom<float>();
-    TilePlan T = plan_tiles(P);
-    if (n > 1 && T.bres) {
-        // the resident Toeplitz tiles belong to one instance: stream them
-        T.bres = 0;
-        T.stage_bytes = 2 * A_BYTES + 2 * T.N * KC * 2;
-        T.stages = std::min(kMaxStages, (kSmemLimit - kSmemExtra) / T.stage_bytes);
-        T.b_off = T.stages * T.stage_bytes;
-        T.ring_bytes = T.b_off;
-        T.smem = T.ring_bytes + kSmemExtra;
-    }
+    const TilePlan T = plan_tiles(P);
     const int64_t Cp = (int64_t)T.nchunk * KC;                  // Toeplitz row pitch (elements)
     const int64_t W = std::max<int64_t>(KC, (A[2].L + 7) / 8 * 8);  // data row pitch (16-byte multiple)
     const int64_t Rt = A[0].K * T.ngroups * T.N;                // Toeplitz rows per instance
