@@ -401,14 +401,15 @@ __global__ void __launch_bounds__(kThreads, 1)
                         atomicOr(bad, 1);
                         break;
                     }
-                    mbar_expect_tx(bfull, per_group * 2 * b_bytes);
-                    for (int i = 0; i < per_group; i++) {
-                        const int kz = i / P.nchunk, ch = i % P.nchunk;
-                        unsigned char *bs = base + P.b_off + i * 2 * b_bytes;
-                        const int trow = (int)(c.inst * P.Rt) + kz * P.N;
-                        tma_2d(bs, &tT_hi, ch * KC, trow, bfull);
-                        tma_2d(bs + b_bytes, &tT_lo, ch * KC, trow, bfull);
-                    }
+                    mbar_expect_tx(bfull, P.ngroups * per_group * 2 * b_bytes);
+                    for (int g = 0; g < P.ngroups; g++)
+                        for (int i = 0; i < per_group; i++) {
+                            const int kz = i / P.nchunk, ch = i % P.nchunk;
+                            unsigned char *bs = base + P.b_off + (g * per_group + i) * 2 * b_bytes;
+                            const int trow = (int)(c.inst * P.Rt) + (kz * P.ngroups + g) * P.N;
+                            tma_2d(bs, &tT_hi, ch * KC, trow, bfull);
+                            tma_2d(bs + b_bytes, &tT_lo, ch * KC, trow, bfull);
+                        }
                     cur = c.inst;
                     *b_issued = ++bl;
                 }
@@ -478,7 +479,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                         const uint32_t sa = smem_u32(base + s * P.stage_bytes);
                         const uint32_t a_hi = sa, a_lo = sa + A_BYTES;
                         const uint32_t b_hi =
-                            P.bres ? smem_u32(base + P.b_off + i * 2 * b_bytes) : sa + 2 * A_BYTES;
+                            P.bres ? smem_u32(base + P.b_off + (g * per_group + i) * 2 * b_bytes) : sa + 2 * A_BYTES;
                         const uint32_t b_lo = b_hi + b_bytes;
                         const int nk = (i % P.nchunk == P.nchunk - 1) ? P.klast : KC / 16;
                         for (int kk = 0; kk < nk; kk++) {
@@ -761,12 +762,12 @@ TilePlan plan_tiles(const Plan3 &P) {
     t.nchunk = (int)((t.Kpad + KC - 1) / KC);
     t.klast = (int)((t.Kpad - (int64_t)(t.nchunk - 1) * KC) / 16);
     t.mvalid = (int)((BM - 1 - (int64_t)(t.G - 1) * A[1].d) / A[1].s + 1);
-    // a kernel of one row group whose Toeplitz tiles (all plane taps and K
-    // chunks) take at most 96 KB keeps them in shared memory for the whole
-    // launch; the ring then streams only the data boxes
+    // a kernel whose Toeplitz tiles (every row group, plane tap and K chunk)
+    // fit beside a ring of at least two data stages keeps them in shared
+    // memory (per instance); the ring then streams only the data boxes
     const int bslot = 2 * t.N * KC * 2;
-    const int64_t bres_bytes = (int64_t)A[0].K * t.nchunk * bslot;
-    t.bres = t.ngroups == 1 && bres_bytes <= 96 * 1024;
+    const int64_t bres_bytes = (int64_t)t.ngroups * A[0].K * t.nchunk * bslot;
+    t.bres = bres_bytes + 2 * (2 * A_BYTES) <= kSmemLimit - kSmemExtra;
     t.stage_bytes = 2 * A_BYTES + (t.bres ? 0 : bslot);
     t.stages = std::min<int64_t>(kMaxStages, (kSmemLimit - kSmemExtra - (t.bres ? bres_bytes : 0)) / t.stage_bytes);
     t.b_off = t.stages * t.stage_bytes;
