@@ -212,19 +212,41 @@ __global__ void __launch_bounds__(256) split_data_kernel(const float *__restrict
         const float *xi = xs ? xs[inst] : x;
         const int64_t i1 = row % g.ax[1].L, i0 = row / g.ax[1].L;
         const int64_t m0 = axis_map(g.ax[0], i0), m1 = axis_map(g.ax[1], i1);
+        float v[8];
+        const int64_t j0 = c0 - A2.p0;  // input index of the first sample
+        if (m0 >= 0 && m1 >= 0 && A2.xs == 1 && j0 >= 0 && j0 + 8 <= A2.n) {
+            // interior samples of a contiguous row: plain (vector) loads
+            const float *src = xi + m0 * g.ax[0].xs + m1 * g.ax[1].xs + j0;
+            if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+                const float4 a = __ldg(reinterpret_cast<const float4 *>(src));
+                const float4 b = __ldg(reinterpret_cast<const float4 *>(src) + 1);
+                v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+                v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+            } else if ((reinterpret_cast<uintptr_t>(src) & 7) == 0) {
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const float2 a = __ldg(reinterpret_cast<const float2 *>(src) + q);
+                    v[2 * q] = a.x;
+                    v[2 * q + 1] = a.y;
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < 8; q++) v[q] = __ldg(src + q);
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const int64_t i2 = c0 + q;
+                v[q] = i2 < A2.L ? resolve_padded<float>(xi, g, m0, m1, axis_map(A2, i2)) : 0.f;
+            }
+        }
         uint32_t h[4], l[4];
 #pragma unroll
         for (int e = 0; e < 4; e++) {
-            float v[2];
-#pragma unroll
-            for (int q = 0; q < 2; q++) {
-                const int64_t i2 = c0 + 2 * e + q;
-                v[q] = i2 < A2.L ? resolve_padded<float>(xi, g, m0, m1, axis_map(A2, i2)) : 0.f;
-                if (!isfinite(v[q])) bad = true;
-            }
-            const __nv_bfloat162 hh = __floats2bfloat162_rn(v[0], v[1]);
+            if (!isfinite(v[2 * e]) || !isfinite(v[2 * e + 1])) bad = true;
+            const __nv_bfloat162 hh = __floats2bfloat162_rn(v[2 * e], v[2 * e + 1]);
             const float2 hf = __bfloat1622float2(hh);
-            const __nv_bfloat162 ll = __floats2bfloat162_rn(v[0] - hf.x, v[1] - hf.y);
+            const __nv_bfloat162 ll = __floats2bfloat162_rn(v[2 * e] - hf.x, v[2 * e + 1] - hf.y);
             h[e] = *reinterpret_cast<const uint32_t *>(&hh);
             l[e] = *reinterpret_cast<const uint32_t *>(&ll);
         }
