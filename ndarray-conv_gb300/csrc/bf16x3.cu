@@ -260,34 +260,37 @@ __global__ void __launch_bounds__(256) split_data_kernel(const float *__restrict
 // of an instance, column c holds kf[kz][ky][tx] when ky = group G + kl < K1
 // and c = b s2 + tx d2 (kf: the kernel in tap order, reversed for
 // convolution); zero elsewhere (the padding rows of the last group included).
+// One warp per band row (its coordinates decoded once), lanes along c.
 __global__ void toeplitz_kernel(const float *__restrict__ k1, const float *const *ks, int64_t n, Geom3<float> g,
                                 int reverse, int G, int BN, int ngroups, int64_t Cp,
                                 __nv_bfloat16 *__restrict__ hi, __nv_bfloat16 *__restrict__ lo, int *status) {
     const AxisGeom &A0 = g.ax[0], &A1 = g.ax[1], &A2 = g.ax[2];
-    const int64_t per = A0.K * ngroups * G * BN * Cp, total = n * per;
+    const int64_t per = A0.K * ngroups * G * BN, rows = n * per;
+    const int lane = threadIdx.x & 31;
+    const int64_t wstep = (int64_t)gridDim.x * (blockDim.x >> 5);
     bool bad = false;
-    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total;
-         u += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t inst = u / per;
-        const float *k = ks ? ks[inst] : k1;
-        const int64_t c = u % Cp;
-        int64_t r = (u - inst * per) / Cp;
+    for (int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < rows; row += wstep) {
+        const int64_t inst = row / per;
+        int64_t r = row - inst * per;
         const int64_t b = r % BN;
         r /= BN;
         const int64_t kl = r % G;
         r /= G;
         const int64_t ky = (r % ngroups) * G + kl, kz = r / ngroups;
-        float w = 0.f;
-        const int64_t off = c - b * A2.s;
-        if (ky < A1.K && off >= 0 && off % A2.d == 0 && off / A2.d < A2.K) {
-            const int64_t tx = off / A2.d;
-            w = k[tap_source(kz, A0.K, reverse) * A0.ks + tap_source(ky, A1.K, reverse) * A1.ks +
-                  tap_source(tx, A2.K, reverse) * A2.ks];
-            if (!isfinite(w)) bad = true;
+        const float *k = ks ? ks[inst] : k1;
+        const float *krow = ky < A1.K ? k + tap_source(kz, A0.K, reverse) * A0.ks + tap_source(ky, A1.K, reverse) * A1.ks
+                                      : nullptr;
+        for (int64_t c = lane; c < Cp; c += 32) {
+            float w = 0.f;
+            const int64_t off = c - b * A2.s;
+            if (krow && off >= 0 && off % A2.d == 0 && off / A2.d < A2.K) {
+                w = krow[tap_source(off / A2.d, A2.K, reverse) * A2.ks];
+                if (!isfinite(w)) bad = true;
+            }
+            const __nv_bfloat16 h = __float2bfloat16_rn(w);
+            hi[row * Cp + c] = h;
+            lo[row * Cp + c] = __float2bfloat16_rn(w - __bfloat162float(h));
         }
-        const __nv_bfloat16 h = __float2bfloat16_rn(w);
-        hi[u] = h;
-        lo[u] = __float2bfloat16_rn(w - __bfloat162float(h));
     }
     if (bad) atomicOr(status, 1);
 }
@@ -873,7 +876,11 @@ int run_bf16x3(const ndconv_problem *p, int64_t n, const float *x, const float *
         const unsigned nb = (unsigned)std::max<int64_t>(1, std::min<int64_t>(152 * 16, (items + 255) / 256));
         split_data_kernel<<<nb, 256, 0, st>>>(x, xs, n, g, W, xh, xl, status);
     }
-    toeplitz_kernel<<<152 * 4, 256, 0, st>>>(k, ks, n, g, P.reverse, T.G, T.BN, T.ngroups, Cp, th, tl, status);
+    {
+        const int64_t rows = n * Rt;  // one warp per band row, 8 warps per block
+        const unsigned nb = (unsigned)std::max<int64_t>(1, std::min<int64_t>(152 * 16, (rows + 7) / 8));
+        toeplitz_kernel<<<nb, 256, 0, st>>>(k, ks, n, g, P.reverse, T.G, T.BN, T.ngroups, Cp, th, tl, status);
+    }
     ndconv_count_launch(2);
     Params Q{};
     Q.out0 = A[0].out;
