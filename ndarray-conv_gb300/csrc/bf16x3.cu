@@ -507,11 +507,21 @@ __global__ void __launch_bounds__(kThreads, 1)
                             P.bres ? smem_u32(base + P.b_off + (g * per_group + i) * 2 * b_bytes) : sa + 2 * A_BYTES;
                         const uint32_t b_lo = b_hi + b_bytes;
                         const int nk = (i % P.nchunk == P.nchunk - 1) ? P.klast : KC / 16;
-                        for (int kk = 0; kk < nk; kk++) {
-                            const uint32_t o = kk * 32;  // 16 bf16 along the swizzled 128-byte row
-                            mma_bf16(d, sw128_desc(a_hi + o), sw128_desc(b_hi + o), P.idesc, (i | kk) != 0);
-                            mma_bf16(d, sw128_desc(a_hi + o), sw128_desc(b_lo + o), P.idesc, 1);
-                            mma_bf16(d, sw128_desc(a_lo + o), sw128_desc(b_hi + o), P.idesc, 1);
+                        // a K step of 16 bf16 moves 32 bytes along the swizzled
+                        // rows: 2 in the descriptors' start-address field
+                        const uint64_t dah = sw128_desc(a_hi), dal = sw128_desc(a_lo);
+                        const uint64_t dbh = sw128_desc(b_hi), dbl = sw128_desc(b_lo);
+                        auto kstep = [&](int kk) {
+                            const uint64_t o = (uint64_t)(2 * kk);
+                            mma_bf16(d, dah + o, dbh + o, P.idesc, (i | kk) != 0);
+                            mma_bf16(d, dah + o, dbl + o, P.idesc, 1);
+                            mma_bf16(d, dal + o, dbh + o, P.idesc, 1);
+                        };
+                        if (nk == KC / 16) {
+#pragma unroll
+                            for (int kk = 0; kk < KC / 16; kk++) kstep(kk);
+                        } else {
+                            for (int kk = 0; kk < nk; kk++) kstep(kk);
                         }
                         mma_commit(&empty[s]);  // stage reusable once these MMAs have read it
                     }
