@@ -27,14 +27,16 @@
 // Operands are K-major bf16 tiles of 64 elements per row (one 128-byte
 // swizzled row) staged by TMA from two pre-built planes in global memory:
 // the padded data (border map applied once, split into hi / lo) and the
-// Toeplitz bands.  One thread issues TMA, one issues tcgen05.mma, all four
-// warps drain TMEM with tcgen05.ld.  Every mbarrier wait is bounded; a
-// timeout (not expected) writes NaN to the tile's outputs, records the event
-// in a library-owned per-device word (read and cleared by
-// ndconv_bf16x3_status), waits (bounded) for the tile's TMA loads and MMAs
-// already in flight, and the CTA still releases TMEM.
+// Toeplitz bands.  The kernel is persistent (one CTA per SM over contiguous
+// tile ranges; batches of instances of one geometry share the launch) and
+// warp-specialised: one thread issues TMA, one issues tcgen05.mma into two
+// TMEM accumulators in turn, eight warps drain the other with tcgen05.ld.
+// Every mbarrier wait is bounded; a timeout (not expected) writes NaN to the
+// CTA's tiles, records the event in a library-owned per-device word (read
+// and cleared by ndconv_bf16x3_status), waits (bounded) for the TMA loads and
+// MMAs already in flight, and the CTA still releases TMEM.
 // Non-finite inputs (bit 0, found by the pre-pass) make every CTA compute its
-// tile with the FP32 direct loop instead, like the reference's sums.
+// tiles with the FP32 direct loop instead, like the reference's sums.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -78,7 +80,7 @@ struct Params {
     int64_t ntiles;      // out0 * nrt * nct
     int nchunk, klast;   // 64-wide K chunks per (group, kz); 16-wide steps in the last one
     int stages, stage_bytes, ring_bytes;  // ring_bytes includes the resident Toeplitz tiles
-    int bres, b_off;     // Toeplitz tiles resident per group (at byte b_off), or in each stage
+    int bres, b_off;     // Toeplitz tiles of all groups resident (at byte b_off), or in each stage
     int tmem_cols;
     int shfl_epi;        // epilogue by warp shuffles (unit middle stride, (G - 1) d1 < 32)
     uint32_t idesc;
@@ -411,7 +413,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (lane == 0) {
             // producer: data boxes (shared by a group's kernel rows) and the
             // Toeplitz tiles -- in each stage, or kept resident per instance
-            // when the kernel is a single row group whose tiles fit
+            // (every row group's) when they fit beside two data stages
             const int b_bytes = P.N * KC * 2;
             int it = 0, bl = 0;
             int64_t cur = -1;  // instance whose Toeplitz tiles are resident
