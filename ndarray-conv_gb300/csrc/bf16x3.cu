@@ -35,8 +35,8 @@
 // CTA's tiles, records the event in a library-owned per-device word (read
 // and cleared by ndconv_bf16x3_status), waits (bounded) for the TMA loads and
 // MMAs already in flight, and the CTA still releases TMEM.
-// Non-finite inputs (bit 0, found by the pre-pass) make every CTA compute its
-// tiles with the FP32 direct loop instead, like the reference's sums.
+// Non-finite inputs (flagged per block by the pre-pass) make every CTA compute
+// its tiles with the FP32 direct loop instead, like the reference's sums.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -86,7 +86,8 @@ struct Params {
     uint32_t idesc;
     float *y;
     int64_t ys0, ys1;
-    int *status;  // bit 0: non-finite input seen (any instance); bit 1: a wait ran out
+    const int *flags;  // per pre-pass block: a non-finite input seen (any instance)
+    int nflags;
     DirectParams<float> dp;  // FP32 fallback
     const float *x, *k;
     // batches of instances sharing the geometry: device arrays of their
@@ -200,15 +201,15 @@ __device__ __forceinline__ void tmem_ld_wait(uint32_t *r) {
 // array of their data pointers, or null for the one instance x); zero beyond
 // the padded extent.  A thread converts 8 consecutive samples of a row and
 // stores them as 16-byte vectors (W is a multiple of 8).
-__global__ void __launch_bounds__(256) split_data_kernel(const float *__restrict__ x, const float *const *xs,
-                                                         int64_t n, Geom3<float> g, int64_t W,
-                                                         __nv_bfloat16 *__restrict__ hi,
-                                                         __nv_bfloat16 *__restrict__ lo, int *status) {
+// (blocks bid of nblk of the pre-pass launch; returns whether this thread saw
+// a non-finite value)
+__device__ __forceinline__ bool split_part(const float *__restrict__ x, const float *const *xs, int64_t n,
+                                           const Geom3<float> &g, int64_t W, __nv_bfloat16 *__restrict__ hi,
+                                           __nv_bfloat16 *__restrict__ lo, int64_t bid, int64_t nblk) {
     const AxisGeom &A2 = g.ax[2];
     const int64_t cw = W / 8, rows = g.ax[0].L * g.ax[1].L, total = n * rows * cw;
     bool bad = false;
-    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total;
-         u += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t u = bid * blockDim.x + threadIdx.x; u < total; u += nblk * blockDim.x) {
         const int64_t grow = u / cw, c0 = (u - grow * cw) * 8;  // row over all instances
         const int64_t inst = grow / rows, row = grow - inst * rows;
         const float *xi = xs ? xs[inst] : x;
@@ -255,7 +256,7 @@ __global__ void __launch_bounds__(256) split_data_kernel(const float *__restrict
         *reinterpret_cast<uint4 *>(hi + grow * W + c0) = make_uint4(h[0], h[1], h[2], h[3]);
         *reinterpret_cast<uint4 *>(lo + grow * W + c0) = make_uint4(l[0], l[1], l[2], l[3]);
     }
-    if (bad) atomicOr(status, 1);
+    return bad;
 }
 
 // Toeplitz bands [n][K0][ngroups][G][BN][Cp] (hi, lo): row (kz, group, kl, b)
@@ -263,15 +264,16 @@ __global__ void __launch_bounds__(256) split_data_kernel(const float *__restrict
 // and c = b s2 + tx d2 (kf: the kernel in tap order, reversed for
 // convolution); zero elsewhere (the padding rows of the last group included).
 // One warp per band row (its coordinates decoded once), lanes along c.
-__global__ void toeplitz_kernel(const float *__restrict__ k1, const float *const *ks, int64_t n, Geom3<float> g,
-                                int reverse, int G, int BN, int ngroups, int64_t Cp,
-                                __nv_bfloat16 *__restrict__ hi, __nv_bfloat16 *__restrict__ lo, int *status) {
+__device__ __forceinline__ bool toeplitz_part(const float *__restrict__ k1, const float *const *ks, int64_t n,
+                                              const Geom3<float> &g, int reverse, int G, int BN, int ngroups,
+                                              int64_t Cp, __nv_bfloat16 *__restrict__ hi,
+                                              __nv_bfloat16 *__restrict__ lo, int64_t bid, int64_t nblk) {
     const AxisGeom &A0 = g.ax[0], &A1 = g.ax[1], &A2 = g.ax[2];
     const int64_t per = A0.K * ngroups * G * BN, rows = n * per;
     const int lane = threadIdx.x & 31;
-    const int64_t wstep = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t wstep = nblk * (blockDim.x >> 5);
     bool bad = false;
-    for (int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < rows; row += wstep) {
+    for (int64_t row = bid * (blockDim.x >> 5) + (threadIdx.x >> 5); row < rows; row += wstep) {
         const int64_t inst = row / per;
         int64_t r = row - inst * per;
         const int64_t b = r % BN;
@@ -294,7 +296,27 @@ __global__ void toeplitz_kernel(const float *__restrict__ k1, const float *const
             lo[row * Cp + c] = __float2bfloat16_rn(w - __bfloat162float(h));
         }
     }
-    if (bad) atomicOr(status, 1);
+    return bad;
+}
+
+// Both pre-passes in one launch: blocks [0, nbs) split the data, the rest
+// write the Toeplitz bands.  Every block stores whether it saw a non-finite
+// value in flags[blockIdx.x] (no zeroing needed before the launch).
+__global__ void __launch_bounds__(256) prepass_kernel(const float *__restrict__ x, const float *const *xs,
+                                                      const float *__restrict__ k1, const float *const *ks,
+                                                      int64_t n, Geom3<float> g, int64_t W, int reverse, int G,
+                                                      int BN, int ngroups, int64_t Cp, __nv_bfloat16 *xh,
+                                                      __nv_bfloat16 *xl, __nv_bfloat16 *th, __nv_bfloat16 *tl,
+                                                      int nbs, int *flags) {
+    const int b = blockIdx.x;
+    const bool bad = b < nbs ? split_part(x, xs, n, g, W, xh, xl, b, nbs)
+                             : toeplitz_part(k1, ks, n, g, reverse, G, BN, ngroups, Cp, th, tl, b - nbs,
+                                             (int64_t)gridDim.x - nbs);
+    const int any = __syncthreads_or(bad);
+    if (threadIdx.x == 0) flags[b] = any;
+    // the flag array is read as 16-byte vectors: block 0 zeroes its padding
+    if (b == 0 && threadIdx.x > 0 && threadIdx.x < 4 && (int)gridDim.x + (int)threadIdx.x - 1 < ((gridDim.x + 3) & ~3u))
+        flags[gridDim.x + threadIdx.x - 1] = 0;
 }
 
 // ---- main kernel ----------------------------------------------------------
@@ -365,7 +387,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int64_t per_cta = (P.ntiles + gridDim.x - 1) / gridDim.x;
     const int64_t t0 = (int64_t)blockIdx.x * per_cta, t1 = min(P.ntiles, t0 + per_cta);
 
-    if (*reinterpret_cast<volatile int *>(P.status) & 1) {
+    int nonfinite = 0;
+    for (int i = tid; 4 * i < P.nflags; i += kThreads) {
+        const int4 f = reinterpret_cast<const int4 *>(P.flags)[i];
+        nonfinite |= f.x | f.y | f.z | f.w;
+    }
+    if (__syncthreads_or(nonfinite)) {
         // non-finite input somewhere: the FP32 direct loop for this CTA's tiles
         for (int64_t t = t0; t < t1; t++) {
             const TileCoord c = tile_of<BN>(P, t);
@@ -701,7 +728,6 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int i = issued > P.stages ? issued - P.stages : 0; i < issued; i++)
                 mbar_wait(&full[i % P.stages], (i / P.stages) & 1);
             if (*b_issued > 0) mbar_wait(bfull, (*b_issued - 1) & 1);
-            atomicOr(P.status, 2);
             atomicOr(&g_timeouts, 1);
         }
         for (int64_t t = t0; t < t1; t++) {
@@ -860,12 +886,17 @@ int run_bf16x3(const ndconv_problem *p, int64_t n, const float *x, const float *
     NDCONV_CUDA_OK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     const int64_t gx = std::min<int64_t>(ntiles, nsm);  // persistent: one CTA per SM
     unsigned char *ws = nullptr;
-    const size_t bytes = 2 * sizeof(__nv_bfloat16) * (nX + nT) + 256;
+    // pre-pass blocks: data split, then Toeplitz rows (one warp each)
+    const int64_t items = n * A[0].L * A[1].L * (W / 8), trows = n * Rt;
+    const int nbs = (int)std::max<int64_t>(1, std::min<int64_t>(16 * nsm, (items + 255) / 256));
+    const int nbt = (int)std::max<int64_t>(1, std::min<int64_t>(16 * nsm, (trows + 7) / 8));
+    const int nflags = (nbs + nbt + 3) & ~3;  // padded to whole 16-byte vectors
+    const size_t bytes = 2 * sizeof(__nv_bfloat16) * (nX + nT) + sizeof(int) * (size_t)nflags + 256;
     cudaError_t e = cudaMallocAsync((void **)&ws, bytes, st);
     if (e != cudaSuccess) return ndconv_fail(NDCONV_ERR_NO_MEMORY, cudaGetErrorString(e));
     __nv_bfloat16 *xh = reinterpret_cast<__nv_bfloat16 *>(ws), *xl = xh + nX, *th = xl + nX, *tl = th + nT;
-    int *status = reinterpret_cast<int *>(tl + nT);
-    status = reinterpret_cast<int *>((reinterpret_cast<uintptr_t>(status) + 15) & ~(uintptr_t)15);
+    int *flags = reinterpret_cast<int *>(tl + nT);
+    flags = reinterpret_cast<int *>((reinterpret_cast<uintptr_t>(flags) + 15) & ~(uintptr_t)15);
     auto fail = [&](int code) {
         cudaFreeAsync(ws, st);
         return code;
@@ -882,18 +913,9 @@ int run_bf16x3(const ndconv_problem *p, int64_t n, const float *x, const float *
             (s = make_map(&mTh, th, 2, dT, sT, bT)) || (s = make_map(&mTl, tl, 2, dT, sT, bT)))
             return fail(s);
     }
-    cudaMemsetAsync(status, 0, sizeof(int), st);
-    {
-        const int64_t items = n * A[0].L * A[1].L * (W / 8);
-        const unsigned nb = (unsigned)std::max<int64_t>(1, std::min<int64_t>(152 * 16, (items + 255) / 256));
-        split_data_kernel<<<nb, 256, 0, st>>>(x, xs, n, g, W, xh, xl, status);
-    }
-    {
-        const int64_t rows = n * Rt;  // one warp per band row, 8 warps per block
-        const unsigned nb = (unsigned)std::max<int64_t>(1, std::min<int64_t>(152 * 16, (rows + 7) / 8));
-        toeplitz_kernel<<<nb, 256, 0, st>>>(k, ks, n, g, P.reverse, T.G, T.BN, T.ngroups, Cp, th, tl, status);
-    }
-    ndconv_count_launch(2);
+    prepass_kernel<<<nbs + nbt, 256, 0, st>>>(x, xs, k, ks, n, g, W, P.reverse, T.G, T.BN, T.ngroups, Cp, xh, xl, th,
+                                             tl, nbs, flags);
+    ndconv_count_launch();
     Params Q{};
     Q.out0 = A[0].out;
     Q.out1 = A[1].out;
@@ -924,7 +946,8 @@ int run_bf16x3(const ndconv_problem *p, int64_t n, const float *x, const float *
     Q.y = y;
     Q.ys0 = A[1].out * A[2].out;
     Q.ys1 = A[2].out;
-    Q.status = status;
+    Q.flags = flags;
+    Q.nflags = nflags;
     Q.dp = P.direct<float>();
     Q.x = x;
     Q.k = k;
