@@ -459,7 +459,7 @@ VARIANT_CASES = [
     ("c3", "3-D f32 x[10,100,200] * k[5,11,31], Same, Zeros", (10, 100, 200), (5, 11, 31), "Same", "Zeros", "f32",
      ["direct", "bf16x3", "fft"]),
     ("c3_complex", "3-D Complex<f32> x[10,100,200] * k[5,11,31] (re, im i.i.d. N(0,1)), Same, Zeros",
-     (10, 100, 200), (5, 11, 31), "Same", "Zeros", "c32", ["direct", "fft"]),
+     (10, 100, 200), (5, 11, 31), "Same", "Zeros", "c32", ["direct", "bf16x3", "fft"]),
     ("2d_k31x31", "2-D f32 x[1024,1024] * k[31,31], Same, Zeros (a dense kernel of >= 15 taps per axis)",
      (1024, 1024), (31, 31), "Same", "Zeros", "f32", ["direct", "bf16x3", "fft"]),
 ]

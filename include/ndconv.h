@@ -191,7 +191,9 @@ int ndconv_conv_batch_host(const ndconv_problem *p, int32_t algo, int64_t n, con
                            const void *const *kernel, void *const *out, ndconv_fft_processor *proc,
                            void *stream);
 
-/* ConvExt::conv for f32 on the tensor cores: 3xBF16 split products
+/* ConvExt::conv for f32 and Complex<f32> on the tensor cores (a complex
+ * problem runs as four real convolutions of the interleaved parts, combined
+ * as num-complex's product): 3xBF16 split products
  * (x k ~ xh kh + xh kl + xl kh) accumulated in f32, normwise error ~1e-6 vs
  * f64: row correlations of the padded data with groups of kernel rows on
  * the tensor cores, summed over each group's rows in the epilogue.  Any
@@ -212,7 +214,8 @@ int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, const void *ke
  * so small instances keep the tensor pipeline full.  Each instance's
  * result equals its ndconv_conv_bf16x3 call bit for bit.  A non-finite
  * value in any instance sends every instance through the FP32 loop.  No
- * reference counterpart (the crate convolves one array per call). */
+ * reference counterpart (the crate convolves one array per call).  f32
+ * only (NDCONV_ERR_UNSUPPORTED for other element types). */
 int ndconv_conv_bf16x3_batch(const ndconv_problem *p, int64_t n, const void *const *data,
                              const void *const *kernel, void *const *out, void *stream);
 /* Synchronises stream, then reports (NDCONV_ERR_TIMEOUT) and clears the

@@ -749,6 +749,25 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
 }
 
+// ---- Complex<f32> as four real convolutions -------------------------------
+// Device arrays of the four real instances' pointers (written by a kernel so
+// that the call stays capturable into a CUDA graph).
+__global__ void set_ptrs_kernel(const float **xs, const float **ks, float **ys, const float *x0, const float *x1,
+                                const float *x2, const float *x3, const float *k0, const float *k1, const float *k2,
+                                const float *k3, float *y0, float *y1, float *y2, float *y3) {
+    xs[0] = x0; xs[1] = x1; xs[2] = x2; xs[3] = x3;
+    ks[0] = k0; ks[1] = k1; ks[2] = k2; ks[3] = k3;
+    ys[0] = y0; ys[1] = y1; ys[2] = y2; ys[3] = y3;
+}
+
+// y = (xr kr - xi ki) + i (xr ki + xi kr) from the four real results
+__global__ void complex_combine_kernel(const float *__restrict__ rr, const float *__restrict__ ii,
+                                       const float *__restrict__ ri, const float *__restrict__ ir,
+                                       float2 *__restrict__ y, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = make_float2(rr[i] - ii[i], ri[i] + ir[i]);
+}
+
 // ---- host -------------------------------------------------------------------
 typedef CUresult (*EncodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
@@ -972,6 +991,80 @@ int run_bf16x3(const ndconv_problem *p, int64_t n, const float *x, const float *
     if (e != cudaSuccess) return ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e));
     return NDCONV_OK;
 }
+// Complex<f32>: the real and imaginary parts are strided f32 views of the
+// interleaved arrays (element strides doubled, the imaginary part one float
+// further); the padded real view takes the real part of each border
+// constant, the imaginary view the imaginary part (the other border kinds
+// commute with taking parts).  Batched launches give xr*kr, xr*ki (real view
+// of the data) and xi*ki, xi*kr -- one launch when both views pad alike, two
+// otherwise; a last pass combines them as num-complex's product does.
+int run_bf16x3_complex(const ndconv_problem *p, const c32 *x, const c32 *k, c32 *y, cudaStream_t st) {
+    Plan3 P;
+    int s = plan_problem(p, 0, &P);
+    if (s) return s;
+    ndconv_problem q = *p;
+    q.dtype = NDCONV_F32;
+    const int r = p->rank;
+    auto doubled = [&](const int64_t *shape, const int64_t *strides, int64_t *outs) {
+        bool contig = true;
+        for (int i = 0; i < r; i++) contig = contig && strides[i] == 0;
+        int64_t run = 1;
+        for (int i = r - 1; i >= 0; i--) {
+            outs[i] = 2 * (contig ? run : strides[i]);
+            run *= shape[i];
+        }
+    };
+    doubled(p->data_shape, p->data_strides, q.data_strides);
+    doubled(p->kernel_shape, p->kernel_strides, q.kernel_strides);
+    ndconv_problem qi = q;  // the imaginary view: the constants' imaginary parts
+    qi.const_value[0] = p->const_value[1];
+    qi.const_value[1] = 0;
+    q.const_value[1] = 0;
+    for (int a = 0; a < 3; a++)
+        for (int sd = 0; sd < 2; sd++) {
+            qi.border_value[a][sd][0] = p->border_value[a][sd][1];
+            qi.border_value[a][sd][1] = 0;
+            q.border_value[a][sd][1] = 0;
+        }
+    Plan3 Q;
+    if ((s = plan_problem(&q, 0, &Q))) return s;
+    if (!applies(Q)) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "3xBF16 path: beyond the TMA index range");
+    const int64_t ny = P.ax[0].out * P.ax[1].out * P.ax[2].out;
+    unsigned char *ws = nullptr;
+    const size_t bytes = sizeof(float) * 4 * (size_t)ny + 3 * 4 * sizeof(void *) + 256;
+    cudaError_t e = cudaMallocAsync((void **)&ws, bytes, st);
+    if (e != cudaSuccess) return ndconv_fail(NDCONV_ERR_NO_MEMORY, cudaGetErrorString(e));
+    float *t = reinterpret_cast<float *>(ws);  // rr, ri, ii, ir
+    const float **xs = reinterpret_cast<const float **>(
+        (reinterpret_cast<uintptr_t>(t + 4 * ny) + 15) & ~(uintptr_t)15);
+    const float **ks = xs + 4;
+    float **ys = reinterpret_cast<float **>(reinterpret_cast<uintptr_t>(ks + 4));
+    const float *xr = reinterpret_cast<const float *>(x), *kr = reinterpret_cast<const float *>(k);
+    set_ptrs_kernel<<<1, 1, 0, st>>>(xs, ks, ys, xr, xr, xr + 1, xr + 1, kr, kr + 1, kr + 1, kr, t, t + ny,
+                                     t + 2 * ny, t + 3 * ny);
+    ndconv_count_launch();
+    // one launch for all four when both views pad alike (no constant has an
+    // imaginary part that differs from its real part)
+    bool alike = q.const_value[0] == qi.const_value[0];
+    for (int a = 0; a < 3; a++)
+        for (int sd = 0; sd < 2; sd++) alike = alike && q.border_value[a][sd][0] == qi.border_value[a][sd][0];
+    if (alike) {
+        s = run_bf16x3(&q, 4, nullptr, nullptr, nullptr, xs, ks, ys, st);
+    } else {
+        s = run_bf16x3(&q, 2, nullptr, nullptr, nullptr, xs, ks, ys, st);
+        if (!s) s = run_bf16x3(&qi, 2, nullptr, nullptr, nullptr, xs + 2, ks + 2, ys + 2, st);
+    }
+    if (!s) {
+        const unsigned nb = (unsigned)std::max<int64_t>(1, std::min<int64_t>(152 * 8, (ny + 255) / 256));
+        complex_combine_kernel<<<nb, 256, 0, st>>>(t, t + 2 * ny, t + ny, t + 3 * ny, reinterpret_cast<float2 *>(y),
+                                                   ny);
+        ndconv_count_launch();
+        e = cudaGetLastError();
+        if (e != cudaSuccess) s = ndconv_fail(NDCONV_ERR_CUDA, cudaGetErrorString(e));
+    }
+    cudaFreeAsync(ws, st);
+    return s;
+}
 }  // namespace
 
 extern "C" int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, const void *kernel, void *out,
@@ -981,6 +1074,9 @@ extern "C" int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, con
         if (const int s = plan_problem(p, 0, &P)) return s;
         return ndconv_fail(NDCONV_ERR_INVALID, "null pointer");
     }
+    if (p && p->dtype == NDCONV_C32)
+        return run_bf16x3_complex(p, static_cast<const c32 *>(data), static_cast<const c32 *>(kernel),
+                                  static_cast<c32 *>(out), (cudaStream_t)stream);
     return run_bf16x3(p, 1, static_cast<const float *>(data), static_cast<const float *>(kernel),
                       static_cast<float *>(out), nullptr, nullptr, nullptr, (cudaStream_t)stream);
 }

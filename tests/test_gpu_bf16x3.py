@@ -136,3 +136,36 @@ def test_bf16x3_batch_nonfinite_instance():
         assert np.array_equal(np.isnan(y), np.isnan(y64))
         fin = np.isfinite(y64)
         assert np.allclose(y[fin], y64[fin], rtol=1e-5, atol=1e-5)
+
+
+@pytest.mark.parametrize("shape,kshape,dil,mode,pm", [
+    ((10, 100, 200), (5, 11, 31), 1, ConvMode.Same, PaddingMode.Zeros),
+    ((70, 180), (9, 17), [2, 1], ConvMode.Same, PaddingMode.Const(complex(0.5, -1.25))),
+    ((40, 90), (5, 7), 1, ConvMode.Custom([2, 3], [1, 2]),
+     PaddingMode.Custom([BorderType.Reflect, BorderType.Const(complex(-0.75, 2.0))])),
+    ((600,), (33,), 1, ConvMode.Full, PaddingMode.Circular),
+])
+def test_bf16x3_complex_vs_oracle(shape, kshape, dil, mode, pm):
+    """Complex<f32> on the tensor cores (four real 3xBF16 convolutions over
+    the interleaved parts): within 1e-5 normwise of the f64 oracle, border
+    constants with imaginary parts included."""
+    rng = np.random.default_rng(sum(shape) + 7)
+    x = (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+    k = (rng.standard_normal(kshape) + 1j * rng.standard_normal(kshape)).astype(np.complex64)
+    y64 = _oracle64(x, with_dilation(k, dil), mode, pm)
+    y = ndconv.conv_algo(x, with_dilation(k, dil), mode, pm, BF)
+    assert y.shape == y64.shape
+    assert normwise_err(y, y64) <= TOL32, normwise_err(y, y64)
+
+
+def test_bf16x3_complex_strided_view():
+    """A strided complex view (every other column) is read in place."""
+    import torch
+    rng = np.random.default_rng(5)
+    base = (rng.standard_normal((50, 160)) + 1j * rng.standard_normal((50, 160))).astype(np.complex64)
+    k = (rng.standard_normal((7, 9)) + 1j * rng.standard_normal((7, 9))).astype(np.complex64)
+    xv = torch.from_numpy(base).cuda()[:, ::2]
+    mode, pm = ConvMode.Same, PaddingMode.Replicate
+    y = ndconv.conv_algo(xv, torch.from_numpy(k).cuda(), mode, pm, BF).cpu().numpy()
+    y64 = _oracle64(np.ascontiguousarray(base[:, ::2]), k, mode, pm)
+    assert normwise_err(y, y64) <= TOL32
