@@ -218,6 +218,15 @@ int ndconv_conv_bf16x3(const ndconv_problem *p, const void *data, const void *ke
  * only (NDCONV_ERR_UNSUPPORTED for other element types). */
 int ndconv_conv_bf16x3_batch(const ndconv_problem *p, int64_t n, const void *const *data,
                              const void *const *kernel, void *const *out, void *stream);
+/* Host only: the tile plan of ndconv_conv_bf16x3 for p (a complex
+ * problem: its real views'), for tests and tuning.  out[0..15] = kernel
+ * rows per group G, row groups, output columns per tile BN, MMA N = G BN,
+ * K extent Kpad, 64-wide K chunks, 16-wide steps in the last chunk, output
+ * rows per tile, ring stages, stage bytes, ring bytes (resident Toeplitz
+ * tiles included), dynamic shared memory, Toeplitz tiles resident (0/1),
+ * tiles along the middle axis, tiles along the contiguous axis, the shared
+ * memory limit.  No reference counterpart. */
+int ndconv_bf16x3_plan(const ndconv_problem *p, int64_t out[16]);
 /* Synchronises stream, then reports (NDCONV_ERR_TIMEOUT) and clears the
  * timeouts of every 3xBF16 launch on the current device since the last
  * call; NDCONV_OK when there were none.  No reference counterpart. */

@@ -1094,6 +1094,24 @@ extern "C" int ndconv_conv_bf16x3_batch(const ndconv_problem *p, int64_t n, cons
                       (cudaStream_t)stream);
 }
 
+// See include/ndconv.h.  Host only: the tile plan ndconv_conv_bf16x3 would
+// launch for p (f32 geometry; a complex problem's plan is its real views').
+extern "C" int ndconv_bf16x3_plan(const ndconv_problem *p, int64_t out[16]) {
+    if (!out) return ndconv_fail(NDCONV_ERR_INVALID, "null output");
+    ndconv_problem q = *p;
+    if (q.dtype == NDCONV_C32) q.dtype = NDCONV_F32;
+    Plan3 P;
+    if (const int s = plan_problem(&q, 0, &P)) return s;
+    if (!applies(P)) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "3xBF16 path: f32 within the TMA index range only");
+    const TilePlan T = plan_tiles(P);
+    const AxisGeom *A = P.ax;
+    const int64_t v[16] = {T.G, T.ngroups, T.BN, T.N, T.Kpad, T.nchunk, T.klast, T.mvalid,
+                           T.stages, T.stage_bytes, T.ring_bytes, T.smem, T.bres, (A[1].out + T.mvalid - 1) / T.mvalid,
+                           (A[2].out + T.BN - 1) / T.BN, kSmemLimit};
+    for (int i = 0; i < 16; i++) out[i] = v[i];
+    return NDCONV_OK;
+}
+
 // See include/ndconv.h.  Waits for the stream, then reads and clears the
 // device's timeout word.
 extern "C" int ndconv_bf16x3_status(void *stream) {

@@ -111,6 +111,7 @@ def lib():
         "ndconv_batch_stall_one_wait": (ctypes.c_int, [vp, i32]),
         "ndconv_bf16x3_status": (ctypes.c_int, [vp]),
         "ndconv_conv_bf16x3_batch": (ctypes.c_int, [pp, ctypes.c_int64, vp, vp, vp, vp]),
+        "ndconv_bf16x3_plan": (ctypes.c_int, [pp, i64p]),
         "ndconv_set_tuning": (ctypes.c_int, [i32, i32]),
         "ndconv_get_tuning": (ctypes.c_int32, [i32]),
         "ndconv_batch_info": (ctypes.c_int, [vp, i64p]),
