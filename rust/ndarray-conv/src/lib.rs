@@ -16,11 +16,13 @@ mod conv;
 mod conv_fft;
 mod device;
 mod dilation;
+mod tensor;
 
 pub use conv::ConvExt;
 pub use conv_fft::{get_processor as get_fft_processor, ConvFFTExt, FftNum, FftProcessor, GetProcessor, Processor};
 pub use device::DeviceElem;
 pub use dilation::{IntoDilation, IntoKernelWithDilation, KernelWithDilation, ReverseKernel, WithDilation};
+pub use tensor::{ConvTensorExt, TensorElem};
 
 /// How the output size is determined (the original's `ConvMode<N>`).
 #[derive(Debug, Clone, Copy)]
