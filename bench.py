@@ -20,6 +20,8 @@ The default line also carries, in `config`:
                 drop-in (per-instance calls with the library's default picks)
   direct_tensor_cores  the same 64 instances through the batched 3xBF16
                 tensor-core direct path (one persistent launch)
+  replicated    configs 1 and 3 as 64-instance batches through the batched
+                FFT, direct FP32 and tensor-core entry points
   variants      the 1-D and 3-D cases (and the 3-D complex copy, and a 2-D
                 31 x 31 kernel) through direct FP32, 3xBF16 tensor cores
                 and FFT: device time per call and error against f64
@@ -455,7 +457,7 @@ def cpu_baseline_uneven(specs, seconds):
 # normwise error against the f64 oracle: (key, description, x shape, kernel
 # shape, mode, padding, dtype, variants)
 VARIANT_CASES = [
-    ("c1", "1-D f32 x[5000] * k[31], Full, Zeros", (5000,), (31,), "Full", "Zeros", "f32", ["direct", "fft"]),
+    ("c1", "1-D f32 x[5000] * k[31], Full, Zeros", (5000,), (31,), "Full", "Zeros", "f32", ["direct", "bf16x3", "fft"]),
     ("c3", "3-D f32 x[10,100,200] * k[5,11,31], Same, Zeros", (10, 100, 200), (5, 11, 31), "Same", "Zeros", "f32",
      ["direct", "bf16x3", "fft"]),
     ("c3_complex", "3-D Complex<f32> x[10,100,200] * k[5,11,31] (re, im i.i.d. N(0,1)), Same, Zeros",
@@ -532,6 +534,65 @@ def _variant_case(desc, xs, ksh, mode_n, pad_n, dt, variants, reps):
     if "bf16x3" in variants:
         res["bf16x3_over_direct_speedup"] = res["direct"]["us_per_call"] / res["bf16x3"]["us_per_call"]
     return res
+
+
+def measure_replicated(B=64, reps=10):
+    """Configs 1 and 3 as B-fold replicated batches (distinct seeded
+    instances, one submission per step) through the batched FFT, direct FP32
+    and 3xBF16 tensor-core entry points: GB/s of algorithmic bytes and the
+    f64-oracle error of instance 0."""
+    import torch
+    import ndconv
+    from ndconv import _abi, build_problem, with_dilation, ConvMode, PaddingMode
+    from oracle import oracle as O
+    L = _abi.lib()
+    cases = [("c1", "1-D f32 x[5000] * k[31], Full, Zeros", (5000,), (31,), ConvMode.Full),
+             ("c3", "3-D f32 x[10,100,200] * k[5,11,31], Same, Zeros", (10, 100, 200), (5, 11, 31), ConvMode.Same)]
+    out = {}
+    for key, desc, xs_shape, ks_shape, mode in cases:
+        pm = PaddingMode.Zeros
+        rng = np.random.default_rng(5000 + len(xs_shape))
+        xs_np = [rng.random(xs_shape, dtype=np.float32) for _ in range(B)]
+        ks_np = [rng.random(ks_shape, dtype=np.float32) for _ in range(B)]
+        xs = [torch.from_numpy(a).cuda() for a in xs_np]
+        ks = [torch.from_numpy(a).cuda() for a in ks_np]
+        p = build_problem(_abi.F32, xs_shape, with_dilation(ks[0], 1), mode, pm)
+        p64 = build_problem(_abi.F64, xs_shape, with_dilation(ks_np[0], 1), mode, pm)
+        st64, y64 = O.conv(p64, xs_np[0].astype(np.float64), ks_np[0].astype(np.float64))
+        osh = (ctypes.c_int64 * 3)()
+        assert L.ndconv_output_shape(ctypes.byref(p), 0, osh) == 0, _abi.last_error()
+        oshape = tuple(osh[i] for i in range(len(xs_shape)))
+        nbytes = 4 * (int(np.prod(xs_shape)) + int(np.prod(ks_shape)) + int(np.prod(oshape)))
+        ys = [torch.empty(oshape, device="cuda") for _ in range(B)]
+        PX, PK, PY = [torch.tensor([t.data_ptr() for t in ts], dtype=torch.int64, device="cuda") for ts in (xs, ks, ys)]
+        sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        proc = ndconv.get_fft_processor(torch.float32)
+        a = [ctypes.byref(p), B, ctypes.c_void_p(PX.data_ptr()), ctypes.c_void_p(PK.data_ptr()),
+             ctypes.c_void_p(PY.data_ptr())]
+        calls = {"fft": lambda: L.ndconv_conv_fft_batch(*a, proc._handle, sp),
+                 "direct": lambda: L.ndconv_conv_batch(*a, sp),
+                 "bf16x3": lambda: L.ndconv_conv_bf16x3_batch(*a, sp)}
+        res = {"workload": f"{B} x {desc}, one batched submission per step", "bytes_per_instance": nbytes}
+        for name, call in calls.items():
+            try:
+                for _ in range(3):
+                    if call():
+                        raise RuntimeError(_abi.last_error())
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(reps):
+                    call()
+                e1.record()
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1) / reps
+                y0 = ys[0].cpu().numpy().astype(np.float64)
+                err = float(np.linalg.norm(y0 - y64) / np.linalg.norm(y64)) if st64 == 0 else None
+                res[name] = {"gbs": nbytes * B / (ms * 1e-3) / 1e9, "ms_per_step": ms, "normwise_err": err}
+            except Exception as ex:
+                res[name] = {"error": f"{type(ex).__name__}: {ex}"[:200]}
+        out[key] = res
+    return out
 
 
 def measure_c2_tensor(args, world, rank, local_rank, dist):
@@ -782,7 +843,7 @@ def main():
             return bench_uneven(args, world, rank, local_rank, dist)
         algo = 1 if args.algo == "fft" else 0
         r = measure_c2(args, algo, args.form, world, rank, local_rank, dist)
-        extra_direct = extra_uneven = extra_variants = extra_tensor = None
+        extra_direct = extra_uneven = extra_variants = extra_tensor = extra_replicated = None
         if not args.no_extra and algo == 1 and args.form == "batched":
             extra_direct = measure_c2(args, 0, "batched", world, rank, local_rank, dist)
             try:
@@ -792,6 +853,10 @@ def main():
             extra_uneven = measure_uneven(args, world, rank, local_rank, dist)
             if rank == 0:
                 extra_variants = measure_variants()
+                try:
+                    extra_replicated = measure_replicated()
+                except Exception as ex:  # the line still prints; the block says why it has no figures
+                    extra_replicated = {"error": f"{type(ex).__name__}: {ex}"[:200]}
         if rank != 0:
             return
         B = args.batch
@@ -829,6 +894,8 @@ def main():
             config["variants"] = extra_variants
         if extra_tensor:
             config["direct_tensor_cores"] = extra_tensor
+        if extra_replicated:
+            config["replicated"] = extra_replicated
         line = {
             "metric": METRIC,
             "value": gbs(r["ms"]), "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,

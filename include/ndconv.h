@@ -225,8 +225,12 @@ int ndconv_conv_bf16x3_batch(const ndconv_problem *p, int64_t n, const void *con
  * rows per tile, ring stages, stage bytes, ring bytes (resident Toeplitz
  * tiles included), dynamic shared memory, Toeplitz tiles resident (0/1),
  * tiles along the middle axis, tiles along the contiguous axis, the shared
- * memory limit.  No reference counterpart. */
-int ndconv_bf16x3_plan(const ndconv_problem *p, int64_t out[16]);
+ * memory limit, then out[16..17] = outputs per virtual row S and virtual
+ * rows R of a folded single row (0 and 1 when not folded: a single row --
+ * a 1-D signal, or one row with one-row kernels -- is cut into R stretches
+ * of S outputs that fill the tile's 128 accumulator lanes; the tile counts
+ * before are those of the folded geometry).  No reference counterpart. */
+int ndconv_bf16x3_plan(const ndconv_problem *p, int64_t out[18]);
 /* Synchronises stream, then reports (NDCONV_ERR_TIMEOUT) and clears the
  * timeouts of every 3xBF16 launch on the current device since the last
  * call; NDCONV_OK when there were none.  No reference counterpart. */

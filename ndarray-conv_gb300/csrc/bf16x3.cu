@@ -86,6 +86,7 @@ struct Params {
     uint32_t idesc;
     float *y;
     int64_t ys0, ys1;
+    int64_t xlast;     // outputs in the last output row (a folded row's ragged end; out2 otherwise)
     const int *flags;  // per pre-pass block: a non-finite input seen (any instance)
     int nflags;
     DirectParams<float> dp;  // FP32 fallback
@@ -197,27 +198,35 @@ __device__ __forceinline__ void tmem_ld_wait(uint32_t *r) {
 }
 
 // ---- pre-passes -----------------------------------------------------------
-// Padded data planes [n][P0][P1][W] (hi, lo) of n instances (xs: device
+// Padded data planes [n][rows][W] (hi, lo) of n instances (xs: device
 // array of their data pointers, or null for the one instance x); zero beyond
-// the padded extent.  A thread converts 8 consecutive samples of a row and
-// stores them as 16-byte vectors (W is a multiple of 8).
+// column lim.  Unfolded (hop 0): rows = P0 P1 planes' rows, lim the padded
+// extent.  A folded row (hop > 0): row r holds padded positions r hop ..
+// r hop + lim - 1 of the one padded row.  A thread converts 8 consecutive
+// samples of a row and stores them as 16-byte vectors (W is a multiple of 8).
 // (blocks bid of nblk of the pre-pass launch; returns whether this thread saw
 // a non-finite value)
 __device__ __forceinline__ bool split_part(const float *__restrict__ x, const float *const *xs, int64_t n,
-                                           const Geom3<float> &g, int64_t W, __nv_bfloat16 *__restrict__ hi,
+                                           const Geom3<float> &g, int64_t W, int64_t rows, int64_t hop,
+                                           int64_t lim, __nv_bfloat16 *__restrict__ hi,
                                            __nv_bfloat16 *__restrict__ lo, int64_t bid, int64_t nblk) {
     const AxisGeom &A2 = g.ax[2];
-    const int64_t cw = W / 8, rows = g.ax[0].L * g.ax[1].L, total = n * rows * cw;
+    const int64_t cw = W / 8, total = n * rows * cw;
     bool bad = false;
     for (int64_t u = bid * blockDim.x + threadIdx.x; u < total; u += nblk * blockDim.x) {
         const int64_t grow = u / cw, c0 = (u - grow * cw) * 8;  // row over all instances
         const int64_t inst = grow / rows, row = grow - inst * rows;
         const float *xi = xs ? xs[inst] : x;
-        const int64_t i1 = row % g.ax[1].L, i0 = row / g.ax[1].L;
-        const int64_t m0 = axis_map(g.ax[0], i0), m1 = axis_map(g.ax[1], i1);
+        int64_t m0 = 0, m1 = 0, q0 = c0;  // q0: padded position of the first sample
+        if (hop) {
+            q0 += row * hop;
+        } else {
+            m0 = axis_map(g.ax[0], row / g.ax[1].L);
+            m1 = axis_map(g.ax[1], row % g.ax[1].L);
+        }
         float v[8];
-        const int64_t j0 = c0 - A2.p0;  // input index of the first sample
-        if (m0 >= 0 && m1 >= 0 && A2.xs == 1 && j0 >= 0 && j0 + 8 <= A2.n) {
+        const int64_t j0 = q0 - A2.p0;  // input index of the first sample
+        if (m0 >= 0 && m1 >= 0 && A2.xs == 1 && j0 >= 0 && j0 + 8 <= A2.n && c0 + 8 <= lim) {
             // interior samples of a contiguous row: plain (vector) loads
             const float *src = xi + m0 * g.ax[0].xs + m1 * g.ax[1].xs + j0;
             if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
@@ -239,8 +248,8 @@ __device__ __forceinline__ bool split_part(const float *__restrict__ x, const fl
         } else {
 #pragma unroll
             for (int q = 0; q < 8; q++) {
-                const int64_t i2 = c0 + q;
-                v[q] = i2 < A2.L ? resolve_padded<float>(xi, g, m0, m1, axis_map(A2, i2)) : 0.f;
+                const int64_t i2 = q0 + q;
+                v[q] = c0 + q < lim && i2 < A2.L ? resolve_padded<float>(xi, g, m0, m1, axis_map(A2, i2)) : 0.f;
             }
         }
         uint32_t h[4], l[4];
@@ -304,12 +313,13 @@ __device__ __forceinline__ bool toeplitz_part(const float *__restrict__ k1, cons
 // value in flags[blockIdx.x] (no zeroing needed before the launch).
 __global__ void __launch_bounds__(256) prepass_kernel(const float *__restrict__ x, const float *const *xs,
                                                       const float *__restrict__ k1, const float *const *ks,
-                                                      int64_t n, Geom3<float> g, int64_t W, int reverse, int G,
+                                                      int64_t n, Geom3<float> g, int64_t W, int64_t rows,
+                                                      int64_t hop, int64_t lim, int reverse, int G,
                                                       int BN, int ngroups, int64_t Cp, __nv_bfloat16 *xh,
                                                       __nv_bfloat16 *xl, __nv_bfloat16 *th, __nv_bfloat16 *tl,
                                                       int nbs, int *flags) {
     const int b = blockIdx.x;
-    const bool bad = b < nbs ? split_part(x, xs, n, g, W, xh, xl, b, nbs)
+    const bool bad = b < nbs ? split_part(x, xs, n, g, W, rows, hop, lim, xh, xl, b, nbs)
                              : toeplitz_part(k1, ks, n, g, reverse, G, BN, ngroups, Cp, th, tl, b - nbs,
                                              (int64_t)gridDim.x - nbs);
     const int any = __syncthreads_or(bad);
@@ -400,7 +410,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             float *y = out_of(P, c.inst);
             for (int u = tid; u < P.mvalid * BN; u += kThreads) {
                 const int64_t oy = c.oy0 + u / BN, ox = c.ox0 + u % BN;
-                if (ox < P.out2 && oy < P.out1) direct_naive_one<float>(x, k, y, P.dp, (c.oz * P.out1 + oy) * P.out2 + ox);
+                if (oy < P.out1 && ox < (oy == P.out1 - 1 ? P.xlast : P.out2))
+                    direct_naive_one<float>(x, k, y, P.dp, (c.oz * P.out1 + oy) * P.out2 + ox);
             }
         }
         return;
@@ -702,8 +713,9 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (lane == 0) mbar_arrive(&tempty[buf]);
             }
             if (!stop && !eg && et < P.mvalid && c.oy0 + et < P.out1) {
+                const int64_t xl = c.oy0 + et == P.out1 - 1 ? P.xlast : P.out2;  // columns of this row
                 float *yr = out_of(P, c.inst) + c.oz * P.ys0 + (c.oy0 + et) * P.ys1 + c.ox0;
-                if (c.ox0 + BN <= P.out2 && (reinterpret_cast<uintptr_t>(yr) & 15) == 0) {
+                if (c.ox0 + BN <= xl && (reinterpret_cast<uintptr_t>(yr) & 15) == 0) {
 #pragma unroll
                     for (int q = 0; q < BN / 4; q++)
                         reinterpret_cast<float4 *>(yr)[q] =
@@ -711,7 +723,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 } else {
 #pragma unroll
                     for (int q = 0; q < BN; q++)
-                        if (c.ox0 + q < P.out2) yr[q] = acc[q];
+                        if (c.ox0 + q < xl) yr[q] = acc[q];
                 }
             }
         }
@@ -735,7 +747,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             float *y = out_of(P, c.inst);
             for (int u = tid; u < P.mvalid * BN; u += kThreads) {
                 const int64_t oy = c.oy0 + u / BN, ox = c.ox0 + u % BN;
-                if (ox < P.out2 && oy < P.out1) y[c.oz * P.ys0 + oy * P.ys1 + ox] = __int_as_float(0x7fc00000);
+                if (oy < P.out1 && ox < (oy == P.out1 - 1 ? P.xlast : P.out2))
+                    y[c.oz * P.ys0 + oy * P.ys1 + ox] = __int_as_float(0x7fc00000);
             }
         }
         __syncthreads();
@@ -869,6 +882,50 @@ bool applies(const Plan3 &P) {
            A[0].L * A[1].L < 0x7fffffff;
 }
 
+// A single row (a 1-D signal, or an array of one row with one-row kernels)
+// folds into R virtual rows of S outputs: virtual row r starts at padded
+// position r S s2, so the 128 accumulator lanes of a tile hold 128 stretches
+// of the row instead of one row and 127 lanes of padding.  S is the least
+// multiple of BN that is at least 4 (K2 - 1) d2 / s2: neighbouring stretches
+// share (K2 - 1) d2 + 1 - s2 inputs, at most about a fifth of a virtual row.
+struct RowFold {
+    int64_t S = 0;      // outputs per virtual row (0: not folded)
+    int64_t R = 1;      // virtual rows
+    int64_t hop = 0;    // padded positions between virtual rows (S s2)
+    int64_t xlast = 0;  // outputs in the last output row
+};
+Plan3 fold_row(const Plan3 &P, int BN, RowFold *f) {
+    const AxisGeom *A = P.ax;
+    *f = RowFold{};
+    f->xlast = A[2].out;
+    if (!(A[0].L == 1 && A[1].L == 1 && A[0].K == 1 && A[1].K == 1 && A[0].out == 1 && A[1].out == 1)) return P;
+    const int64_t want = (4 * (A[2].K - 1) * A[2].d + A[2].s - 1) / A[2].s;
+    const int64_t S = std::max<int64_t>(BN, (want + BN - 1) / BN * BN);
+    const int64_t R = (A[2].out + S - 1) / S;
+    if (R < 2) return P;  // one stretch: nothing to fold
+    Plan3 V = P;
+    AxisGeom &v1 = V.ax[1], &v2 = V.ax[2];
+    v1.n = v1.L = v1.out = R;
+    v1.p0 = v1.p1 = 0;
+    v1.K = v1.d = v1.keff = v1.s = 1;
+    v2.out = S;
+    v2.L = v2.n = (S - 1) * A[2].s + (A[2].K - 1) * A[2].d + 1;
+    v2.p0 = v2.p1 = 0;
+    v2.keff = (A[2].K - 1) * A[2].d + 1;
+    f->S = S;
+    f->R = R;
+    f->hop = S * A[2].s;
+    f->xlast = A[2].out - (R - 1) * S;
+    return V;
+}
+
+// The plan a call runs: the problem's own geometry, or its folded row.
+Plan3 tile_geometry(const Plan3 &P, TilePlan *T, RowFold *f) {
+    const Plan3 V = fold_row(P, plan_tiles(P).BN, f);
+    *T = plan_tiles(V);
+    return V;
+}
+
 }  // namespace bf16x3
 
 bool bf16x3_applies(const Plan3 &P) { return bf16x3::applies(P); }
@@ -889,9 +946,11 @@ int run_bf16x3(const ndconv_problem *p, int64_t n, const float *x, const float *
     int s = plan_problem(p, 0, &P);
     if (s) return s;
     if (!applies(P)) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "3xBF16 path: f32 within the TMA index range only");
-    const AxisGeom *A = P.ax;
-    const Geom3<float> g = P.geom<float>();
-    const TilePlan T = plan_tiles(P);
+    const Geom3<float> g = P.geom<float>();  // where the samples come from
+    TilePlan T;
+    RowFold f;
+    const Plan3 V = tile_geometry(P, &T, &f);  // what the tiles cover
+    const AxisGeom *A = V.ax;
     const int64_t Cp = (int64_t)T.nchunk * KC;                  // Toeplitz row pitch (elements)
     const int64_t W = std::max<int64_t>(KC, (A[2].L + 7) / 8 * 8);  // data row pitch (16-byte multiple)
     const int64_t Rt = A[0].K * T.ngroups * T.N;                // Toeplitz rows per instance
@@ -932,8 +991,8 @@ int run_bf16x3(const ndconv_problem *p, int64_t n, const float *x, const float *
             (s = make_map(&mTh, th, 2, dT, sT, bT)) || (s = make_map(&mTl, tl, 2, dT, sT, bT)))
             return fail(s);
     }
-    prepass_kernel<<<nbs + nbt, 256, 0, st>>>(x, xs, k, ks, n, g, W, P.reverse, T.G, T.BN, T.ngroups, Cp, xh, xl, th,
-                                             tl, nbs, flags);
+    prepass_kernel<<<nbs + nbt, 256, 0, st>>>(x, xs, k, ks, n, g, W, A[0].L * A[1].L, f.hop, A[2].L, P.reverse,
+                                             T.G, T.BN, T.ngroups, Cp, xh, xl, th, tl, nbs, flags);
     ndconv_count_launch();
     Params Q{};
     Q.out0 = A[0].out;
@@ -965,6 +1024,7 @@ int run_bf16x3(const ndconv_problem *p, int64_t n, const float *x, const float *
     Q.y = y;
     Q.ys0 = A[1].out * A[2].out;
     Q.ys1 = A[2].out;
+    Q.xlast = f.xlast;
     Q.flags = flags;
     Q.nflags = nflags;
     Q.dp = P.direct<float>();
@@ -1096,19 +1156,21 @@ extern "C" int ndconv_conv_bf16x3_batch(const ndconv_problem *p, int64_t n, cons
 
 // See include/ndconv.h.  Host only: the tile plan ndconv_conv_bf16x3 would
 // launch for p (f32 geometry; a complex problem's plan is its real views').
-extern "C" int ndconv_bf16x3_plan(const ndconv_problem *p, int64_t out[16]) {
+extern "C" int ndconv_bf16x3_plan(const ndconv_problem *p, int64_t out[18]) {
     if (!out) return ndconv_fail(NDCONV_ERR_INVALID, "null output");
     ndconv_problem q = *p;
     if (q.dtype == NDCONV_C32) q.dtype = NDCONV_F32;
     Plan3 P;
     if (const int s = plan_problem(&q, 0, &P)) return s;
     if (!applies(P)) return ndconv_fail(NDCONV_ERR_UNSUPPORTED, "3xBF16 path: f32 within the TMA index range only");
-    const TilePlan T = plan_tiles(P);
-    const AxisGeom *A = P.ax;
-    const int64_t v[16] = {T.G, T.ngroups, T.BN, T.N, T.Kpad, T.nchunk, T.klast, T.mvalid,
+    TilePlan T;
+    RowFold f;
+    const Plan3 V = tile_geometry(P, &T, &f);
+    const AxisGeom *A = V.ax;
+    const int64_t v[18] = {T.G, T.ngroups, T.BN, T.N, T.Kpad, T.nchunk, T.klast, T.mvalid,
                            T.stages, T.stage_bytes, T.ring_bytes, T.smem, T.bres, (A[1].out + T.mvalid - 1) / T.mvalid,
-                           (A[2].out + T.BN - 1) / T.BN, kSmemLimit};
-    for (int i = 0; i < 16; i++) out[i] = v[i];
+                           (A[2].out + T.BN - 1) / T.BN, kSmemLimit, f.S, f.R};
+    for (int i = 0; i < 18; i++) out[i] = v[i];
     return NDCONV_OK;
 }
 

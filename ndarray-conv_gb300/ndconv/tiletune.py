@@ -94,8 +94,9 @@ class KnobTimes:
         return db
 
 
-def time_spec(spec, gen, reps=2):
-    """[len(ALGOS), MAX_COMBOS] best-of-reps times (ms) of one instance."""
+def time_spec(spec, gen, reps=2, only=None):
+    """[len(ALGOS), MAX_COMBOS] best-of-reps times (ms) of one instance
+    (variants outside `only`, when given, stay inf)."""
     import torch
     L = _abi.lib()
     x = torch.rand(spec.shape, generator=gen, device="cuda") * 2 - 1
@@ -108,6 +109,8 @@ def time_spec(spec, gen, reps=2):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     out = np.full((len(ALGOS), MAX_COMBOS), np.inf)
     for ai, (algo, combos) in enumerate(KNOB_SPACE):
+        if only is not None and algo not in only:
+            continue
         for ci, settings in enumerate(combos):
             with tuning(settings):
                 call = (ctypes.byref(p), algo, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(k.data_ptr()),
@@ -212,6 +215,10 @@ def main():
     ap.add_argument("--seed", type=int, default=7000)
     ap.add_argument("--out", required=True)
     ap.add_argument("--timings", default=None, help="reuse saved knob timings")
+    ap.add_argument("--retime-algo", type=int, default=None,
+                    help="with --timings: time this variant's knob settings again")
+    ap.add_argument("--retime-rank", type=int, nargs="*", default=[1, 2, 3],
+                    help="ranks whose instances --retime-algo times again")
     args = ap.parse_args()
     import torch
     from .autotune import dispatcher_configs
@@ -221,6 +228,13 @@ def main():
     t0 = time.time()
     if args.timings:
         db = KnobTimes.load(args.timings)
+        if args.retime_algo is not None:
+            ai = ALGOS.index(args.retime_algo)
+            gen = torch.Generator(device="cuda").manual_seed(args.seed)
+            for i, s in enumerate(db.specs):
+                if s.rank in args.retime_rank:
+                    db.times[i][ai] = time_spec(s, gen, only=(args.retime_algo,))[ai]
+            db.save(os.path.join(args.out, "knob_timings.npz"))
     else:
         specs = dispatcher_configs(args.train + args.holdout, seed=args.seed)
         gen = torch.Generator(device="cuda").manual_seed(args.seed)

@@ -126,6 +126,7 @@ extern "C" {
     pub fn ndconv_conv_bf16x3_batch(p: *const ndconv_problem, n: i64, data: *const *const c_void,
                                     kernel: *const *const c_void, out: *const *mut c_void,
                                     stream: *mut c_void) -> i32;
+    /// `out` holds 18 values (the tile plan, then a folded row's S and R).
     pub fn ndconv_bf16x3_plan(p: *const ndconv_problem, out: *mut i64) -> i32;
     pub fn ndconv_bf16x3_status(stream: *mut c_void) -> i32;
     pub fn ndconv_conv_batch(p: *const ndconv_problem, n: i64, data: *const *const c_void,

@@ -2,7 +2,8 @@
 bounds its kernel relies on, over random geometries: the MMA shape
 (N = G BN, a multiple of 16 in 16..256), the kernel rows of a group inside
 the 128 staged rows for every output row the tile keeps, the K extent
-covering the tile's input window, tiles covering the output, and the
+covering the tile's input window, tiles covering the output (a folded
+single row: its virtual rows of S outputs), and the
 shared memory of the ring, the resident Toeplitz tiles, the epilogue's
 blocks and the barriers within the per-CTA limit."""
 import ctypes
@@ -48,18 +49,18 @@ def _random_problem(rng):
 
 def test_tile_plan_bounds(lib):
     rng = np.random.default_rng(2026)
-    checked = 0
+    checked = folded = 0
     for _ in range(3000):
         p, rank, kshape, dil = _random_problem(rng)
         osh = (ctypes.c_int64 * 3)()
         if lib.ndconv_output_shape(ctypes.byref(p), 0, osh) != _abi.OK:
             continue  # kernel larger than the padded input etc.: no plan
-        out = (ctypes.c_int64 * 16)()
+        out = (ctypes.c_int64 * 18)()
         st = lib.ndconv_bf16x3_plan(ctypes.byref(p), out)
         if st == _abi.ERR_UNSUPPORTED:
             continue
         assert st == _abi.OK, _abi.last_error()
-        G, ng, BN, N, Kpad, nchunk, klast, mvalid, stages, stage_b, ring, smem, bres, nrt, nct, lim = list(out)
+        G, ng, BN, N, Kpad, nchunk, klast, mvalid, stages, stage_b, ring, smem, bres, nrt, nct, lim, S, R = list(out)
         # canonical axes: the problem's axes in the last `rank` of three
         ks = [1] * (3 - rank) + list(kshape)
         ds = [1] * (3 - rank) + list(dil)
@@ -71,7 +72,15 @@ def test_tile_plan_bounds(lib):
         assert mvalid >= 1 and (mvalid - 1) * ss[1] + (G - 1) * ds[1] <= BM - 1
         assert Kpad % 16 == 0 and Kpad >= (BN - 1) * ss[2] + (K2 - 1) * ds[2] + 1
         assert nchunk == (Kpad + KC - 1) // KC and 1 <= klast <= 4 and Kpad == (nchunk - 1) * KC + 16 * klast
-        assert nrt * mvalid >= oo[1] and nct * BN >= oo[2]
+        if S:
+            # a single row cut into R stretches of S outputs, the last ragged
+            assert oo[0] == oo[1] == 1 and K0 == K1 == 1 and S % BN == 0 and R >= 2
+            assert (R - 1) * S < oo[2] <= R * S and S * ss[2] >= 4 * (K2 - 1) * ds[2]
+            assert nrt * mvalid >= R and nct * BN == S
+            folded += 1
+        else:
+            assert R == 1
+            assert nrt * mvalid >= oo[1] and nct * BN >= oo[2]
         assert stages >= 2 and stage_b % 1024 == 0
         bslot = 2 * N * KC * 2
         if bres:
@@ -80,4 +89,4 @@ def test_tile_plan_bounds(lib):
             assert stage_b == 2 * BM * KC * 2 + bslot and ring == stages * stage_b
         assert smem >= ring + EPILOGUE_AND_BARRIERS + 1024 and smem <= lim
         checked += 1
-    assert checked > 1000, checked
+    assert checked > 1000 and folded > 100, (checked, folded)

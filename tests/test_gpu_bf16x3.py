@@ -169,3 +169,103 @@ def test_bf16x3_complex_strided_view():
     y = ndconv.conv_algo(xv, torch.from_numpy(k).cuda(), mode, pm, BF).cpu().numpy()
     y64 = _oracle64(np.ascontiguousarray(base[:, ::2]), k, mode, pm)
     assert normwise_err(y, y64) <= TOL32
+
+
+def _fold_of(x, k, mode, pm):
+    """(S, R) of the tile plan: outputs per virtual row and virtual rows of a
+    folded single row, (0, 1) when the row is not folded."""
+    import ctypes
+    p = problem(_abi.F32, x, k, mode, pm)
+    out = (ctypes.c_int64 * 18)()
+    assert _abi.lib().ndconv_bf16x3_plan(ctypes.byref(p), out) == 0, _abi.last_error()
+    return int(out[16]), int(out[17])
+
+
+@pytest.mark.parametrize("shape,kshape,dil,mode,pm", [
+    ((200000,), (255,), 1, ConvMode.Same, PaddingMode.Reflect),
+    ((50000,), (31,), 2, ConvMode.Custom([7], [3]), PaddingMode.Circular),
+    ((30000,), (17,), 3, ConvMode.Explicit([[5, 40]], [2]), PaddingMode.Replicate),
+    ((611,), (31,), 1, ConvMode.Full, PaddingMode.Zeros),        # last virtual row: one output
+    ((5000,), (3,), 1, ConvMode.Same, PaddingMode.Zeros),        # S = BN
+    ((9000,), (63,), 1, ConvMode.Same, PaddingMode.Const(0.5)),
+    ((1, 20000), (1, 101), [1, 2], ConvMode.Same, PaddingMode.Custom([BorderType.Zeros, BorderType.Reflect])),
+    ((100000,), (1001,), 1, ConvMode.Valid, PaddingMode.Zeros),
+])
+def test_bf16x3_folded_row_vs_oracle(shape, kshape, dil, mode, pm):
+    """A single row cut into stretches that fill the 128 accumulator lanes:
+    within 1e-5 normwise of the f64 oracle, every output written once (the
+    output buffer starts as NaN)."""
+    import torch
+    rng = np.random.default_rng(sum(shape) + sum(kshape))
+    x = rng.random(shape).astype(np.float32) - 0.5
+    k = rng.random(kshape).astype(np.float32) - 0.5
+    kw = with_dilation(k, dil)
+    S, R = _fold_of(x, kw, mode, pm)
+    assert S > 0 and R >= 2
+    y64 = _oracle64(x, kw, mode, pm)
+    import ctypes
+    xd, kd = torch.from_numpy(x).cuda(), torch.from_numpy(k).cuda()
+    yd = torch.full(y64.shape, float("nan"), device="cuda")
+    p = problem(_abi.F32, x, kw, mode, pm)
+    st = _abi.lib().ndconv_conv_algo(ctypes.byref(p), BF, ctypes.c_void_p(xd.data_ptr()),
+                                     ctypes.c_void_p(kd.data_ptr()), ctypes.c_void_p(yd.data_ptr()),
+                                     ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == 0, _abi.last_error()
+    y = yd.cpu().numpy()
+    assert np.isfinite(y).all()
+    assert normwise_err(y, y64) <= TOL32, normwise_err(y, y64)
+
+
+@pytest.mark.parametrize("bn", [16, 32, 64])
+def test_bf16x3_folded_row_tile_widths(bn):
+    """Each tile width folds the row into its own stretch length."""
+    rng = np.random.default_rng(40 + bn)
+    x = rng.random((33333,)).astype(np.float32) - 0.5
+    k = rng.random((45,)).astype(np.float32) - 0.5
+    mode, pm = ConvMode.Full, PaddingMode.Reflect
+    y64 = _oracle64(x, k, mode, pm)
+    L = _abi.lib()
+    old = L.ndconv_get_tuning(_abi.TUNE_BF16X3_BN)
+    try:
+        assert L.ndconv_set_tuning(_abi.TUNE_BF16X3_BN, bn) == 0
+        S, R = _fold_of(x, k, mode, pm)
+        assert S % bn == 0 and R >= 2
+        assert normwise_err(ndconv.conv_algo(x, k, mode, pm, BF), y64) <= TOL32
+    finally:
+        L.ndconv_set_tuning(_abi.TUNE_BF16X3_BN, old)
+
+
+def test_bf16x3_folded_row_nonfinite():
+    """A non-finite sample in a folded row: the FP32 loop over the virtual
+    rows gives the reference's NaN pattern."""
+    rng = np.random.default_rng(12)
+    x = rng.random((7000,)).astype(np.float32)
+    k = rng.random((31,)).astype(np.float32)
+    x[4321] = np.inf
+    mode, pm = ConvMode.Full, PaddingMode.Zeros
+    assert _fold_of(x, k, mode, pm)[1] >= 2
+    st, y64 = O.conv(problem(F64, x, k, mode, pm), x.astype(np.float64), k.astype(np.float64))
+    y = ndconv.conv_algo(x, k, mode, pm, BF)
+    assert np.array_equal(np.isnan(y), np.isnan(y64)) and np.array_equal(np.isinf(y), np.isinf(y64))
+    fin = np.isfinite(y64)
+    assert np.allclose(y[fin], y64[fin], rtol=1e-5, atol=1e-5)
+
+
+def test_bf16x3_folded_row_batch_and_complex():
+    """Folded rows in a batch (bit for bit the single calls) and in the
+    complex form's four real views."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(21)
+    mode, pm = ConvMode.Same, PaddingMode.Circular
+    xs = [torch.rand((12345,), generator=g, device="cuda") - 0.5 for _ in range(6)]
+    ks = [torch.rand((37,), generator=g, device="cuda") - 0.5 for _ in range(6)]
+    ys = ndconv.conv_bf16x3_batch(xs, ks, mode, pm)
+    for i in range(6):
+        assert torch.equal(ys[i], ndconv.conv_algo(xs[i], ks[i], mode, pm, BF)), i
+    y64 = _oracle64(xs[5].cpu().numpy(), ks[5].cpu().numpy(), mode, pm)
+    assert normwise_err(ys[5].cpu().numpy(), y64) <= TOL32
+    rng = np.random.default_rng(22)
+    x = (rng.standard_normal(20000) + 1j * rng.standard_normal(20000)).astype(np.complex64)
+    k = (rng.standard_normal(63) + 1j * rng.standard_normal(63)).astype(np.complex64)
+    y64 = _oracle64(x, k, ConvMode.Full, PaddingMode.Reflect)
+    assert normwise_err(ndconv.conv_algo(x, k, ConvMode.Full, PaddingMode.Reflect, BF), y64) <= TOL32
