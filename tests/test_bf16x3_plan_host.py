@@ -90,3 +90,55 @@ def test_tile_plan_bounds(lib):
         assert smem >= ring + EPILOGUE_AND_BARRIERS + 1024 and smem <= lim
         checked += 1
     assert checked > 1000 and folded > 100, (checked, folded)
+
+
+def test_folded_row_reassembles_the_oracle(lib):
+    """The single-row fold as the kernel runs it, restated with the oracle:
+    with S and R from the library's plan, virtual row r is the padded row's
+    positions r S s .. r S s + (S - 1) s + (K - 1) d, each virtual row is
+    convolved Valid at the problem's stride (S outputs), and the first
+    out outputs of the R S equal the oracle's convolution of the row."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(77)
+    folded = 0
+    for _ in range(120):
+        n = int(rng.integers(50, 3000))
+        K = int(rng.choice([2, 3, 5, 17, 31, 63]))
+        d = int(rng.integers(1, 4))
+        s = int(rng.integers(1, 4))
+        mode = [ConvMode.Full, ConvMode.Same,
+                ConvMode.Custom([int(rng.integers(0, 20))], [s]),
+                ConvMode.Explicit([[int(rng.integers(0, 30)), int(rng.integers(0, 30))]], [s])][int(rng.integers(4))]
+        pm = [PaddingMode.Zeros, PaddingMode.Reflect, PaddingMode.Replicate, PaddingMode.Circular,
+              PaddingMode.Const(0.25)][int(rng.integers(5))]
+        x = rng.standard_normal(n)
+        k = rng.standard_normal(K)
+        kw32 = with_dilation(k.astype(np.float32), d)
+        p32 = build_problem(_abi.F32, (n,), kw32, mode, pm)
+        osh = (ctypes.c_int64 * 3)()
+        if lib.ndconv_output_shape(ctypes.byref(p32), 0, osh) != _abi.OK:
+            continue
+        out = (ctypes.c_int64 * 18)()
+        if lib.ndconv_bf16x3_plan(ctypes.byref(p32), out) != _abi.OK:
+            continue
+        S, R = int(out[16]), int(out[17])
+        if not S:
+            continue
+        p64 = build_problem(_abi.F64, (n,), with_dilation(k, d), mode, pm)
+        st, y = O.conv(p64, x, k)
+        assert st == 0
+        st, xp = O.padding(p64, x)
+        assert st == 0
+        ss = int(p64.mode_strides[0]) if p64.conv_mode >= 3 else 1
+        hop, wv = S * ss, (S - 1) * ss + (K - 1) * d + 1
+        rows = np.zeros((R, wv))
+        for r in range(R):
+            seg = xp[r * hop: r * hop + wv]
+            rows[r, :len(seg)] = seg
+        # each virtual row: Valid with the problem's stride, zero padding
+        pv = build_problem(_abi.F64, (wv,), with_dilation(k, d), ConvMode.Explicit([[0, 0]], [ss]), PaddingMode.Zeros)
+        yv = np.concatenate([O.conv(pv, rows[r], k)[1] for r in range(R)])
+        assert len(yv) == R * S and (R - 1) * S < len(y) <= R * S
+        assert np.allclose(yv[:len(y)], y, rtol=1e-12, atol=1e-12)
+        folded += 1
+    assert folded > 40, folded
