@@ -83,6 +83,7 @@ struct Params {
     int bres, b_off;     // Toeplitz tiles of all groups resident (at byte b_off), or in each stage
     int tmem_cols;
     int shfl_epi;        // epilogue by warp shuffles (unit middle stride, (G - 1) d1 < 32)
+    int row_epi;         // one kernel row per group and unit middle stride: TMEM row m is output row m
     uint32_t idesc;
     float *y;
     int64_t ys0, ys1;
@@ -369,8 +370,9 @@ __device__ __forceinline__ float *out_of(const Params &P, int64_t inst) { return
 // tile the kernel-row groups are work items.  Warp 8 (one lane) streams the
 // items' stages through the TMA ring, warp 9 (one lane) issues the MMAs of
 // item j into TMEM buffer j % 2, warps 0-7 drain buffer j % 2 (the shifted
-// sums: warp shuffles, or a row block in shared memory) while the MMAs of
-// item j + 1 run in the other buffer.
+// sums: warp shuffles, or a row block in shared memory; none with one kernel
+// row per group at unit middle stride) while the MMAs of item j + 1 run in
+// the other buffer.
 template <int BN>
 __global__ void __launch_bounds__(kThreads, 1)
     conv_kernel(const __grid_constant__ CUtensorMap tX_hi, const __grid_constant__ CUtensorMap tX_lo,
@@ -598,7 +600,18 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t tb = tmem + lane_base + (uint32_t)(buf * P.tmem_cols);
-                if (P.shfl_epi) {
+                if (P.row_epi) {
+                    // no shifted sum: each group takes alternate 16-column
+                    // blocks of its lanes' rows (no exchange, no barrier)
+#pragma unroll
+                    for (int bc = 0; bc < BN / 16; bc++) {
+                        if ((bc & 1) != eg) continue;
+                        float v[16];
+                        tmem_ld16(tb + (uint32_t)(bc * 16), v);
+#pragma unroll
+                        for (int q = 0; q < 16; q++) acc[bc * 16 + q] += v[q];
+                    }
+                } else if (P.shfl_epi) {
                     // unit middle stride, row shifts kl d1 < 32: lane l takes the
                     // value of lane (l + kl d1) mod 32 of its own warp -- its own
                     // output's term when l + kl d1 < 32, else a term of output
@@ -712,10 +725,28 @@ __global__ void __launch_bounds__(kThreads, 1)
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&tempty[buf]);
             }
-            if (!stop && !eg && et < P.mvalid && c.oy0 + et < P.out1) {
+            if (!stop && (!eg || P.row_epi) && et < P.mvalid && c.oy0 + et < P.out1) {
                 const int64_t xl = c.oy0 + et == P.out1 - 1 ? P.xlast : P.out2;  // columns of this row
                 float *yr = out_of(P, c.inst) + c.oz * P.ys0 + (c.oy0 + et) * P.ys1 + c.ox0;
-                if (c.ox0 + BN <= xl && (reinterpret_cast<uintptr_t>(yr) & 15) == 0) {
+                if (P.row_epi) {
+                    // each group stores the 16-column blocks it summed
+#pragma unroll
+                    for (int bc = 0; bc < BN / 16; bc++) {
+                        if ((bc & 1) != eg) continue;
+                        float *yb = yr + bc * 16;
+                        if (c.ox0 + bc * 16 + 16 <= xl && (reinterpret_cast<uintptr_t>(yb) & 15) == 0) {
+#pragma unroll
+                            for (int q = 0; q < 4; q++)
+                                reinterpret_cast<float4 *>(yb)[q] =
+                                    make_float4(acc[bc * 16 + 4 * q], acc[bc * 16 + 4 * q + 1],
+                                                acc[bc * 16 + 4 * q + 2], acc[bc * 16 + 4 * q + 3]);
+                        } else {
+#pragma unroll
+                            for (int q = 0; q < 16; q++)
+                                if (c.ox0 + bc * 16 + q < xl) yb[q] = acc[bc * 16 + q];
+                        }
+                    }
+                } else if (c.ox0 + BN <= xl && (reinterpret_cast<uintptr_t>(yr) & 15) == 0) {
 #pragma unroll
                     for (int q = 0; q < BN / 4; q++)
                         reinterpret_cast<float4 *>(yr)[q] =
@@ -1018,7 +1049,8 @@ int run_bf16x3(const ndconv_problem *p, int64_t n, const float *x, const float *
     Q.ring_bytes = T.ring_bytes;
     Q.bres = T.bres;
     Q.b_off = T.b_off;
-    Q.shfl_epi = (A[1].s == 1 && (T.G - 1) * A[1].d < 32) ? 1 : 0;
+    Q.row_epi = (T.G == 1 && A[1].s == 1) ? 1 : 0;
+    Q.shfl_epi = (!Q.row_epi && A[1].s == 1 && (T.G - 1) * A[1].d < 32) ? 1 : 0;
     Q.tmem_cols = T.N <= 32 ? 32 : T.N <= 64 ? 64 : T.N <= 128 ? 128 : 256;
     Q.idesc = idesc_bf16(BM, T.N);
     Q.y = y;

@@ -37,6 +37,10 @@ def _lib():
     ((260, 180), (9, 7), [30, 1], ConvMode.Same, PaddingMode.Replicate),
     ((4, 260, 90), (3, 33, 5), [2, 1, 3], ConvMode.Custom([2, 5, 1], [1, 3, 2]), PaddingMode.Zeros),
     ((1, 4000), (1, 127), 1, ConvMode.Valid, PaddingMode.Zeros),
+    # one kernel row per group (row dilation 70) in several groups, and a
+    # kernel of one row: the epilogue reads TMEM rows as output rows
+    ((300, 120), (3, 7), [70, 1], ConvMode.Same, PaddingMode.Reflect),
+    ((200, 333), (1, 45), 1, ConvMode.Full, PaddingMode.Replicate),
 ])
 def test_bf16x3_vs_oracle(shape, kshape, dil, mode, pm):
     rng = np.random.default_rng(sum(shape) + sum(kshape))
