@@ -579,7 +579,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         // epilogue: two groups of four warps (eg = warp / 4); warp w reads
         // TMEM lanes 32 (w % 4) .. +31 (tile rows).  Output row y of the tile
         // sums the kernel rows kl of the item at rows y s1 + kl d1; group eg
-        // takes the rows kl = eg, eg + 2, ... and group 0 combines.
+        // takes the rows kl = eg, eg + 2, ... and group 0 combines and
+        // stores.  With one kernel row per group at unit middle stride
+        // (row_epi) there is nothing to combine: group eg sums and stores
+        // the 16-column blocks eg, eg + 2, ... of its rows.
         const int eg = warp >> 2, et = tid & 127, ew = warp & 3;
         const uint32_t lane_base = (uint32_t)(ew * 32) << 16;
         float *X0 = R, *X1 = R + BM * RP, *X2 = R + 2 * BM * RP;  // exchange blocks
